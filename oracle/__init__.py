@@ -1,0 +1,265 @@
+"""ctypes bindings for the oracles (test infrastructure only).
+
+* ``port()`` -> the CPU restatement in ``oracle/pars_oracle.cpp`` (``liboracle.so``),
+  built on every machine by ``__graft_entry__.build()``.
+* ``reference()`` -> the reference's own hot-path sources compiled against
+  ``oracle/ref_shim`` (``oracle/_ref/libpars_ref.so``), available only where the
+  reference checkout exists (``oracle/build_ref.sh``); ``None`` elsewhere.
+
+Only tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use this
+module.  The product path never imports it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libpars_ref.so")
+
+_P = ctypes.c_void_p
+_LL = ctypes.c_longlong
+_I = ctypes.c_int
+_F = ctypes.c_float
+_D = ctypes.c_double
+
+PARTICLE_DTYPE = np.dtype([
+    ("position", np.float32, 4),
+    ("remaining_iterations", np.int32),
+    ("vector_field_index", np.int32),
+    ("original_rank", np.int32),
+    ("original_voxel", np.int32, 3),
+    ("padding", np.int32, 2),
+])
+assert PARTICLE_DTYPE.itemsize == 48
+
+COLOR_MODES = {"hsl_constant_s": 0, "hsl_constant_l": 1, "hsv_constant_s": 2, "hsv_constant_v": 3, "rgb": 4}
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class Curves:
+    """Batches of integral curves as numpy arrays: list of dicts with
+    vertices (n,4) f32, indices (m,) i32, colors (n,4) f32 (NaN = never written),
+    rank, round."""
+
+    def __init__(self, batches, steps=None):
+        self.batches = batches
+        self.steps = steps
+
+
+class _Lib:
+    def __init__(self, path, prefix):
+        self.lib = ctypes.CDLL(path)
+        self.prefix = prefix
+        L = self.lib
+        fn = lambda name: getattr(L, prefix + name)
+        for name in ("curves_batches",):
+            fn(name).restype = _LL
+            fn(name).argtypes = [_P]
+        for name in ("curves_vertex_count", "curves_index_count"):
+            fn(name).restype = _LL
+            fn(name).argtypes = [_P, _LL]
+        for name in ("curves_vertices", "curves_colors", "curves_indices"):
+            fn(name).restype = _P
+            fn(name).argtypes = [_P, _LL]
+        for name in ("curves_batch_rank", "curves_batch_round"):
+            fn(name).restype = _I
+            fn(name).argtypes = [_P, _LL]
+        fn("curves_free").restype = None
+        fn("curves_free").argtypes = [_P]
+        fn("field_sample").restype = None
+        fn("field_sample").argtypes = [_P] * 5 + [_P, _LL, _P, _P]
+        fn("seed_generate").restype = _LL
+        fn("seed_generate").argtypes = [_P, _P, _P, _I, _I, _P]
+        fn("partition").restype = None
+        fn("partition").argtypes = [_I, _I, _P, _P]
+        fn("trace_single").restype = _P
+        fn("trace_single").argtypes = [_P] * 5 + [_P, _LL, _I, _F, _I, _F]
+        fn("trace_multi").restype = _P
+        fn("trace_multi").argtypes = [_P, _P, _P, _I, _P, _P, _I, _F, _I, _F]
+        fn("index_generate").restype = _LL
+        fn("index_generate").argtypes = [_P, _LL, _P]
+        fn("color_generate").restype = None
+        fn("color_generate").argtypes = [_P, _LL, _P, _LL, _I, _F, _P]
+
+    def _f(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    # -- curves ---------------------------------------------------------------
+    def _collect(self, handle, with_steps=False):
+        out = []
+        nb = self._f("curves_batches")(handle)
+        for b in range(nb):
+            nv = self._f("curves_vertex_count")(handle, b)
+            ni = self._f("curves_index_count")(handle, b)
+            vp = self._f("curves_vertices")(handle, b)
+            cp = self._f("curves_colors")(handle, b)
+            ip = self._f("curves_indices")(handle, b)
+            v = np.ctypeslib.as_array(ctypes.cast(vp, ctypes.POINTER(_F)), (nv * 4,)).reshape(-1, 4).copy() if nv else np.zeros((0, 4), np.float32)
+            c = np.ctypeslib.as_array(ctypes.cast(cp, ctypes.POINTER(_F)), (nv * 4,)).reshape(-1, 4).copy() if (nv and cp) else None
+            i = np.ctypeslib.as_array(ctypes.cast(ip, ctypes.POINTER(_I)), (ni,)).copy() if ni else np.zeros(0, np.int32)
+            out.append({"vertices": v, "colors": c, "indices": i,
+                        "rank": self._f("curves_batch_rank")(handle, b),
+                        "round": self._f("curves_batch_round")(handle, b)})
+        steps = None
+        if with_steps:
+            steps = int(self.lib.orc_curves_steps(ctypes.c_void_p(handle)))
+        self._f("curves_free")(handle)
+        return Curves(out, steps)
+
+    # -- stages -----------------------------------------------------------------
+    def field_sample(self, field, positions):
+        positions = np.ascontiguousarray(positions, np.float32).reshape(-1, 4)
+        n = positions.shape[0]
+        inside = np.zeros(n, np.uint8)
+        vel = np.zeros((n, 3), np.float32)
+        self._f("field_sample")(*field.ctypes_args(), _ptr(positions), n, _ptr(inside), _ptr(vel))
+        return inside.astype(bool), vel
+
+    def seed_generate(self, offset, size, stride, iterations, rank=0):
+        o, s, st = (np.ascontiguousarray(a, np.float32) for a in (offset, size, stride))
+        n = self._f("seed_generate")(_ptr(o), _ptr(s), _ptr(st), iterations, rank, None)
+        out = np.zeros(n, PARTICLE_DTYPE)
+        self._f("seed_generate")(_ptr(o), _ptr(s), _ptr(st), iterations, rank, _ptr(out))
+        return out
+
+    def partition(self, ranks, rank, domain):
+        d = np.ascontiguousarray(domain, np.int32)
+        info = np.zeros(21, np.int32)
+        self._f("partition")(ranks, rank, _ptr(d), _ptr(info))
+        return {"grid": info[0:3].copy(), "block": info[3:6].copy(), "multi_rank": info[6:9].copy(),
+                "offset": info[9:12].copy(), "ghosted": info[12:15].copy(), "neighbors": info[15:21].copy()}
+
+    def trace_single(self, field, particles, integrator=2, step=0.01, color="rgb", parameter=0.5):
+        particles = np.ascontiguousarray(particles, PARTICLE_DTYPE)
+        cm = -1 if color is None else COLOR_MODES[color]
+        h = self._f("trace_single")(*field.ctypes_args(), _ptr(particles), len(particles), integrator, step, cm, parameter)
+        return self._collect(h, with_steps=(self.prefix == "orc_"))
+
+    def trace_multi(self, domain_field, ranks, seed_offsets, seeds, integrator=2, step=0.01, color="rgb", parameter=0.5):
+        seeds = np.ascontiguousarray(seeds, PARTICLE_DTYPE)
+        offs = np.ascontiguousarray(seed_offsets, np.int64)
+        dims = np.ascontiguousarray(domain_field.dims, np.int32)
+        sp = np.ascontiguousarray(domain_field.spacing, np.float32)
+        cm = -1 if color is None else COLOR_MODES[color]
+        h = self._f("trace_multi")(_ptr(domain_field.xyz), _ptr(dims), _ptr(sp), ranks, _ptr(offs), _ptr(seeds),
+                                   integrator, step, cm, parameter)
+        return self._collect(h, with_steps=(self.prefix == "orc_"))
+
+    def index_generate(self, vertices):
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 4)
+        out = np.zeros(max(len(v), 1), np.int32)
+        n = self._f("index_generate")(_ptr(v), len(v), _ptr(out))
+        return out[:n].copy()
+
+    def color_generate(self, vertices, indices, mode="rgb", parameter=0.5):
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 4)
+        i = np.ascontiguousarray(indices, np.int32)
+        out = np.zeros_like(v)
+        self._f("color_generate")(_ptr(v), len(v), _ptr(i), len(i), COLOR_MODES[mode], parameter, _ptr(out))
+        return out
+
+
+class Port(_Lib):
+    """The CPU restatement (liboracle.so)."""
+
+    def __init__(self, path=PORT_PATH):
+        super().__init__(path, "orc_")
+        L = self.lib
+        L.orc_curves_steps.restype = _LL
+        L.orc_curves_steps.argtypes = [_P]
+        L.orc_max_threads.restype = _I
+        L.orc_set_threads.argtypes = [_I]
+        L.orc_flow_map.restype = _LL
+        L.orc_flow_map.argtypes = [_P] * 5 + [_I, _F, _I, _F, _LL, _LL, _P]
+        L.orc_advect_fp64.restype = None
+        L.orc_advect_fp64.argtypes = [_P] * 5 + [_P, _LL, _I, _I, _D, _LL, _P, _P, _P]
+        L.orc_ftle_fp64.restype = None
+        L.orc_ftle_fp64.argtypes = [_P, _P, _P, _D, _P]
+        L.orc_largest_eigenvalue.restype = None
+        L.orc_largest_eigenvalue.argtypes = [_P, _LL, _P]
+
+    def max_threads(self):
+        return self.lib.orc_max_threads()
+
+    def set_threads(self, n):
+        self.lib.orc_set_threads(n)
+
+    def flow_map(self, field, iterations, scale=1.0, integrator=2, step=0.01, first=0, count=None):
+        """Frozen-velocity FP32 flow map (reference semantics).  Returns
+        (flow [X',Y',Z',3] f32 with NaN where no particle landed, steps)."""
+        fm = [int(np.float32(d) * np.float32(scale)) for d in field.dims]
+        flow = np.full(fm + [3], np.nan, np.float32)
+        total = int(np.prod(fm))
+        if count is None:
+            count = total - first
+        steps = self.lib.orc_flow_map(*field.ctypes_args(), iterations, scale, integrator, step, first, count, _ptr(flow))
+        return flow, steps
+
+    def advect_fp64(self, field, start, max_steps, integrator=2, mode=1, step=0.01, keep_vertices=False):
+        start = np.ascontiguousarray(start, np.float64).reshape(-1, 3)
+        n = len(start)
+        end = np.zeros_like(start)
+        steps = np.zeros(n, np.int64)
+        verts = np.full((n, max_steps + 1, 3), np.nan) if keep_vertices else None
+        self.lib.orc_advect_fp64(*field.ctypes_args(), _ptr(start), n, integrator, mode, step, max_steps,
+                                 _ptr(end), _ptr(steps), _ptr(verts))
+        return end, steps, verts
+
+    def ftle_fp64(self, flow, spacing, time):
+        flow = np.ascontiguousarray(flow, np.float32)
+        dims = np.array(flow.shape[:3], np.int32)
+        sp = np.ascontiguousarray(spacing, np.float32)
+        out = np.zeros(flow.shape[:3], np.float64)
+        self.lib.orc_ftle_fp64(_ptr(flow), _ptr(dims), _ptr(sp), time, _ptr(out))
+        return out
+
+    def largest_eigenvalue(self, matrices):
+        m = np.ascontiguousarray(matrices, np.float64).reshape(-1, 9)
+        out = np.zeros(len(m))
+        self.lib.orc_largest_eigenvalue(_ptr(m), len(m), _ptr(out))
+        return out
+
+
+class Reference(_Lib):
+    """The reference's own sources built against oracle/ref_shim (libpars_ref.so)."""
+
+    def __init__(self, path=REF_PATH):
+        super().__init__(path, "ref_")
+        L = self.lib
+        L.ref_flow_map.restype = _LL
+        L.ref_flow_map.argtypes = [_P] * 5 + [_I, _F, _I, _F, _P, _P]
+        L.ref_ftle.restype = None
+        L.ref_ftle.argtypes = [_P] * 5 + [_F, _I, _P]
+
+    def flow_map(self, field, iterations, scale=1.0, integrator=2, step=0.01):
+        dims = np.zeros(3, np.int32)
+        n = self.lib.ref_flow_map(*field.ctypes_args(), iterations, scale, integrator, step, None, _ptr(dims))
+        flow = np.zeros(list(dims) + [3], np.float32)
+        self.lib.ref_flow_map(*field.ctypes_args(), iterations, scale, integrator, step, _ptr(flow), _ptr(dims))
+        return flow
+
+
+_port = None
+_ref = None
+
+
+def port():
+    global _port
+    if _port is None:
+        if not os.path.exists(PORT_PATH):
+            raise RuntimeError("oracle/liboracle.so is not built; run __graft_entry__.build()")
+        _port = Port()
+    return _port
+
+
+def reference():
+    """The reference build, or None where the reference sources were not available."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        _ref = Reference()
+    return _ref

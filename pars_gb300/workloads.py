@@ -1,0 +1,99 @@
+"""Seeded synthetic inputs with the shapes of the five tracing workloads.
+
+The reference's benchmarks ran on a private dataset; these fields stand in for
+it.  A field follows ``pa::vector_field`` (pa/include/pa/math/vector_field.hpp:
+14-24): ``xyz`` is ``[X][Y][Z][3]`` FP32 in C order (z fastest), ``offset``,
+``size`` and ``spacing`` are FP32 3-vectors, and ``size = shape * spacing`` as
+data_io.cpp:113 sets it (it counts one cell more than can be interpolated).
+"""
+import ctypes
+
+import numpy as np
+
+ABC_A = np.sqrt(3.0)
+ABC_B = np.sqrt(2.0)
+ABC_C = 1.0
+
+
+class Field:
+    """A steady vector field on a regular grid (host copy)."""
+
+    def __init__(self, xyz, offset, spacing, size=None):
+        self.xyz = np.ascontiguousarray(xyz, np.float32)
+        assert self.xyz.ndim == 4 and self.xyz.shape[3] == 3
+        self.dims = np.array(self.xyz.shape[:3], np.int32)
+        self.offset = np.ascontiguousarray(offset, np.float32)
+        self.spacing = np.ascontiguousarray(spacing, np.float32)
+        if size is None:
+            size = (self.dims.astype(np.float32) * self.spacing).astype(np.float32)
+        self.size = np.ascontiguousarray(size, np.float32)
+
+    def ctypes_args(self):
+        return (self.xyz.ctypes.data, self.dims.ctypes.data, self.offset.ctypes.data,
+                self.size.ctypes.data, self.spacing.ctypes.data)
+
+    @property
+    def nbytes(self):
+        return self.xyz.nbytes
+
+
+def abc_velocity(x, y, z, A=ABC_A, B=ABC_B, C=ABC_C):
+    """Arnold-Beltrami-Childress flow (u, v, w) in FP64."""
+    return (A * np.sin(z) + C * np.cos(y),
+            B * np.sin(x) + A * np.cos(z),
+            C * np.sin(y) + B * np.cos(x))
+
+
+def abc_field(n, noise_sigma=0.0, seed=None, A=ABC_A, B=ABC_B, C=ABC_C):
+    """ABC flow sampled at the n^3 vertices of [0, 2pi]^3 (spacing 2pi/(n-1),
+    offset 0), optionally plus N(0, noise_sigma) per component from
+    numpy's PCG64 generator with the given seed.  Built slab by slab to keep
+    the FP64 temporaries small at 256^3 and above."""
+    h = 2.0 * np.pi / (n - 1)
+    coords = np.arange(n) * h
+    xyz = np.empty((n, n, n, 3), np.float32)
+    Y, Z = np.meshgrid(coords, coords, indexing="ij")
+    rng = np.random.default_rng(seed) if noise_sigma else None
+    for i in range(n):
+        u, v, w = abc_velocity(coords[i], Y, Z, A, B, C)
+        slab = np.stack([np.broadcast_to(u, Y.shape), v, np.broadcast_to(w, Y.shape)], -1)
+        if rng is not None:
+            slab = slab + rng.standard_normal(slab.shape) * noise_sigma
+        xyz[i] = slab
+    spacing = np.full(3, np.float32(h), np.float32)
+    return Field(xyz, np.zeros(3, np.float32), spacing)
+
+
+def linear_field(n, matrix, spacing=0.1, offset=(0.0, 0.0, 0.0)):
+    """v(x) = M (x - centre) sampled on an n^3 grid; trilinear interpolation
+    reproduces it exactly (up to FP32 rounding of the samples)."""
+    h = np.float32(spacing)
+    coords = np.arange(n, dtype=np.float64) * float(h)
+    X, Y, Z = np.meshgrid(coords, coords, coords, indexing="ij")
+    c = float(h) * (n - 1) / 2.0
+    P = np.stack([X - c, Y - c, Z - c], -1)
+    xyz = (P @ np.asarray(matrix, np.float64).T).astype(np.float32)
+    return Field(xyz, np.asarray(offset, np.float32) + 0, np.full(3, h, np.float32))
+
+
+def uniform_field(n, velocity, spacing=0.25):
+    xyz = np.empty((n, n, n, 3), np.float32)
+    xyz[...] = np.asarray(velocity, np.float32)
+    return Field(xyz, np.zeros(3, np.float32), np.full(3, np.float32(spacing), np.float32))
+
+
+def streamline_config():
+    """The plain streamline workload: 64^3 ABC, seeds on a stride-4 lattice
+    (16^3), RK4 h = 0.01, 1000 steps (remaining_iterations = 1002: seed, at most
+    1000 steps, termination vertex; particle_tracer.cpp:266-278)."""
+    field = abc_field(64)
+    stride = (field.spacing * np.float32(4)).astype(np.float32)
+    return {"field": field, "stride": stride, "iterations": 1002, "step": 0.01}
+
+
+def ftle_config(n=256, noise_sigma=0.01, seed=0):
+    """The FTLE workload: n^3 ABC + N(0, 0.01) noise (seed 0), one seed per
+    vertex, RK4 h = 0.01 integrated to T = 5 (iterations = 501: at most 500
+    steps; particle_advector.cpp:74,132)."""
+    field = abc_field(n, noise_sigma=noise_sigma, seed=seed)
+    return {"field": field, "iterations": 501, "step": 0.01, "time": 5.0}
