@@ -1,0 +1,308 @@
+#!/usr/bin/env python
+"""Benchmark of the particle-tracing hot path on GB300.
+
+Workload (one "step"): the FTLE pipeline on a 256^3 FP32 ABC flow plus
+N(0, 0.01) noise (seed 0): one seed per grid vertex (16,777,216 particles),
+classical RK4 with four field samples per step, h = 0.01, at most 500 steps
+(T = 5), flow map, then the fused gradient / Cauchy-Green / FP64 eigenvalue /
+log FTLE kernel.  Metric: RK4 particle-steps per second (steps actually
+taken), with FTLE voxels per second beside it.
+
+value : device-resident input, timed with CUDA events on the library's stream.
+e2e   : the same through the C ABI from pinned HOST buffers: field upload
+        (host -> device), flow map, FTLE, FTLE download (device -> host).
+--impl reference : the reference's CPU algorithm (the oracle port of it,
+        frozen-velocity RK4 as the reference computes it) on the host cores,
+        on a bounded sample of the same workload.
+
+Multi-GPU: independent replicas (one process per GPU under torchrun), weak
+scaling; value = all ranks' steps / max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RK4 particle-steps/s"
+UNIT = "particle-steps/s"
+BYTES_PER_RK4_STEP = 512          # 4 samples x 8 corners x 16 B (flow-map mode: no vertex store)
+BYTES_PER_FTLE_VOXEL = 100        # 6 neighbour float4 reads + one FP32 write
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--size", type=int, default=256)
+    p.add_argument("--iterations", type=int, default=501)
+    p.add_argument("--cpu-sample", type=int, default=1048576, help="seeds in the CPU baseline's bounded sample")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic(steps_per_launch):
+    """DRAM bytes per launch of the flow-map kernel from the committed ncu
+    summary (bytes per particle-step measured there, scaled to this launch)."""
+    path = os.path.join(ROOT, "profiles", "advect_flow_map_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_particle_step:"):
+            return float(line.split(":")[1]) * steps_per_launch
+    return None
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        visible = os.environ.get("CUDA_VISIBLE_DEVICES")
+        self.index = visible.split(",")[device] if visible else str(device)
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", self.index], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cpu_reference_run(field, iterations, sample, steps, warmup):
+    """The reference's algorithm on the host cores: the oracle port's flow map
+    (frozen-velocity RK4, FP32, the reference's operation order), all threads."""
+    import oracle
+    port = oracle.port()
+    threads = port.max_threads()
+    for _ in range(warmup):
+        port.flow_map(field, iterations, 1.0, 2, 0.01, 0, sample)
+    total, t0 = 0, time.perf_counter()
+    for _ in range(steps):
+        _, s = port.flow_map(field, iterations, 1.0, 2, 0.01, 0, sample)
+        total += s
+    dt = time.perf_counter() - t0
+    return total / dt, threads, dt
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    from pars_gb300 import workloads
+
+    n = args.size
+    seeds = n ** 3
+    max_steps = args.iterations - 1
+    config = {"workload": f"ftle_{n}: ABC + N(0,0.01) noise (seed 0) on {n}^3 FP32 vertices of [0,2pi]^3, one seed per vertex "
+                          f"({seeds} particles), classical RK4 (4 samples/step) h=0.01, <= {max_steps} steps (T=5), "
+                          "flow map + fused central-difference / Cauchy-Green / FP64 eigenvalue / log FTLE",
+              "grid": n, "seeds": seeds, "max_steps": max_steps, "step_size": 0.01, "stage_mode": "resampled",
+              "ranks": world, "l2": "inputs larger than L2 (268 MB float4 field) and a 256 MB L2 flush before every step"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        field = workloads.abc_field(n, noise_sigma=0.01, seed=0)
+        value, threads, dt = cpu_reference_run(field, args.iterations, args.cpu_sample, args.steps, args.warmup)
+        sample = (f"first {args.cpu_sample} of {seeds} seeds (C order) of the {n}^3 FTLE workload per step, frozen-velocity "
+                  "RK4 (one sample per step) as the reference computes it, FP32, all host threads")
+        print(json.dumps({"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                          "data": "synthetic", "config": config,
+                          "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+                          "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+
+    import torch
+    from pars_gb300 import native
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    field = workloads.abc_field(n, noise_sigma=0.01, seed=0)
+    ctx = native.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    handle = ctx.upload_field(field)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    T = 0.01 * max_steps
+
+    def device_step(stage_mode=native.STAGES_RESAMPLED):
+        fm, steps = ctx.flow_map_generate(handle, args.iterations, 1.0, native.RUNGE_KUTTA_4, stage_mode, 0.01)
+        ctx.ftle_generate(fm, T, native.FTLE_REGULAR, download=False)
+        ctx.release_field(fm)
+        return steps
+
+    for _ in range(max(args.warmup, 3)):
+        device_step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    ctx.profile_reset()
+    ctx.profile_enable(True)
+    launches0 = ctx.launch_count()
+    sampler.start()
+    time.sleep(0.3)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    total_steps = 0
+    start.record(stream)
+    for _ in range(args.steps):
+        flush.zero_()
+        total_steps += device_step()
+    stop.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    launches = ctx.launch_count() - launches0
+    ctx.profile_enable(False)
+    elapsed_ms = start.elapsed_time(stop)
+    advect_ms, advect_n = ctx.profile_get("advect_flow_map")
+    ftle_ms, ftle_n = ctx.profile_get("ftle_fused")
+
+    if dist:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+        s = torch.tensor([float(total_steps)], device="cuda", dtype=torch.float64)
+        dist.all_reduce(s)
+        total_steps_all = float(s.item())
+    else:
+        total_steps_all = float(total_steps)
+
+    value = total_steps_all / (elapsed_ms * 1e-3)
+    ftle_voxels_per_s = world * seeds * args.steps / (elapsed_ms * 1e-3)
+    steps_per_launch = total_steps / args.steps
+    peak, peak_kind = measured_peaks()
+    advect_avg_s = advect_ms / max(advect_n, 1) * 1e-3
+    achieved = steps_per_launch * BYTES_PER_RK4_STEP / advect_avg_s / 1e9
+    ftle_avg_s = ftle_ms / max(ftle_n, 1) * 1e-3
+
+    # The reference's scheme (frozen velocity, one sample per step) on the GPU.
+    device_step(native.STAGES_FROZEN)
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    frozen_steps = 0
+    f0.record(stream)
+    for _ in range(2):
+        flush.zero_()
+        frozen_steps += device_step(native.STAGES_FROZEN)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    frozen_value = frozen_steps / (f0.elapsed_time(f1) * 1e-3)
+
+    # End to end through the C ABI from pinned host buffers.
+    pinned = torch.empty((n, n, n, 3), dtype=torch.float32, pin_memory=True).numpy()
+    pinned[...] = field.xyz
+    host_field = workloads.Field(pinned, field.offset, field.spacing, field.size)
+    ftle_out = torch.empty((n, n, n), dtype=torch.float32, pin_memory=True).numpy()
+
+    def e2e_step():
+        h = ctx.upload_field(host_field)
+        fm, steps = ctx.flow_map_generate(h, args.iterations, 1.0, native.RUNGE_KUTTA_4, native.STAGES_RESAMPLED, 0.01)
+        ctx.ftle_generate(fm, T, native.FTLE_REGULAR, out=ftle_out)
+        ctx.release_field(fm)
+        ctx.release_field(h)
+        return steps
+
+    e2e_step()
+    torch.cuda.synchronize()
+    e2e_steps, t0 = 0, time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        e2e_steps += e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * e2e_steps / e2e_s
+
+    cpu = None
+    if rank == 0 and world == 1:
+        cpu_value, threads, _ = cpu_reference_run(field, args.iterations, args.cpu_sample, 1, 0)
+        cpu = {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"first {args.cpu_sample} of {seeds} seeds (C order) of this workload, frozen-velocity RK4 "
+                         "(one sample per step) as the reference computes it, FP32, all host threads"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+                "ftle_voxels_per_s": ftle_voxels_per_s,
+                "frozen_velocity_steps_per_s": frozen_value,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                             "traffic": committed_traffic(steps_per_launch), "kernel": "advect_flow_map",
+                             "bytes_per_unit": BYTES_PER_RK4_STEP, "units_per_launch": steps_per_launch,
+                             "avg_launch_ms": advect_avg_s * 1e3, "peak_source": peak_kind,
+                             "ftle_kernel": {"avg_launch_ms": ftle_avg_s * 1e3,
+                                             "achieved_gbs": seeds * BYTES_PER_FTLE_VOXEL / ftle_avg_s / 1e9}},
+                "cpu_baseline": cpu,
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(field.xyz.nbytes),
+                        "d2h_bytes_per_step": int(ftle_out.nbytes)},
+                "clocks": clocks, "gpu_launches": launches}
+        print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

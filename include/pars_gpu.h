@@ -1,0 +1,249 @@
+/*
+ * pars_gpu.h — C ABI of the GB300 (sm_103a) particle-tracing library
+ * (libpars_gpu.so).
+ *
+ * The library replaces the CPU/TBB stages of the pars hot path behind plain C
+ * calls: plain pointers and sizes, int32 status codes, no exceptions and no C++
+ * or torch types.  Every function returns PARS_OK (0) or a negative status;
+ * pars_gpu_last_error() gives the message of the last failure on a context.
+ *
+ * Units and conventions are the reference's: positions are pa::vector4
+ * (x, y, z, w) FP32, fields are pa::vector_field (offset, size, spacing, data
+ * [X][Y][Z] of xyz FP32 in C order), curves are the integral_curves buffers of
+ * pa/include/pa/math/integral_curves.hpp:11-20 (vector4 vertices with the
+ * termination vertex (-2,-2,-2,0) ending each curve, vector4 colours, int32
+ * line indices), split into batches exactly as particle_tracer::
+ * compute_round_info does (particle_tracer.cpp:210-234).
+ *
+ * Threading: calls on one context are serialised by the context; separate
+ * contexts are independent.  Work is issued on the context's CUDA stream
+ * (its own, or one set with pars_gpu_set_stream).
+ */
+#ifndef PARS_GPU_H
+#define PARS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PARS_GPU_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------- */
+enum pars_gpu_status
+{
+  PARS_OK                    =  0,
+  PARS_ERR_INVALID_ARGUMENT  = -1,
+  PARS_ERR_CUDA              = -2,
+  PARS_ERR_OUT_OF_MEMORY     = -3,
+  PARS_ERR_UNSUPPORTED       = -4,
+  PARS_ERR_NOT_FOUND         = -5,
+  PARS_ERR_BUDGET            = -6,
+  PARS_ERR_CANCELLED         = -7,
+  PARS_ERR_TIMEOUT           = -8,
+  PARS_ERR_STATE             = -9
+};
+
+/* ---- enumerations ---------------------------------------------------------- */
+/* Order of pa::variant_integrator (pa/include/pa/math/integrators.hpp:24-32). */
+enum pars_integrator
+{
+  PARS_EULER                         = 0,
+  PARS_MODIFIED_MIDPOINT             = 1,
+  PARS_RUNGE_KUTTA_4                 = 2,
+  PARS_RUNGE_KUTTA_CASH_KARP_54      = 3,
+  PARS_RUNGE_KUTTA_DORMAND_PRINCE_5  = 4,
+  PARS_RUNGE_KUTTA_FEHLBERG_78       = 5,
+  PARS_ADAMS_BASHFORTH_2             = 6,
+  PARS_ADAMS_BASHFORTH_MOULTON_2     = 7
+};
+
+/* How the integrator's stages see the field.
+ * FROZEN:    the reference's behaviour — the right-hand side returns the
+ *            velocity sampled once at the step start for every stage
+ *            (particle_tracer.cpp:315-318), with the reference's FP32 operation
+ *            order (bit-exact with the reference on equal inputs).
+ * RESAMPLED: each stage samples the field at its own stage point (classical
+ *            RK4: four samples per step).  Stage points outside the grid use
+ *            the nearest boundary cell with its weight clamped to 0 or 1. */
+enum pars_stage_mode
+{
+  PARS_STAGES_FROZEN    = 0,
+  PARS_STAGES_RESAMPLED = 1
+};
+
+/* Order of pa::color_generator::mode (pa/include/pa/stages/color_generator.hpp:13-20). */
+enum pars_color_mode
+{
+  PARS_COLOR_NONE           = -1,
+  PARS_COLOR_HSL_CONSTANT_S =  0,
+  PARS_COLOR_HSL_CONSTANT_L =  1,
+  PARS_COLOR_HSV_CONSTANT_S =  2,
+  PARS_COLOR_HSV_CONSTANT_V =  3,
+  PARS_COLOR_RGB            =  4
+};
+
+/* pa::ftle_map_generator::mode (pa/include/pa/stages/ftle_map_generator.hpp:15-19). */
+enum pars_ftle_mode
+{
+  PARS_FTLE_REGULAR               = 0,
+  PARS_FTLE_FRACTIONAL_ANISOTROPY = 1
+};
+
+/* ---- types ------------------------------------------------------------------ */
+/* Byte layout of pa::particle (pa/include/pa/math/particle.hpp:12-36): Eigen
+ * Vector4f position (16-byte aligned), remaining_iterations,
+ * vector_field_index (-1 = local block, 0..5 = neighbour face), original_rank,
+ * Eigen Vector3i original_voxel; 48 bytes with the tail padding. */
+typedef struct pars_particle
+{
+  float   position[4];
+  int32_t remaining_iterations;
+  int32_t vector_field_index;
+  int32_t original_rank;
+  int32_t original_voxel[3];
+  int32_t padding[2];
+} pars_particle;
+
+/* partitioner::set_domain_size / rank_info (pa/source/stages/partitioner.cpp:8-53). */
+typedef struct pars_partition_info
+{
+  int32_t grid_size[3];
+  int32_t block_size[3];
+  int32_t multi_rank[3];
+  int32_t offset[3];              /* voxel offset of the block */
+  int32_t ghosted_block_size[3];  /* +1 on the + side of interior faces */
+  int32_t neighbor_rank[6];       /* faces -x,+x,-y,+y,-z,+z; -1 where absent */
+} pars_partition_info;
+
+/* Summary of one tracing call. */
+typedef struct pars_gpu_trace_summary
+{
+  int64_t batches;        /* integral_curves batches produced */
+  int64_t vertices;       /* vertices over all batches (after prune) */
+  int64_t steps;          /* integrator steps taken (particle-steps) */
+  int32_t rounds;         /* tracing rounds (1 for a single block) */
+  int32_t padding;
+} pars_gpu_trace_summary;
+
+typedef struct pars_gpu_context pars_gpu_context;
+
+/* ---- context ------------------------------------------------------------------ */
+/* Creates a context on CUDA device `device` with its own non-blocking stream. */
+int32_t     pars_gpu_create       (pars_gpu_context** context, int32_t device);
+int32_t     pars_gpu_destroy      (pars_gpu_context*  context);
+const char* pars_gpu_last_error   (const pars_gpu_context* context);
+int32_t     pars_gpu_abi_version  (void);
+/* Issues all later work on `stream` (a cudaStream_t); NULL restores the
+ * context's own stream. */
+int32_t     pars_gpu_set_stream   (pars_gpu_context* context, void* stream);
+int32_t     pars_gpu_synchronize  (pars_gpu_context* context);
+/* Device bytes currently held by the context. */
+int32_t     pars_gpu_memory_in_use(pars_gpu_context* context, int64_t* bytes);
+
+/* ---- vector_field (pa/include/pa/math/vector_field.hpp:14-24) ----------------- */
+/* Uploads a field from HOST memory: xyz is [shape0][shape1][shape2][3] FP32
+ * (the layout data_io.cpp:99-106 fills).  The device copy is padded to float4.
+ * Every shape entry must be >= 2.  *field receives a handle. */
+int32_t pars_gpu_field_upload       (pars_gpu_context* context, const float* xyz, const int32_t shape[3],
+                                     const float offset[3], const float size[3], const float spacing[3], int32_t* field);
+/* Same, from DEVICE memory (xyz already resident, e.g. produced on the GPU). */
+int32_t pars_gpu_field_upload_device(pars_gpu_context* context, const float* device_xyz, const int32_t shape[3],
+                                     const float offset[3], const float size[3], const float spacing[3], int32_t* field);
+int32_t pars_gpu_field_release      (pars_gpu_context* context, int32_t field);
+/* Shape, offset, size and spacing of a resident field (any pointer may be NULL). */
+int32_t pars_gpu_field_info         (pars_gpu_context* context, int32_t field, int32_t shape[3], float offset[3],
+                                     float size[3], float spacing[3]);
+/* Copies a resident field (e.g. a flow map) to HOST xyz, [X][Y][Z][3] FP32. */
+int32_t pars_gpu_field_download     (pars_gpu_context* context, int32_t field, float* xyz);
+/* vector_field::contains + ::interpolate (vector_field.cpp:12-48) at n host
+ * positions (vector4); velocity is 0 where the position is outside. */
+int32_t pars_gpu_field_sample       (pars_gpu_context* context, int32_t field, const float* positions, int64_t n,
+                                     uint8_t* inside, float* velocity);
+
+/* ---- seed_generator::generate (pa/source/stages/seed_generator.cpp:9-21) ------- */
+/* Writes up to `capacity` particles to host `particles` (may be NULL to count). */
+int32_t pars_gpu_seed_generate(pars_gpu_context* context, const float offset[3], const float size[3], const float stride[3],
+                               int32_t iterations, int32_t rank, pars_particle* particles, int64_t capacity, int64_t* count);
+
+/* ---- partitioner (pa/source/stages/partitioner.cpp:8-53) ------------------------ */
+int32_t pars_gpu_partition(int32_t ranks, int32_t rank, const int32_t domain_size[3], pars_partition_info* info);
+
+/* ---- particle_tracer (pa/source/stages/particle_tracer.cpp:39-56, 210-337, 402-409)
+ * Traces host particles through one block (`field`, no neighbours: particles
+ * leaving it are dropped) and prunes, leaving the curves on the device.
+ * integrator: PARS_EULER or PARS_RUNGE_KUTTA_4 (others: PARS_ERR_UNSUPPORTED). */
+int32_t pars_gpu_trace(pars_gpu_context* context, int32_t field, const pars_particle* particles, int64_t count,
+                       int32_t integrator, int32_t stage_mode, float step_size, pars_gpu_trace_summary* summary);
+/* Same with the particles already in DEVICE memory. */
+int32_t pars_gpu_trace_device(pars_gpu_context* context, int32_t field, const pars_particle* device_particles, int64_t count,
+                              int32_t integrator, int32_t stage_mode, float step_size, pars_gpu_trace_summary* summary);
+
+/* Partitioned domain on one GPU: the domain field (HOST, [X][Y][Z][3]) is split
+ * into `ranks` blocks exactly as partitioner::set_domain_size does, each block
+ * resident with its + side ghost layer; offset = voxel offset * spacing,
+ * size = block_size * spacing (data_io.cpp:91-115).  *domain receives a handle. */
+int32_t pars_gpu_domain_create (pars_gpu_context* context, const float* xyz, const int32_t domain_size[3],
+                                const float spacing[3], int32_t ranks, int32_t* domain);
+int32_t pars_gpu_domain_release(pars_gpu_context* context, int32_t domain);
+/* Traces seeds over a partitioned domain: rank r's seeds are
+ * particles[seed_offsets[r] .. seed_offsets[r+1]).  Every round each block
+ * traces its particles; particles leaving a block move to the face neighbour
+ * through device queues (particle_tracer.cpp:280-309, 376-393), until none is
+ * left.  The next round's particles of a block are, in order of the sending
+ * block, the particles each sender handed over, in the sender's order. */
+int32_t pars_gpu_trace_domain(pars_gpu_context* context, int32_t domain, const pars_particle* particles,
+                              const int64_t* seed_offsets, int32_t integrator, int32_t stage_mode, float step_size,
+                              pars_gpu_trace_summary* summary);
+
+/* Curves of the last trace call, resident on the device.
+ * pars_gpu_curves_index: index_generator::generate on every batch.
+ * pars_gpu_curves_color: color_generator::generate on every batch (needs indices). */
+int32_t pars_gpu_curves_index     (pars_gpu_context* context);
+int32_t pars_gpu_curves_color     (pars_gpu_context* context, int32_t mode, float parameter);
+int32_t pars_gpu_curves_batch_info(pars_gpu_context* context, int64_t batch, int64_t* vertices, int64_t* indices,
+                                   int32_t* rank, int32_t* round);
+/* Copies one batch to HOST memory; any pointer may be NULL. */
+int32_t pars_gpu_curves_download  (pars_gpu_context* context, int64_t batch, float* vertices, float* colors, int32_t* indices);
+
+/* ---- index / colour stages on host buffers -------------------------------------- */
+/* index_generator::generate (index_generator.cpp:10-24) on one batch of n host
+ * vertices; indices needs room for n entries. */
+int32_t pars_gpu_index_generate(pars_gpu_context* context, const float* vertices, int64_t n, int32_t* indices, int64_t* index_count);
+/* color_generator::generate (color_generator.cpp:16-39); colours the reference
+ * leaves unwritten are left unchanged in `colors`. */
+int32_t pars_gpu_color_generate(pars_gpu_context* context, const float* vertices, int64_t n, const int32_t* indices,
+                                int64_t index_count, int32_t mode, float parameter, float* colors);
+
+/* ---- flow map + FTLE ---------------------------------------------------------- */
+/* flow_map_generator::generate (flow_map_generator.cpp:12-52) on one block:
+ * one particle per voxel of an int(shape * scale) grid with spacing
+ * spacing / scale, advected with particle_advector's rules
+ * (particle_advector.cpp:74-139; at most iterations - 1 steps).  The flow map
+ * becomes a new field handle (*flow_map) resident on the device. */
+int32_t pars_gpu_flow_map_generate(pars_gpu_context* context, int32_t field, int32_t iterations, float resolution_scale,
+                                   int32_t integrator, int32_t stage_mode, float step_size, int32_t* flow_map, int64_t* steps);
+/* FTLE of a flow-map field: central-difference gradient (one-sided at the
+ * borders), Cauchy-Green tensor, largest eigenvalue in FP64 closed form,
+ * log(sqrt(lambda)) / |time| (mode REGULAR) or fractional anisotropy.  Writes
+ * the FP32 field to HOST `ftle` (X*Y*Z floats) unless it is NULL, in which case
+ * the result stays on the device (pars_gpu_ftle_device_pointer). */
+int32_t pars_gpu_ftle_generate    (pars_gpu_context* context, int32_t flow_map, float time, int32_t mode, float* ftle);
+int32_t pars_gpu_ftle_device_pointer(pars_gpu_context* context, const float** device_ftle, int64_t* count);
+
+/* ---- instrumentation ---------------------------------------------------------- */
+/* When enabled, each kernel launch is bracketed by CUDA events on the launch
+ * stream and its time is accumulated per kernel name. */
+int32_t pars_gpu_profile_enable(pars_gpu_context* context, int32_t enable);
+int32_t pars_gpu_profile_reset (pars_gpu_context* context);
+/* Accumulated time and launches of the kernel called `name` (0 if never run). */
+int32_t pars_gpu_profile_get   (pars_gpu_context* context, const char* name, double* milliseconds, int64_t* launches);
+/* Kernel launches issued by this library on the context since creation. */
+int32_t pars_gpu_launch_count  (pars_gpu_context* context, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PARS_GPU_H */

@@ -182,6 +182,8 @@ class Port(_Lib):
         L.orc_ftle_fp64.argtypes = [_P, _P, _P, _D, _P]
         L.orc_largest_eigenvalue.restype = None
         L.orc_largest_eigenvalue.argtypes = [_P, _LL, _P]
+        L.orc_largest_eigenvalue_closed_form.restype = None
+        L.orc_largest_eigenvalue_closed_form.argtypes = [_P, _LL, _P]
 
     def max_threads(self):
         return self.lib.orc_max_threads()
@@ -218,10 +220,11 @@ class Port(_Lib):
         self.lib.orc_ftle_fp64(_ptr(flow), _ptr(dims), _ptr(sp), time, _ptr(out))
         return out
 
-    def largest_eigenvalue(self, matrices):
+    def largest_eigenvalue(self, matrices, closed_form=False):
         m = np.ascontiguousarray(matrices, np.float64).reshape(-1, 9)
         out = np.zeros(len(m))
-        self.lib.orc_largest_eigenvalue(_ptr(m), len(m), _ptr(out))
+        fn = self.lib.orc_largest_eigenvalue_closed_form if closed_form else self.lib.orc_largest_eigenvalue
+        fn(_ptr(m), len(m), _ptr(out))
         return out
 
 

@@ -522,8 +522,47 @@ inline void step_fp64(const field& f, int integrator, int mode, double h, const 
   for (int c = 0; c < 3; ++c) out[c] = x[c] + h / 6.0 * (k1[c] + 2.0 * k2[c] + 2.0 * k3[c] + k4[c]);
 }
 
+// Largest eigenvalue of a symmetric 3x3 matrix by cyclic Jacobi rotations
+// (each rotation zeroes one off-diagonal entry; sweeps repeat until the
+// off-diagonal part vanishes), accurate to a few ulps of the matrix norm even
+// for repeated eigenvalues.  The FTLE oracle uses this one.
+double largest_eigenvalue_jacobi(const double in[3][3])
+{
+  double a[3][3];
+  for (int r = 0; r < 3; ++r) for (int c = 0; c < 3; ++c) a[r][c] = 0.5 * (in[r][c] + in[c][r]);
+  for (int sweep = 0; sweep < 64; ++sweep)
+  {
+    const double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+    if (off == 0.0) break;
+    for (int p = 0; p < 2; ++p)
+      for (int q = p + 1; q < 3; ++q)
+      {
+        if (a[p][q] == 0.0) continue;
+        // rotation angle that zeroes a[p][q]: t = tan(theta), smaller root
+        const double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < 3; ++k)   // A <- A J (columns p, q)
+        {
+          const double akp = a[k][p], akq = a[k][q];
+          a[k][p] = c * akp - s * akq;
+          a[k][q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < 3; ++k)   // A <- J^T A (rows p, q)
+        {
+          const double apk = a[p][k], aqk = a[q][k];
+          a[p][k] = c * apk - s * aqk;
+          a[q][k] = s * apk + c * aqk;
+        }
+        a[p][q] = a[q][p] = 0.0;
+      }
+  }
+  return std::max(a[0][0], std::max(a[1][1], a[2][2]));
+}
+
 // Largest eigenvalue of a symmetric 3x3 matrix (trigonometric closed form,
 // O. K. Smith, "Eigenvalues of a symmetric 3x3 matrix", CACM 4(4), 1961).
+// Kept as a cross-check of the GPU's formula.
 double largest_eigenvalue(const double a[3][3])
 {
   const double p1 = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
@@ -864,13 +903,25 @@ void orc_ftle_fp64(const float* flow, const int dims[3], const float spacing[3],
         for (int r = 0; r < 3; ++r)
           for (int c = 0; c < 3; ++c)
             C[r][c] = J[0][r] * J[0][c] + J[1][r] * J[1][c] + J[2][r] * J[2][c];
-        const double lambda = largest_eigenvalue(C);
+        const double lambda = largest_eigenvalue_jacobi(C);
         out[(x * Y + y) * Z + z] = std::log(std::sqrt(lambda)) / std::fabs(time);
       }
 }
 
 // Largest eigenvalue of symmetric 3x3 matrices (row-major, 9 doubles each).
 void orc_largest_eigenvalue(const double* matrices, long long n, double* out)
+{
+  for (long long i = 0; i < n; ++i)
+  {
+    double a[3][3];
+    for (int r = 0; r < 3; ++r) for (int c = 0; c < 3; ++c) a[r][c] = matrices[9 * i + 3 * r + c];
+    out[i] = largest_eigenvalue_jacobi(a);
+  }
+}
+
+// The same with the trigonometric closed form (cross-check of the formula the
+// GPU's FTLE kernel evaluates).
+void orc_largest_eigenvalue_closed_form(const double* matrices, long long n, double* out)
 {
   for (long long i = 0; i < n; ++i)
   {

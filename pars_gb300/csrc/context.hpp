@@ -1,0 +1,243 @@
+// Host-side state of a pars_gpu context: device buffers, resident fields and
+// domains, the curves of the last trace, scratch, and launch instrumentation.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/pars_gpu.h"
+#include "device_math.cuh"
+
+namespace pars
+{
+// Error carrying a pars_gpu status; thrown inside the library and turned into
+// a status code at the C boundary (no exception crosses it).
+struct error : std::runtime_error
+{
+  int32_t status;
+  error(int32_t s, const std::string& message) : std::runtime_error(message), status(s) {}
+};
+
+#define PARS_CUDA(call)                                                                            \
+  do {                                                                                             \
+    cudaError_t pars_e_ = (call);                                                                  \
+    if (pars_e_ != cudaSuccess)                                                                    \
+      throw ::pars::error(pars_e_ == cudaErrorMemoryAllocation ? PARS_ERR_OUT_OF_MEMORY : PARS_ERR_CUDA, \
+                          std::string(#call) + ": " + cudaGetErrorString(pars_e_));                \
+  } while (0)
+
+#define PARS_REQUIRE(condition, message)                                                            \
+  do { if (!(condition)) throw ::pars::error(PARS_ERR_INVALID_ARGUMENT, message); } while (0)
+
+// Grow-only device allocation owned by the context.
+class device_buffer
+{
+public:
+  device_buffer() = default;
+  device_buffer(const device_buffer&) = delete;
+  device_buffer& operator=(const device_buffer&) = delete;
+  device_buffer(device_buffer&& o) noexcept : ptr_(o.ptr_), bytes_(o.bytes_) { o.ptr_ = nullptr; o.bytes_ = 0; }
+  device_buffer& operator=(device_buffer&& o) noexcept { release(); ptr_ = o.ptr_; bytes_ = o.bytes_; o.ptr_ = nullptr; o.bytes_ = 0; return *this; }
+  ~device_buffer() { release(); }
+
+  void reserve(std::size_t bytes)
+  {
+    if (bytes <= bytes_) return;
+    release();
+    if (bytes == 0) return;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess)
+    {
+      (void)cudaGetLastError();
+      throw error(PARS_ERR_OUT_OF_MEMORY, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
+    }
+    ptr_ = p;
+    bytes_ = bytes;
+  }
+  void release()
+  {
+    if (ptr_) cudaFree(ptr_);
+    ptr_ = nullptr;
+    bytes_ = 0;
+  }
+  template <typename T> T* as() const { return static_cast<T*>(ptr_); }
+  void*       get()   const { return ptr_; }
+  std::size_t bytes() const { return bytes_; }
+
+private:
+  void*       ptr_   = nullptr;
+  std::size_t bytes_ = 0;
+};
+
+struct field_entry
+{
+  device_buffer data;          // float4 [X][Y][Z]
+  int           shape[3];
+  float         offset[3], size[3], spacing[3];
+  field_view view() const
+  {
+    field_view v;
+    v.data = data.as<const float4>();
+    v.nx = shape[0]; v.ny = shape[1]; v.nz = shape[2];
+    v.ox = offset[0]; v.oy = offset[1]; v.oz = offset[2];
+    v.hx = spacing[0]; v.hy = spacing[1]; v.hz = spacing[2];
+    v.maxx = offset[0] + size[0]; v.maxy = offset[1] + size[1]; v.maxz = offset[2] + size[2];
+    return v;
+  }
+};
+
+// One block of a traced domain as the tracing kernel sees it.
+struct trace_block
+{
+  field_view field;
+  int        neighbor[6];   // block index per face, -1 where absent
+};
+
+struct domain_entry
+{
+  int                      ranks = 0;
+  pars_partition_info      first {};
+  std::vector<int>         fields;      // field handle per block
+  std::vector<trace_block> blocks;
+  device_buffer            device_blocks;
+};
+
+// A batch of integral curves resident on the device.
+struct curves_batch
+{
+  long long vertex_offset = 0;   // into curves.vertices / colors
+  long long vertex_count  = 0;
+  long long index_offset  = 0;   // into curves.indices (valid after indexing)
+  long long index_count   = 0;
+  int       rank = 0, round = 0;
+};
+
+struct curves_store
+{
+  device_buffer             vertices;   // float4
+  device_buffer             colors;     // float4
+  device_buffer             indices;    // int32
+  long long                 vertex_total = 0;
+  bool                      indexed = false;
+  bool                      colored = false;
+  std::vector<curves_batch> batches;
+};
+
+struct profile_entry
+{
+  double    milliseconds = 0.0;
+  long long launches     = 0;
+};
+
+struct timed_launch
+{
+  std::string name;
+  cudaEvent_t start, stop;
+};
+}
+
+struct pars_gpu_context
+{
+  int                                     device = 0;
+  cudaStream_t                            own_stream = nullptr;
+  cudaStream_t                            stream = nullptr;
+  std::mutex                              mutex;
+  std::string                             last_error;
+  int                                     next_handle = 1;
+  std::map<int, std::unique_ptr<pars::field_entry>>  fields;
+  std::map<int, std::unique_ptr<pars::domain_entry>> domains;
+  pars::curves_store                      curves;
+  // scratch
+  pars::device_buffer                     particles_in, particles_next, slots, kept, written, offsets, block_of,
+                                          block_of_next, exits, exit_keys, exit_keys_sorted, exit_order,
+                                          exit_order_sorted, counters, block_max, cub_temp, scan_input, tile_counts,
+                                          tile_offsets, staging, boundary_positions, boundary_offsets, single_block;
+  pars::device_buffer                     ftle;
+  long long                               ftle_count = 0;
+  // instrumentation
+  bool                                    profile = false;
+  std::map<std::string, pars::profile_entry> profile_totals;
+  std::vector<pars::timed_launch>         pending;
+  std::vector<cudaEvent_t>                event_pool;
+  long long                               launches = 0;
+  long long                               held_bytes() const;
+};
+
+namespace pars
+{
+// Brackets one kernel launch for the instrumentation: call begin() just before
+// and end() just after the launch (same stream).
+class launch_scope
+{
+public:
+  launch_scope(pars_gpu_context& ctx, const char* name);
+  ~launch_scope() noexcept(false);
+private:
+  pars_gpu_context& ctx_;
+  const char*       name_;
+  cudaEvent_t       start_ = nullptr;
+};
+
+// Kernel launchers (defined in the *_kernels.cu translation units).
+void launch_pack_field(pars_gpu_context& ctx, const float* xyz, float4* out, long long count);
+void launch_unpack_field(pars_gpu_context& ctx, const float4* data, float* xyz, long long count);
+void launch_field_sample(pars_gpu_context& ctx, const field_view& f, const float4* positions, long long n, uint8_t* inside, float* velocity);
+void launch_seed_generate(pars_gpu_context& ctx, const float offset[3], const float stride[3], const int per_dimension[3],
+                          int iterations, int rank, pars_particle* out);
+
+struct trace_launch
+{
+  const trace_block*   blocks;
+  const pars_particle* particles;
+  const int*           block_of;      // nullptr: every particle is in block 0
+  long long            count;
+  long long            slot_stride;
+  float4*              slots;
+  int*                 written;
+  int*                 kept;
+  step_rule            rule;
+  int                  route_exits;   // 0: particles leaving the block are dropped
+  pars_particle*       exit_particles;
+  unsigned long long*  exit_keys;     // (destination block << 40) | particle index
+  unsigned int*        exit_count;
+  unsigned long long*  steps;
+};
+void launch_trace(pars_gpu_context& ctx, const trace_launch& a);
+void launch_compact_vertices(pars_gpu_context& ctx, const float4* slots, long long slot_stride, const int* written,
+                             const long long* offsets, long long count, float4* out);
+// Exclusive sum of `count` int32 into int64 offsets; offsets[count] = total.
+void exclusive_sum(pars_gpu_context& ctx, const int* in, long long* out, long long count);
+// Stable sort of (key, value) pairs by the low `bits` bits of the key.
+void sort_pairs(pars_gpu_context& ctx, const unsigned long long* keys_in, unsigned long long* keys_out,
+                const unsigned int* values_in, unsigned int* values_out, long long count, int bits);
+// Gathers the sorted exit queue into the next round's particle list and
+// accumulates per-block maximum remaining_iterations and particle counts.
+void launch_gather_exits(pars_gpu_context& ctx, const pars_particle* exits, const unsigned int* order,
+                         const unsigned long long* keys, long long count, pars_particle* out, int* block_of,
+                         int* block_max, int* block_count);
+void launch_iota(pars_gpu_context& ctx, unsigned int* out, long long count);
+// out[k] = offsets[positions[k]] for k < n.
+void launch_gather_offsets(pars_gpu_context& ctx, const long long* offsets, const long long* positions, long long n, long long* out);
+// block_max[0] = max remaining_iterations over particles (block_of == nullptr).
+void launch_particle_stats(pars_gpu_context& ctx, const pars_particle* particles, const int* block_of, long long count, int* block_max);
+// Copies the ghosted block at voxel `offset` of a device [X][Y][Z][3] domain into float4 [shape].
+void launch_extract_block(pars_gpu_context& ctx, const float* domain_xyz, const int32_t domain[3], const int32_t offset[3],
+                          const int shape[3], float4* out);
+
+long long launch_index_generate(pars_gpu_context& ctx, const float4* vertices, long long n, int* indices);
+void launch_color_generate(pars_gpu_context& ctx, const float4* vertices, const int* indices, long long index_count,
+                           int mode, float parameter, float4* colors);
+
+void launch_flow_map(pars_gpu_context& ctx, const field_view& f, const step_rule& rule, int iterations,
+                     const float offset[3], const float fm_spacing[3], const int seeds_per_dimension[3],
+                     const int fm_shape[3], float4* flow, unsigned long long* steps);
+void launch_ftle(pars_gpu_context& ctx, const field_view& flow, double time, int mode, float* out);
+}

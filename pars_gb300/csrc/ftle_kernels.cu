@@ -1,0 +1,185 @@
+// Flow-map advection and the fused FTLE kernel.
+//
+// flow map: one thread per seed of flow_map_generator's lattice
+//   (flow_map_generator.cpp:23-43 + seed_generator.cpp:9-21, seeds generated in
+//   the kernel from the voxel index), advected with particle_advector's rules
+//   (particle_advector.cpp:74-139, one block: a particle stops with its current
+//   position when it leaves the grid, meets a zero velocity, or has taken
+//   iterations - 1 steps) and written to its voxel (flow_map_generator.cpp:44-52).
+// FTLE: per voxel, the flow map's central-difference gradient J (FP32, one-sided
+//   at the borders), the Cauchy-Green tensor C = J^T J and its largest
+//   eigenvalue in FP64 by the trigonometric closed form (O. K. Smith, CACM 4(4),
+//   1961), then log(sqrt(lambda)) / |T| in FP64, stored as FP32 — the intent of
+//   vector_field::gradient + ftle_map_generator::generate
+//   (vector_field.cpp:49-93, ftle_map_generator.cpp:22-60).
+#include "context.hpp"
+
+namespace pars
+{
+namespace
+{
+struct flow_map_args
+{
+  field_view f;
+  step_rule  rule;
+  int        iterations;
+  float      ox, oy, oz;          // seed lattice offset
+  float      sx, sy, sz;          // seed lattice spacing (field spacing / scale)
+  int        px, py, pz;          // seeds per dimension
+  int        fx, fy, fz;          // flow-map shape
+  float4*    flow;
+  unsigned long long* steps;
+};
+
+__global__ void __launch_bounds__(256) flow_map_kernel(const flow_map_args a)
+{
+  const long long total = (long long)a.px * a.py * a.pz;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned int steps = 0;
+  if (i < total)
+  {
+    const int iz = int(i % a.pz);
+    const int iy = int((i / a.pz) % a.py);
+    const int ix = int(i / ((long long)a.pz * a.py));
+    float4 pos = make_float4(__fadd_rn(a.ox, __fmul_rn(a.sx, float(ix))), __fadd_rn(a.oy, __fmul_rn(a.sy, float(iy))),
+                             __fadd_rn(a.oz, __fmul_rn(a.sz, float(iz))), 0.0f);
+    bool finished = false;
+    for (int it = 1; it < a.iterations; ++it)
+    {
+      float3 v;
+      if (!sample_inside(a.f, pos, v)) { finished = true; break; }
+      if (is_zero(v)) { finished = true; break; }
+      pos = take_step(a.f, a.rule, pos, v);
+      ++steps;
+      if (it + 1 == a.iterations) { finished = true; break; }
+    }
+    // With iterations <= 1 the reference never assigns the voxel; it keeps the
+    // seed position here.
+    (void)finished;
+    if (ix < a.fx && iy < a.fy && iz < a.fz)
+      a.flow[((long long)ix * a.fy + iy) * a.fz + iz] = pos;
+  }
+  const unsigned int warp_steps = __reduce_add_sync(0xffffffffu, steps);
+  if ((threadIdx.x & 31) == 0 && warp_steps) atomicAdd(a.steps, (unsigned long long)warp_steps);
+}
+
+// Eigenvalues of a symmetric 3x3 matrix in descending order (trigonometric form).
+__device__ void symmetric_eigenvalues(double a00, double a01, double a02, double a11, double a12, double a22, double out[3])
+{
+  const double p1 = a01 * a01 + a02 * a02 + a12 * a12;
+  if (p1 == 0.0)
+  {
+    double x = a00, y = a11, z = a22, t;
+    if (x < y) { t = x; x = y; y = t; }
+    if (y < z) { t = y; y = z; z = t; }
+    if (x < y) { t = x; x = y; y = t; }
+    out[0] = x; out[1] = y; out[2] = z;
+    return;
+  }
+  const double q  = (a00 + a11 + a22) / 3.0;
+  const double d0 = a00 - q, d1 = a11 - q, d2 = a22 - q;
+  const double p  = sqrt((d0 * d0 + d1 * d1 + d2 * d2 + 2.0 * p1) / 6.0);
+  const double inv = 1.0 / p;
+  const double b00 = d0 * inv, b11 = d1 * inv, b22 = d2 * inv, b01 = a01 * inv, b02 = a02 * inv, b12 = a12 * inv;
+  const double det = b00 * (b11 * b22 - b12 * b12) - b01 * (b01 * b22 - b12 * b02) + b02 * (b01 * b12 - b11 * b02);
+  double r = 0.5 * det;
+  r = r < -1.0 ? -1.0 : (r > 1.0 ? 1.0 : r);
+  const double phi = acos(r) / 3.0;
+  out[0] = q + 2.0 * p * cos(phi);
+  out[2] = q + 2.0 * p * cos(phi + 2.0943951023931954923);   // 2 pi / 3
+  out[1] = 3.0 * q - out[0] - out[2];
+}
+
+struct ftle_args
+{
+  const float4* flow;
+  int           nx, ny, nz;
+  float         hx, hy, hz;
+  double        inverse_time;     // 1 / |T|
+  int           mode;
+  float*        out;
+};
+
+__global__ void __launch_bounds__(256) ftle_kernel(const ftle_args a)
+{
+  const long long total = (long long)a.nx * a.ny * a.nz;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  const int z = int(i % a.nz);
+  const int y = int((i / a.nz) % a.ny);
+  const int x = int(i / ((long long)a.nz * a.ny));
+  const long long sy = a.nz, sx = (long long)a.ny * a.nz;
+
+  // Column j of J: (phi(+e_j) - phi(-e_j)) / (2 h_j), one-sided at borders.
+  float J[3][3];
+  const int   idx[3] = {x, y, z};
+  const int   ext[3] = {a.nx, a.ny, a.nz};
+  const float h[3]   = {a.hx, a.hy, a.hz};
+  const long long stride[3] = {sx, sy, 1};
+  #pragma unroll
+  for (int j = 0; j < 3; ++j)
+  {
+    if (ext[j] == 1) { J[0][j] = J[1][j] = J[2][j] = 0.0f; continue; }
+    long long lo = i, hi = i;
+    float denominator;
+    if (idx[j] == 0)                 { hi = i + stride[j]; denominator = h[j]; }
+    else if (idx[j] == ext[j] - 1)   { lo = i - stride[j]; denominator = h[j]; }
+    else                             { lo = i - stride[j]; hi = i + stride[j]; denominator = 2.0f * h[j]; }
+    const float4 A = __ldg(a.flow + lo), B = __ldg(a.flow + hi);
+    J[0][j] = __fdiv_rn(__fsub_rn(B.x, A.x), denominator);
+    J[1][j] = __fdiv_rn(__fsub_rn(B.y, A.y), denominator);
+    J[2][j] = __fdiv_rn(__fsub_rn(B.z, A.z), denominator);
+  }
+  // Cauchy-Green tensor in FP64.
+  double C[3][3];
+  #pragma unroll
+  for (int r = 0; r < 3; ++r)
+    #pragma unroll
+    for (int c = r; c < 3; ++c)
+      C[r][c] = double(J[0][r]) * double(J[0][c]) + double(J[1][r]) * double(J[1][c]) + double(J[2][r]) * double(J[2][c]);
+  double lambda[3];
+  symmetric_eigenvalues(C[0][0], C[0][1], C[0][2], C[1][1], C[1][2], C[2][2], lambda);
+  double value;
+  if (a.mode == PARS_FTLE_REGULAR)
+    value = log(sqrt(lambda[0])) * a.inverse_time;
+  else
+  {
+    const double d01 = lambda[0] - lambda[1], d12 = lambda[1] - lambda[2], d20 = lambda[2] - lambda[0];
+    value = sqrt(0.5) * sqrt(d01 * d01 + d12 * d12 + d20 * d20) /
+            sqrt(lambda[0] * lambda[0] + lambda[1] * lambda[1] + lambda[2] * lambda[2]);
+  }
+  a.out[i] = float(value);
+}
+}
+
+void launch_flow_map(pars_gpu_context& ctx, const field_view& f, const step_rule& rule, int iterations,
+                     const float offset[3], const float fm_spacing[3], const int seeds_per_dimension[3],
+                     const int fm_shape[3], float4* flow, unsigned long long* steps)
+{
+  flow_map_args a;
+  a.f = f; a.rule = rule; a.iterations = iterations;
+  a.ox = offset[0]; a.oy = offset[1]; a.oz = offset[2];
+  a.sx = fm_spacing[0]; a.sy = fm_spacing[1]; a.sz = fm_spacing[2];
+  a.px = seeds_per_dimension[0]; a.py = seeds_per_dimension[1]; a.pz = seeds_per_dimension[2];
+  a.fx = fm_shape[0]; a.fy = fm_shape[1]; a.fz = fm_shape[2];
+  a.flow = flow; a.steps = steps;
+  const long long total = (long long)a.px * a.py * a.pz;
+  if (total <= 0) return;
+  launch_scope scope(ctx, "advect_flow_map");
+  flow_map_kernel<<<(unsigned)((total + 127) / 128), 128, 0, ctx.stream>>>(a);
+}
+
+void launch_ftle(pars_gpu_context& ctx, const field_view& flow, double time, int mode, float* out)
+{
+  ftle_args a;
+  a.flow = flow.data; a.nx = flow.nx; a.ny = flow.ny; a.nz = flow.nz;
+  a.hx = flow.hx; a.hy = flow.hy; a.hz = flow.hz;
+  a.inverse_time = 1.0 / fabs(time);
+  a.mode = mode;
+  a.out = out;
+  const long long total = (long long)a.nx * a.ny * a.nz;
+  if (total <= 0) return;
+  launch_scope scope(ctx, "ftle_fused");
+  ftle_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx.stream>>>(a);
+}
+}

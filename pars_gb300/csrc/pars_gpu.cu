@@ -1,0 +1,908 @@
+// C ABI of libpars_gpu (include/pars_gpu.h): context, fields, domains, the
+// tracing round loop, curve stages, flow map / FTLE, instrumentation.
+//
+// The round loop follows pars::pipeline::execute (pars/source/pipeline.cpp:
+// 160-208) with load balancing off: per round and per block, round info
+// (particle_tracer.cpp:210-234), trace (:253-337), prune (:402-409), and the
+// out-of-bounds exchange (:376-393) — here a device exit queue sorted by
+// destination block, so the next round's particles never leave the GPU.
+#include <algorithm>
+#include <cstring>
+#include <limits>
+#include <new>
+
+#include "context.hpp"
+
+using pars::device_buffer;
+
+long long pars_gpu_context::held_bytes() const
+{
+  long long total = 0;
+  for (auto& f : fields) total += (long long)f.second->data.bytes();
+  for (auto& d : domains) total += (long long)d.second->device_blocks.bytes();
+  const device_buffer* scratch[] = {&particles_in, &particles_next, &slots, &kept, &written, &offsets, &block_of,
+                                    &block_of_next, &exits, &exit_keys, &exit_keys_sorted, &exit_order,
+                                    &exit_order_sorted, &counters, &block_max, &cub_temp, &scan_input, &tile_counts,
+                                    &tile_offsets, &staging, &ftle, &curves.vertices, &curves.colors,
+                                    &curves.indices, &boundary_positions, &boundary_offsets};
+  for (auto* b : scratch) total += (long long)b->bytes();
+  return total;
+}
+
+namespace pars
+{
+launch_scope::launch_scope(pars_gpu_context& ctx, const char* name) : ctx_(ctx), name_(name)
+{
+  ++ctx_.launches;
+  if (!ctx_.profile) return;
+  if (ctx_.event_pool.empty())
+  {
+    cudaEvent_t e;
+    PARS_CUDA(cudaEventCreate(&e));
+    ctx_.event_pool.push_back(e);
+  }
+  start_ = ctx_.event_pool.back();
+  ctx_.event_pool.pop_back();
+  PARS_CUDA(cudaEventRecord(start_, ctx_.stream));
+}
+
+launch_scope::~launch_scope() noexcept(false)
+{
+  const cudaError_t launch_error = cudaGetLastError();
+  if (start_)
+  {
+    cudaEvent_t stop;
+    if (ctx_.event_pool.empty()) cudaEventCreate(&stop);
+    else { stop = ctx_.event_pool.back(); ctx_.event_pool.pop_back(); }
+    cudaEventRecord(stop, ctx_.stream);
+    ctx_.pending.push_back(timed_launch{name_, start_, stop});
+  }
+  if (launch_error != cudaSuccess && std::uncaught_exceptions() == 0)
+    throw error(PARS_ERR_CUDA, std::string("launch of ") + name_ + ": " + cudaGetErrorString(launch_error));
+}
+
+namespace
+{
+void flush_profile(pars_gpu_context& ctx)
+{
+  if (ctx.pending.empty()) return;
+  PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+  for (auto& p : ctx.pending)
+  {
+    float ms = 0.0f;
+    PARS_CUDA(cudaEventElapsedTime(&ms, p.start, p.stop));
+    auto& entry = ctx.profile_totals[p.name];
+    entry.milliseconds += ms;
+    entry.launches += 1;
+    ctx.event_pool.push_back(p.start);
+    ctx.event_pool.push_back(p.stop);
+  }
+  ctx.pending.clear();
+}
+
+template <typename body_type>
+int32_t guarded(pars_gpu_context* ctx, body_type&& body)
+{
+  if (!ctx) return PARS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(ctx->mutex);
+  try
+  {
+    PARS_CUDA(cudaSetDevice(ctx->device));
+    body();
+    if (ctx->pending.size() > 4096) flush_profile(*ctx);
+    ctx->last_error.clear();
+    return PARS_OK;
+  }
+  catch (const error& e) { ctx->last_error = e.what(); return e.status; }
+  catch (const std::bad_alloc&) { ctx->last_error = "host allocation failed"; return PARS_ERR_OUT_OF_MEMORY; }
+  catch (const std::exception& e) { ctx->last_error = e.what(); return PARS_ERR_STATE; }
+}
+
+field_entry& find_field(pars_gpu_context& ctx, int32_t handle)
+{
+  auto it = ctx.fields.find(handle);
+  if (it == ctx.fields.end()) throw error(PARS_ERR_NOT_FOUND, "no field with handle " + std::to_string(handle));
+  return *it->second;
+}
+
+void check_field_args(const int32_t shape[3], const float spacing[3])
+{
+  PARS_REQUIRE(shape && spacing, "shape and spacing are required");
+  for (int i = 0; i < 3; ++i)
+  {
+    PARS_REQUIRE(shape[i] >= 2, "every field extent must be >= 2");
+    PARS_REQUIRE(spacing[i] > 0.0f, "spacing must be positive");
+  }
+  PARS_REQUIRE((long long)shape[0] * shape[1] * shape[2] < (1LL << 40), "field too large");
+}
+
+int32_t add_field(pars_gpu_context& ctx, std::unique_ptr<field_entry> entry)
+{
+  const int32_t handle = ctx.next_handle++;
+  ctx.fields[handle] = std::move(entry);
+  return handle;
+}
+
+std::unique_ptr<field_entry> make_field(const int32_t shape[3], const float offset[3], const float size[3], const float spacing[3])
+{
+  auto entry = std::make_unique<field_entry>();
+  for (int i = 0; i < 3; ++i)
+  {
+    entry->shape[i] = shape[i];
+    entry->offset[i] = offset ? offset[i] : 0.0f;
+    entry->spacing[i] = spacing[i];
+    entry->size[i] = size ? size[i] : float(shape[i]) * spacing[i];
+  }
+  return entry;
+}
+
+step_rule make_rule(int integrator, int stage_mode, float h)
+{
+  if (integrator != PARS_EULER && integrator != PARS_RUNGE_KUTTA_4)
+    throw error(PARS_ERR_UNSUPPORTED, "integrator " + std::to_string(integrator) + " is not supported (Euler and RK4 are)");
+  PARS_REQUIRE(stage_mode == PARS_STAGES_FROZEN || stage_mode == PARS_STAGES_RESAMPLED, "unknown stage mode");
+  step_rule r {};
+  r.frozen = stage_mode == PARS_STAGES_FROZEN ? 1 : 0;
+  r.rk4 = integrator == PARS_RUNGE_KUTTA_4 ? 1 : 0;
+  r.h = h;
+  // Frozen coefficients b_i * h, b_i formed in FP32 (1.0f/6.0f etc.) as the
+  // generic RK scale-sum does; host FP32 products are IEEE round-to-nearest.
+  if (r.rk4)
+  {
+    const volatile float b0 = 1.0f / 6.0f, b1 = 1.0f / 3.0f;
+    r.count = 4;
+    r.c[0] = b0 * h; r.c[1] = b1 * h; r.c[2] = b1 * h; r.c[3] = b0 * h;
+  }
+  else
+  {
+    r.count = 1;
+    r.c[0] = h;
+  }
+  return r;
+}
+
+// ---- partitioner restated (partitioner.cpp:8-53, prime_factorize.hpp:11-32) ----
+pars_partition_info partition_of(int ranks, int rank, const int32_t domain[3])
+{
+  std::vector<int> factors;
+  int value = ranks, d = 2;
+  while (d * d <= value)
+  {
+    if (value % d == 0) { factors.push_back(d); value /= d; }
+    else ++d;
+  }
+  if (value > 1) factors.push_back(value);
+  pars_partition_info info {};
+  int current[3] = {domain[0], domain[1], domain[2]};
+  for (int i = 0; i < 3; ++i) info.grid_size[i] = 1;
+  while (!factors.empty())
+  {
+    int dim = 0;
+    for (int i = 0; i < 3; ++i) if (current[i] > current[dim]) dim = i;
+    current[dim] /= factors.back();
+    info.grid_size[dim] *= factors.back();
+    factors.pop_back();
+  }
+  long long r = rank;
+  for (int i = 2; i >= 0; --i) { info.multi_rank[i] = int(r % info.grid_size[i]); r /= info.grid_size[i]; }
+  for (int i = 0; i < 3; ++i)
+  {
+    info.block_size[i] = domain[i] / info.grid_size[i];
+    info.offset[i] = info.block_size[i] * info.multi_rank[i];
+    info.ghosted_block_size[i] = info.block_size[i] + (info.multi_rank[i] + 1 < info.grid_size[i] ? 1 : 0);
+  }
+  for (int face = 0; face < 6; ++face)
+  {
+    int n[3] = {info.multi_rank[0], info.multi_rank[1], info.multi_rank[2]};
+    n[face / 2] += (face % 2 == 0) ? -1 : 1;
+    const bool exists = n[face / 2] >= 0 && n[face / 2] < info.grid_size[face / 2];
+    info.neighbor_rank[face] = exists ? int(((long long)n[0] * info.grid_size[1] + n[1]) * info.grid_size[2] + n[2]) : -1;
+  }
+  return info;
+}
+
+void grow_curves(pars_gpu_context& ctx, long long needed_vertices)
+{
+  auto& c = ctx.curves;
+  const std::size_t bytes = sizeof(float4) * (std::size_t)needed_vertices;
+  if (bytes <= c.vertices.bytes()) return;
+  device_buffer bigger;
+  bigger.reserve(std::max<std::size_t>(bytes, c.vertices.bytes() + c.vertices.bytes() / 2));
+  if (c.vertex_total > 0)
+    PARS_CUDA(cudaMemcpyAsync(bigger.get(), c.vertices.get(), sizeof(float4) * c.vertex_total, cudaMemcpyDeviceToDevice, ctx.stream));
+  c.vertices = std::move(bigger);
+}
+
+// The round loop over device-resident particles grouped by block.
+// particles/block_of live in ctx.particles_in / ctx.block_of; block_count and
+// block_max give each block's particle count and maximum remaining_iterations.
+void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, const trace_block* device_blocks,
+                long long count, std::vector<long long> block_count, std::vector<int> block_max,
+                const step_rule& rule, bool route_exits, pars_gpu_trace_summary* summary)
+{
+  auto& curves = ctx.curves;
+  curves.batches.clear();
+  curves.vertex_total = 0;
+  curves.indexed = curves.colored = false;
+  const int nblocks = int(blocks.size());
+  int key_bits = 40;
+  while ((1 << (key_bits - 40)) < nblocks) ++key_bits;
+
+  ctx.counters.reserve(sizeof(unsigned long long) * 2);
+  auto* steps_counter = ctx.counters.as<unsigned long long>();
+  auto* exit_counter = reinterpret_cast<unsigned int*>(steps_counter + 1);
+  PARS_CUDA(cudaMemsetAsync(steps_counter, 0, sizeof(unsigned long long), ctx.stream));
+
+  int round = 0;
+  while (count > 0)
+  {
+    int stride = 1;
+    for (int b = 0; b < nblocks; ++b) if (block_count[b] > 0) stride = std::max(stride, block_max[b]);
+    ctx.slots.reserve(sizeof(float4) * (std::size_t)count * stride);
+    ctx.written.reserve(sizeof(int) * count);
+    ctx.kept.reserve(sizeof(int) * count);
+    ctx.offsets.reserve(sizeof(long long) * (count + 1));
+    if (route_exits)
+    {
+      ctx.exits.reserve(sizeof(pars_particle) * count);
+      ctx.exit_keys.reserve(sizeof(unsigned long long) * count);
+    }
+    PARS_CUDA(cudaMemsetAsync(exit_counter, 0, sizeof(unsigned int), ctx.stream));
+
+    trace_launch a {};
+    a.blocks = device_blocks;
+    a.particles = ctx.particles_in.as<const pars_particle>();
+    a.block_of = nblocks > 1 ? ctx.block_of.as<const int>() : nullptr;
+    a.count = count;
+    a.slot_stride = stride;
+    a.slots = ctx.slots.as<float4>();
+    a.written = ctx.written.as<int>();
+    a.kept = ctx.kept.as<int>();
+    a.rule = rule;
+    a.route_exits = route_exits ? 1 : 0;
+    a.exit_particles = route_exits ? ctx.exits.as<pars_particle>() : nullptr;
+    a.exit_keys = route_exits ? ctx.exit_keys.as<unsigned long long>() : nullptr;
+    a.exit_count = exit_counter;
+    a.steps = steps_counter;
+    launch_trace(ctx, a);
+
+    // prune: packed offsets of every particle's kept vertices.
+    exclusive_sum(ctx, ctx.kept.as<int>(), ctx.offsets.as<long long>(), count);
+
+    // Batch boundaries per block (compute_round_info), as particle indices.
+    struct pending_batch { long long first, last; int rank; };
+    std::vector<pending_batch> pending;
+    long long first = 0;
+    for (int b = 0; b < nblocks; ++b)
+    {
+      const long long n = block_count[b];
+      if (n == 0) continue;
+      const long long max_vertices = std::numeric_limits<int32_t>::max() / 16;
+      const long long ppc = max_vertices / std::max(1, block_max[b]);
+      PARS_REQUIRE(ppc > 0, "remaining_iterations exceeds the batch vertex limit");
+      const long long curve_count = 1 + n / ppc;
+      for (long long k = 0; k < curve_count; ++k)
+        pending.push_back({first + std::min(n, k * ppc), first + std::min(n, (k + 1) * ppc), b});
+      first += n;
+    }
+    std::vector<long long> positions;
+    positions.reserve(pending.size() * 2 + 1);
+    for (auto& p : pending) { positions.push_back(p.first); positions.push_back(p.last); }
+    positions.push_back(count);
+    std::vector<long long> boundary(positions.size());
+    ctx.boundary_positions.reserve(sizeof(long long) * positions.size());
+    ctx.boundary_offsets.reserve(sizeof(long long) * positions.size());
+    PARS_CUDA(cudaMemcpyAsync(ctx.boundary_positions.get(), positions.data(), sizeof(long long) * positions.size(), cudaMemcpyHostToDevice, ctx.stream));
+    launch_gather_offsets(ctx, ctx.offsets.as<const long long>(), ctx.boundary_positions.as<const long long>(), (long long)positions.size(),
+                          ctx.boundary_offsets.as<long long>());
+    unsigned int exit_total = 0;
+    PARS_CUDA(cudaMemcpyAsync(boundary.data(), ctx.boundary_offsets.get(), sizeof(long long) * boundary.size(), cudaMemcpyDeviceToHost, ctx.stream));
+    PARS_CUDA(cudaMemcpyAsync(&exit_total, exit_counter, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx.stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+    const long long round_vertices = boundary.back();
+
+    grow_curves(ctx, curves.vertex_total + round_vertices);
+    launch_compact_vertices(ctx, ctx.slots.as<const float4>(), stride, ctx.written.as<const int>(), ctx.offsets.as<const long long>(),
+                            count, curves.vertices.as<float4>() + curves.vertex_total);
+    for (std::size_t k = 0; k < pending.size(); ++k)
+    {
+      curves_batch batch;
+      batch.vertex_offset = curves.vertex_total + boundary[2 * k];
+      batch.vertex_count = boundary[2 * k + 1] - boundary[2 * k];
+      batch.rank = pending[k].rank;
+      batch.round = round;
+      curves.batches.push_back(batch);
+    }
+    curves.vertex_total += round_vertices;
+
+    // Exchange: the exit queue, stably ordered by (destination block, source
+    // order), becomes the next round's particle list.
+    long long next = route_exits ? (long long)exit_total : 0;
+    std::fill(block_count.begin(), block_count.end(), 0);
+    std::fill(block_max.begin(), block_max.end(), 0);
+    if (next > 0)
+    {
+      ctx.exit_keys_sorted.reserve(sizeof(unsigned long long) * next);
+      ctx.exit_order.reserve(sizeof(unsigned int) * next);
+      ctx.exit_order_sorted.reserve(sizeof(unsigned int) * next);
+      ctx.particles_next.reserve(sizeof(pars_particle) * next);
+      ctx.block_of_next.reserve(sizeof(int) * next);
+      ctx.block_max.reserve(sizeof(int) * 2 * nblocks);
+      PARS_CUDA(cudaMemsetAsync(ctx.block_max.get(), 0, sizeof(int) * 2 * nblocks, ctx.stream));
+      launch_iota(ctx, ctx.exit_order.as<unsigned int>(), next);
+      sort_pairs(ctx, ctx.exit_keys.as<const unsigned long long>(), ctx.exit_keys_sorted.as<unsigned long long>(),
+                 ctx.exit_order.as<const unsigned int>(), ctx.exit_order_sorted.as<unsigned int>(), next, key_bits);
+      launch_gather_exits(ctx, ctx.exits.as<const pars_particle>(), ctx.exit_order_sorted.as<const unsigned int>(),
+                          ctx.exit_keys_sorted.as<const unsigned long long>(), next, ctx.particles_next.as<pars_particle>(),
+                          ctx.block_of_next.as<int>(), ctx.block_max.as<int>(), ctx.block_max.as<int>() + nblocks);
+      std::vector<int> stats(2 * nblocks);
+      PARS_CUDA(cudaMemcpyAsync(stats.data(), ctx.block_max.get(), sizeof(int) * 2 * nblocks, cudaMemcpyDeviceToHost, ctx.stream));
+      PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+      for (int b = 0; b < nblocks; ++b) { block_max[b] = stats[b]; block_count[b] = stats[nblocks + b]; }
+      std::swap(ctx.particles_in, ctx.particles_next);
+      std::swap(ctx.block_of, ctx.block_of_next);
+    }
+    count = next;
+    ++round;
+  }
+
+  unsigned long long steps = 0;
+  PARS_CUDA(cudaMemcpyAsync(&steps, steps_counter, sizeof(steps), cudaMemcpyDeviceToHost, ctx.stream));
+  PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+  if (summary)
+  {
+    summary->batches = (long long)curves.batches.size();
+    summary->vertices = curves.vertex_total;
+    summary->steps = (long long)steps;
+    summary->rounds = round;
+    summary->padding = 0;
+  }
+}
+
+// Single block: one trace_block with no neighbours, kept in a small device array.
+const trace_block* single_block(pars_gpu_context& ctx, const field_entry& f, std::vector<trace_block>& blocks)
+{
+  trace_block b;
+  b.field = f.view();
+  for (int i = 0; i < 6; ++i) b.neighbor[i] = -1;
+  blocks.assign(1, b);
+  ctx.single_block.reserve(sizeof(trace_block));
+  PARS_CUDA(cudaMemcpyAsync(ctx.single_block.get(), &b, sizeof(trace_block), cudaMemcpyHostToDevice, ctx.stream));
+  return ctx.single_block.as<const trace_block>();
+}
+
+void trace_single(pars_gpu_context& ctx, int32_t field, long long count, int32_t integrator, int32_t stage_mode,
+                  float step_size, pars_gpu_trace_summary* summary)
+{
+  auto& f = find_field(ctx, field);
+  const step_rule rule = make_rule(integrator, stage_mode, step_size);
+  std::vector<trace_block> blocks;
+  const trace_block* device_blocks = single_block(ctx, f, blocks);
+  std::vector<long long> block_count(1, count);
+  std::vector<int> block_max(1, 0);
+  if (count > 0)
+  {
+    ctx.block_max.reserve(sizeof(int) * 2);
+    PARS_CUDA(cudaMemsetAsync(ctx.block_max.get(), 0, sizeof(int) * 2, ctx.stream));
+    launch_particle_stats(ctx, ctx.particles_in.as<const pars_particle>(), nullptr, count, ctx.block_max.as<int>());
+    PARS_CUDA(cudaMemcpyAsync(block_max.data(), ctx.block_max.get(), sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+  }
+  run_rounds(ctx, blocks, device_blocks, count, block_count, block_max, rule, false, summary);
+}
+
+std::size_t checked_bytes(long long count, std::size_t element)
+{
+  PARS_REQUIRE(count >= 0, "negative count");
+  return (std::size_t)count * element;
+}
+}
+}
+
+using namespace pars;
+
+// The library is built with hidden visibility; only the C ABI is exported.
+#pragma GCC visibility push(default)
+extern "C" {
+
+int32_t pars_gpu_abi_version(void) { return PARS_GPU_ABI_VERSION; }
+
+int32_t pars_gpu_create(pars_gpu_context** context, int32_t device)
+{
+  if (!context) return PARS_ERR_INVALID_ARGUMENT;
+  *context = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) { (void)cudaGetLastError(); return PARS_ERR_CUDA; }
+  if (device < 0 || device >= count) return PARS_ERR_INVALID_ARGUMENT;
+  auto* ctx = new (std::nothrow) pars_gpu_context();
+  if (!ctx) return PARS_ERR_OUT_OF_MEMORY;
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+  {
+    (void)cudaGetLastError();
+    delete ctx;
+    return PARS_ERR_CUDA;
+  }
+  ctx->stream = ctx->own_stream;
+  *context = ctx;
+  return PARS_OK;
+}
+
+int32_t pars_gpu_destroy(pars_gpu_context* ctx)
+{
+  if (!ctx) return PARS_ERR_INVALID_ARGUMENT;
+  {
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& p : ctx->pending) { cudaEventDestroy(p.start); cudaEventDestroy(p.stop); }
+    for (auto e : ctx->event_pool) cudaEventDestroy(e);
+    ctx->pending.clear();
+    ctx->event_pool.clear();
+    ctx->fields.clear();
+    ctx->domains.clear();
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  }
+  delete ctx;
+  return PARS_OK;
+}
+
+const char* pars_gpu_last_error(const pars_gpu_context* ctx)
+{
+  return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+int32_t pars_gpu_set_stream(pars_gpu_context* ctx, void* stream)
+{
+  return guarded(ctx, [&] {
+    flush_profile(*ctx);
+    ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  });
+}
+
+int32_t pars_gpu_synchronize(pars_gpu_context* ctx)
+{
+  return guarded(ctx, [&] { PARS_CUDA(cudaStreamSynchronize(ctx->stream)); });
+}
+
+int32_t pars_gpu_memory_in_use(pars_gpu_context* ctx, int64_t* bytes)
+{
+  return guarded(ctx, [&] { PARS_REQUIRE(bytes, "bytes is required"); *bytes = ctx->held_bytes(); });
+}
+
+// ---- fields -------------------------------------------------------------------
+int32_t pars_gpu_field_upload(pars_gpu_context* ctx, const float* xyz, const int32_t shape[3], const float offset[3],
+                              const float size[3], const float spacing[3], int32_t* field)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(xyz && field, "xyz and field are required");
+    check_field_args(shape, spacing);
+    auto entry = make_field(shape, offset, size, spacing);
+    const long long count = (long long)shape[0] * shape[1] * shape[2];
+    ctx->staging.reserve(sizeof(float) * 3 * count);
+    entry->data.reserve(sizeof(float4) * count);
+    PARS_CUDA(cudaMemcpyAsync(ctx->staging.get(), xyz, sizeof(float) * 3 * count, cudaMemcpyHostToDevice, ctx->stream));
+    launch_pack_field(*ctx, ctx->staging.as<const float>(), entry->data.as<float4>(), count);
+    *field = add_field(*ctx, std::move(entry));
+  });
+}
+
+int32_t pars_gpu_field_upload_device(pars_gpu_context* ctx, const float* device_xyz, const int32_t shape[3], const float offset[3],
+                                     const float size[3], const float spacing[3], int32_t* field)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(device_xyz && field, "device_xyz and field are required");
+    check_field_args(shape, spacing);
+    auto entry = make_field(shape, offset, size, spacing);
+    const long long count = (long long)shape[0] * shape[1] * shape[2];
+    entry->data.reserve(sizeof(float4) * count);
+    launch_pack_field(*ctx, device_xyz, entry->data.as<float4>(), count);
+    *field = add_field(*ctx, std::move(entry));
+  });
+}
+
+int32_t pars_gpu_field_release(pars_gpu_context* ctx, int32_t field)
+{
+  return guarded(ctx, [&] {
+    auto it = ctx->fields.find(field);
+    if (it == ctx->fields.end()) throw error(PARS_ERR_NOT_FOUND, "no field with handle " + std::to_string(field));
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->fields.erase(it);
+  });
+}
+
+int32_t pars_gpu_field_info(pars_gpu_context* ctx, int32_t field, int32_t shape[3], float offset[3], float size[3], float spacing[3])
+{
+  return guarded(ctx, [&] {
+    auto& f = find_field(*ctx, field);
+    for (int i = 0; i < 3; ++i)
+    {
+      if (shape) shape[i] = f.shape[i];
+      if (offset) offset[i] = f.offset[i];
+      if (size) size[i] = f.size[i];
+      if (spacing) spacing[i] = f.spacing[i];
+    }
+  });
+}
+
+int32_t pars_gpu_field_download(pars_gpu_context* ctx, int32_t field, float* xyz)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(xyz, "xyz is required");
+    auto& f = find_field(*ctx, field);
+    const long long count = (long long)f.shape[0] * f.shape[1] * f.shape[2];
+    ctx->staging.reserve(sizeof(float) * 3 * count);
+    launch_unpack_field(*ctx, f.data.as<const float4>(), ctx->staging.as<float>(), count);
+    PARS_CUDA(cudaMemcpyAsync(xyz, ctx->staging.get(), sizeof(float) * 3 * count, cudaMemcpyDeviceToHost, ctx->stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int32_t pars_gpu_field_sample(pars_gpu_context* ctx, int32_t field, const float* positions, int64_t n, uint8_t* inside, float* velocity)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(n >= 0, "negative count");
+    if (n == 0) return;
+    PARS_REQUIRE(positions && inside && velocity, "positions, inside and velocity are required");
+    auto& f = find_field(*ctx, field);
+    device_buffer p, in, v;
+    p.reserve(checked_bytes(n, sizeof(float4)));
+    in.reserve(checked_bytes(n, 1));
+    v.reserve(checked_bytes(n, 3 * sizeof(float)));
+    PARS_CUDA(cudaMemcpyAsync(p.get(), positions, sizeof(float4) * n, cudaMemcpyHostToDevice, ctx->stream));
+    launch_field_sample(*ctx, f.view(), p.as<const float4>(), n, in.as<uint8_t>(), v.as<float>());
+    PARS_CUDA(cudaMemcpyAsync(inside, in.get(), n, cudaMemcpyDeviceToHost, ctx->stream));
+    PARS_CUDA(cudaMemcpyAsync(velocity, v.get(), sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+// ---- seeds / partition -----------------------------------------------------------
+int32_t pars_gpu_seed_generate(pars_gpu_context* ctx, const float offset[3], const float size[3], const float stride[3],
+                               int32_t iterations, int32_t rank, pars_particle* particles, int64_t capacity, int64_t* count)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(offset && size && stride && count, "offset, size, stride and count are required");
+    int per_dimension[3];
+    long long total = 1;
+    for (int i = 0; i < 3; ++i)
+    {
+      // (size / stride).cast<integer>() (seed_generator.cpp:11): FP32 quotient, truncated.
+      const float q = size[i] / stride[i];
+      per_dimension[i] = (q > 0.0f && q < 2147483647.0f) ? int(q) : 0;
+      total *= per_dimension[i];
+    }
+    *count = total;
+    if (!particles || total == 0) return;
+    PARS_REQUIRE(capacity >= total, "capacity is smaller than the seed count");
+    device_buffer out;
+    out.reserve(checked_bytes(total, sizeof(pars_particle)));
+    launch_seed_generate(*ctx, offset, stride, per_dimension, iterations, rank, out.as<pars_particle>());
+    PARS_CUDA(cudaMemcpyAsync(particles, out.get(), sizeof(pars_particle) * total, cudaMemcpyDeviceToHost, ctx->stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int32_t pars_gpu_partition(int32_t ranks, int32_t rank, const int32_t domain_size[3], pars_partition_info* info)
+{
+  if (!domain_size || !info || ranks < 1 || rank < 0 || rank >= ranks) return PARS_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < 3; ++i) if (domain_size[i] < 1) return PARS_ERR_INVALID_ARGUMENT;
+  *info = partition_of(ranks, rank, domain_size);
+  return PARS_OK;
+}
+
+// ---- tracing --------------------------------------------------------------------
+int32_t pars_gpu_trace(pars_gpu_context* ctx, int32_t field, const pars_particle* particles, int64_t count,
+                       int32_t integrator, int32_t stage_mode, float step_size, pars_gpu_trace_summary* summary)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(count >= 0 && (count == 0 || particles), "particles are required");
+    ctx->particles_in.reserve(checked_bytes(std::max<long long>(count, 1), sizeof(pars_particle)));
+    if (count > 0)
+      PARS_CUDA(cudaMemcpyAsync(ctx->particles_in.get(), particles, sizeof(pars_particle) * count, cudaMemcpyHostToDevice, ctx->stream));
+    trace_single(*ctx, field, count, integrator, stage_mode, step_size, summary);
+  });
+}
+
+int32_t pars_gpu_trace_device(pars_gpu_context* ctx, int32_t field, const pars_particle* device_particles, int64_t count,
+                              int32_t integrator, int32_t stage_mode, float step_size, pars_gpu_trace_summary* summary)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(count >= 0 && (count == 0 || device_particles), "particles are required");
+    ctx->particles_in.reserve(checked_bytes(std::max<long long>(count, 1), sizeof(pars_particle)));
+    if (count > 0)
+      PARS_CUDA(cudaMemcpyAsync(ctx->particles_in.get(), device_particles, sizeof(pars_particle) * count, cudaMemcpyDeviceToDevice, ctx->stream));
+    trace_single(*ctx, field, count, integrator, stage_mode, step_size, summary);
+  });
+}
+
+int32_t pars_gpu_domain_create(pars_gpu_context* ctx, const float* xyz, const int32_t domain_size[3], const float spacing[3],
+                               int32_t ranks, int32_t* domain)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(xyz && domain_size && spacing && domain, "xyz, domain_size, spacing and domain are required");
+    PARS_REQUIRE(ranks >= 1, "ranks must be >= 1");
+    check_field_args(domain_size, spacing);
+    auto entry = std::make_unique<domain_entry>();
+    entry->ranks = ranks;
+    entry->first = partition_of(ranks, 0, domain_size);
+    for (int i = 0; i < 3; ++i) PARS_REQUIRE(entry->first.block_size[i] >= 1, "more blocks than voxels along an axis");
+    const long long total = (long long)domain_size[0] * domain_size[1] * domain_size[2];
+    ctx->staging.reserve(sizeof(float) * 3 * total);
+    PARS_CUDA(cudaMemcpyAsync(ctx->staging.get(), xyz, sizeof(float) * 3 * total, cudaMemcpyHostToDevice, ctx->stream));
+    for (int r = 0; r < ranks; ++r)
+    {
+      const pars_partition_info info = partition_of(ranks, r, domain_size);
+      auto f = std::make_unique<field_entry>();
+      for (int i = 0; i < 3; ++i)
+      {
+        f->shape[i] = info.ghosted_block_size[i];
+        f->spacing[i] = spacing[i];
+        f->offset[i] = float(info.offset[i]) * spacing[i];          // data_io.cpp:113
+        f->size[i] = float(info.block_size[i]) * spacing[i];        // data_io.cpp:114
+      }
+      for (int i = 0; i < 3; ++i) PARS_REQUIRE(f->shape[i] >= 2, "blocks must be at least 2 voxels wide");
+      f->data.reserve(sizeof(float4) * (std::size_t)f->shape[0] * f->shape[1] * f->shape[2]);
+      launch_extract_block(*ctx, ctx->staging.as<const float>(), domain_size, info.offset, f->shape, f->data.as<float4>());
+      trace_block b;
+      b.field = f->view();
+      for (int face = 0; face < 6; ++face) b.neighbor[face] = info.neighbor_rank[face];
+      entry->blocks.push_back(b);
+      entry->fields.push_back(add_field(*ctx, std::move(f)));
+    }
+    entry->device_blocks.reserve(sizeof(trace_block) * ranks);
+    PARS_CUDA(cudaMemcpyAsync(entry->device_blocks.get(), entry->blocks.data(), sizeof(trace_block) * ranks, cudaMemcpyHostToDevice, ctx->stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int32_t handle = ctx->next_handle++;
+    ctx->domains[handle] = std::move(entry);
+    *domain = handle;
+  });
+}
+
+int32_t pars_gpu_domain_release(pars_gpu_context* ctx, int32_t domain)
+{
+  return guarded(ctx, [&] {
+    auto it = ctx->domains.find(domain);
+    if (it == ctx->domains.end()) throw error(PARS_ERR_NOT_FOUND, "no domain with handle " + std::to_string(domain));
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int f : it->second->fields) ctx->fields.erase(f);
+    ctx->domains.erase(it);
+  });
+}
+
+int32_t pars_gpu_trace_domain(pars_gpu_context* ctx, int32_t domain, const pars_particle* particles, const int64_t* seed_offsets,
+                              int32_t integrator, int32_t stage_mode, float step_size, pars_gpu_trace_summary* summary)
+{
+  return guarded(ctx, [&] {
+    auto it = ctx->domains.find(domain);
+    if (it == ctx->domains.end()) throw error(PARS_ERR_NOT_FOUND, "no domain with handle " + std::to_string(domain));
+    auto& d = *it->second;
+    PARS_REQUIRE(seed_offsets, "seed_offsets is required");
+    const step_rule rule = make_rule(integrator, stage_mode, step_size);
+    const int nblocks = d.ranks;
+    const long long count = seed_offsets[nblocks] - seed_offsets[0];
+    PARS_REQUIRE(count >= 0 && (count == 0 || particles), "particles are required");
+    std::vector<long long> block_count(nblocks);
+    std::vector<int> block_max(nblocks, 0);
+    std::vector<int> block_of(std::max<long long>(count, 1));
+    for (int b = 0; b < nblocks; ++b)
+    {
+      const long long begin = seed_offsets[b] - seed_offsets[0], end = seed_offsets[b + 1] - seed_offsets[0];
+      PARS_REQUIRE(end >= begin, "seed_offsets must be non-decreasing");
+      block_count[b] = end - begin;
+      for (long long i = begin; i < end; ++i)
+      {
+        block_of[i] = b;
+        block_max[b] = std::max(block_max[b], particles[seed_offsets[0] + i].remaining_iterations);
+      }
+    }
+    ctx->particles_in.reserve(checked_bytes(std::max<long long>(count, 1), sizeof(pars_particle)));
+    ctx->block_of.reserve(checked_bytes(std::max<long long>(count, 1), sizeof(int)));
+    if (count > 0)
+    {
+      PARS_CUDA(cudaMemcpyAsync(ctx->particles_in.get(), particles + seed_offsets[0], sizeof(pars_particle) * count, cudaMemcpyHostToDevice, ctx->stream));
+      PARS_CUDA(cudaMemcpyAsync(ctx->block_of.get(), block_of.data(), sizeof(int) * count, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    run_rounds(*ctx, d.blocks, d.device_blocks.as<const trace_block>(), count, block_count, block_max, rule, true, summary);
+  });
+}
+
+// ---- curve stages -----------------------------------------------------------------
+int32_t pars_gpu_curves_index(pars_gpu_context* ctx)
+{
+  return guarded(ctx, [&] {
+    auto& c = ctx->curves;
+    c.indices.reserve(sizeof(int) * (std::size_t)std::max<long long>(c.vertex_total, 1));
+    for (auto& b : c.batches)
+    {
+      b.index_offset = b.vertex_offset;
+      b.index_count = launch_index_generate(*ctx, c.vertices.as<const float4>() + b.vertex_offset, b.vertex_count,
+                                            c.indices.as<int>() + b.index_offset);
+    }
+    c.indexed = true;
+    c.colored = false;
+  });
+}
+
+int32_t pars_gpu_curves_color(pars_gpu_context* ctx, int32_t mode, float parameter)
+{
+  return guarded(ctx, [&] {
+    auto& c = ctx->curves;
+    if (!c.indexed) throw error(PARS_ERR_STATE, "curves must be indexed before they are coloured");
+    PARS_REQUIRE(mode >= PARS_COLOR_HSL_CONSTANT_S && mode <= PARS_COLOR_RGB, "unknown colour mode");
+    c.colors.reserve(sizeof(float4) * (std::size_t)std::max<long long>(c.vertex_total, 1));
+    PARS_CUDA(cudaMemsetAsync(c.colors.get(), 0, sizeof(float4) * c.vertex_total, ctx->stream));
+    for (auto& b : c.batches)
+      launch_color_generate(*ctx, c.vertices.as<const float4>() + b.vertex_offset, c.indices.as<const int>() + b.index_offset,
+                            b.index_count, mode, parameter, c.colors.as<float4>() + b.vertex_offset);
+    c.colored = true;
+  });
+}
+
+int32_t pars_gpu_curves_batch_info(pars_gpu_context* ctx, int64_t batch, int64_t* vertices, int64_t* indices, int32_t* rank, int32_t* round)
+{
+  return guarded(ctx, [&] {
+    auto& c = ctx->curves;
+    PARS_REQUIRE(batch >= 0 && batch < (int64_t)c.batches.size(), "batch out of range");
+    const auto& b = c.batches[batch];
+    if (vertices) *vertices = b.vertex_count;
+    if (indices) *indices = c.indexed ? b.index_count : 0;
+    if (rank) *rank = b.rank;
+    if (round) *round = b.round;
+  });
+}
+
+int32_t pars_gpu_curves_download(pars_gpu_context* ctx, int64_t batch, float* vertices, float* colors, int32_t* indices)
+{
+  return guarded(ctx, [&] {
+    auto& c = ctx->curves;
+    PARS_REQUIRE(batch >= 0 && batch < (int64_t)c.batches.size(), "batch out of range");
+    const auto& b = c.batches[batch];
+    if (vertices && b.vertex_count)
+      PARS_CUDA(cudaMemcpyAsync(vertices, c.vertices.as<float4>() + b.vertex_offset, sizeof(float4) * b.vertex_count, cudaMemcpyDeviceToHost, ctx->stream));
+    if (colors && b.vertex_count)
+    {
+      if (!c.colored) throw error(PARS_ERR_STATE, "curves are not coloured");
+      PARS_CUDA(cudaMemcpyAsync(colors, c.colors.as<float4>() + b.vertex_offset, sizeof(float4) * b.vertex_count, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if (indices && c.indexed && b.index_count)
+      PARS_CUDA(cudaMemcpyAsync(indices, c.indices.as<int>() + b.index_offset, sizeof(int) * b.index_count, cudaMemcpyDeviceToHost, ctx->stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int32_t pars_gpu_index_generate(pars_gpu_context* ctx, const float* vertices, int64_t n, int32_t* indices, int64_t* index_count)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(index_count && n >= 0 && (n == 0 || (vertices && indices)), "vertices, indices and index_count are required");
+    *index_count = 0;
+    if (n < 2) return;
+    device_buffer v, i;
+    v.reserve(checked_bytes(n, sizeof(float4)));
+    i.reserve(checked_bytes(n, sizeof(int)));
+    PARS_CUDA(cudaMemcpyAsync(v.get(), vertices, sizeof(float4) * n, cudaMemcpyHostToDevice, ctx->stream));
+    const long long m = launch_index_generate(*ctx, v.as<const float4>(), n, i.as<int>());
+    if (m) PARS_CUDA(cudaMemcpyAsync(indices, i.get(), sizeof(int) * m, cudaMemcpyDeviceToHost, ctx->stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+    *index_count = m;
+  });
+}
+
+int32_t pars_gpu_color_generate(pars_gpu_context* ctx, const float* vertices, int64_t n, const int32_t* indices, int64_t index_count,
+                                int32_t mode, float parameter, float* colors)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(n >= 0 && index_count >= 0 && (n == 0 || (vertices && colors)) && (index_count == 0 || indices), "buffers are required");
+    PARS_REQUIRE(mode >= PARS_COLOR_HSL_CONSTANT_S && mode <= PARS_COLOR_RGB, "unknown colour mode");
+    if (n == 0 || index_count == 0) return;
+    for (int64_t k = 0; k < index_count; ++k)
+      PARS_REQUIRE(indices[k] >= 0 && indices[k] + 1 < n, "index out of range");
+    device_buffer v, i, c;
+    v.reserve(checked_bytes(n, sizeof(float4)));
+    i.reserve(checked_bytes(index_count, sizeof(int)));
+    c.reserve(checked_bytes(n, sizeof(float4)));
+    PARS_CUDA(cudaMemcpyAsync(v.get(), vertices, sizeof(float4) * n, cudaMemcpyHostToDevice, ctx->stream));
+    PARS_CUDA(cudaMemcpyAsync(i.get(), indices, sizeof(int) * index_count, cudaMemcpyHostToDevice, ctx->stream));
+    PARS_CUDA(cudaMemcpyAsync(c.get(), colors, sizeof(float4) * n, cudaMemcpyHostToDevice, ctx->stream));
+    launch_color_generate(*ctx, v.as<const float4>(), i.as<const int>(), index_count, mode, parameter, c.as<float4>());
+    PARS_CUDA(cudaMemcpyAsync(colors, c.get(), sizeof(float4) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+// ---- flow map / FTLE -------------------------------------------------------------
+int32_t pars_gpu_flow_map_generate(pars_gpu_context* ctx, int32_t field, int32_t iterations, float resolution_scale,
+                                   int32_t integrator, int32_t stage_mode, float step_size, int32_t* flow_map, int64_t* steps)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(flow_map, "flow_map is required");
+    PARS_REQUIRE(resolution_scale > 0.0f, "resolution_scale must be positive");
+    auto& f = find_field(*ctx, field);
+    const step_rule rule = make_rule(integrator, stage_mode, step_size);
+    auto entry = std::make_unique<field_entry>();
+    int seeds[3];
+    for (int i = 0; i < 3; ++i)
+    {
+      entry->shape[i] = int(float(f.shape[i]) * resolution_scale);      // flow_map_generator.cpp:27-30
+      entry->spacing[i] = f.spacing[i] / resolution_scale;              // :34-37
+      entry->offset[i] = f.offset[i];
+      entry->size[i] = f.size[i];
+      const float q = f.size[i] / entry->spacing[i];                     // seed_generator.cpp:11
+      seeds[i] = (q > 0.0f && q < 2147483647.0f) ? int(q) : 0;
+      PARS_REQUIRE(entry->shape[i] >= 1, "flow map would be empty");
+    }
+    const long long voxels = (long long)entry->shape[0] * entry->shape[1] * entry->shape[2];
+    entry->data.reserve(sizeof(float4) * voxels);
+    // Voxels no seed reaches stay NaN (the reference leaves them unassigned).
+    PARS_CUDA(cudaMemsetAsync(entry->data.get(), 0xff, sizeof(float4) * voxels, ctx->stream));
+    ctx->counters.reserve(sizeof(unsigned long long) * 2);
+    auto* counter = ctx->counters.as<unsigned long long>();
+    PARS_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
+    launch_flow_map(*ctx, f.view(), rule, iterations, f.offset, entry->spacing, seeds, entry->shape, entry->data.as<float4>(), counter);
+    if (steps)
+    {
+      unsigned long long s = 0;
+      PARS_CUDA(cudaMemcpyAsync(&s, counter, sizeof(s), cudaMemcpyDeviceToHost, ctx->stream));
+      PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+      *steps = (int64_t)s;
+    }
+    *flow_map = add_field(*ctx, std::move(entry));
+  });
+}
+
+int32_t pars_gpu_ftle_generate(pars_gpu_context* ctx, int32_t flow_map, float time, int32_t mode, float* ftle)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(mode == PARS_FTLE_REGULAR || mode == PARS_FTLE_FRACTIONAL_ANISOTROPY, "unknown FTLE mode");
+    PARS_REQUIRE(time != 0.0f, "time must be non-zero");
+    auto& f = find_field(*ctx, flow_map);
+    const long long voxels = (long long)f.shape[0] * f.shape[1] * f.shape[2];
+    ctx->ftle.reserve(sizeof(float) * voxels);
+    ctx->ftle_count = voxels;
+    launch_ftle(*ctx, f.view(), double(time), mode, ctx->ftle.as<float>());
+    if (ftle)
+    {
+      PARS_CUDA(cudaMemcpyAsync(ftle, ctx->ftle.get(), sizeof(float) * voxels, cudaMemcpyDeviceToHost, ctx->stream));
+      PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+  });
+}
+
+int32_t pars_gpu_ftle_device_pointer(pars_gpu_context* ctx, const float** device_ftle, int64_t* count)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(device_ftle && count, "device_ftle and count are required");
+    *device_ftle = ctx->ftle.as<const float>();
+    *count = ctx->ftle_count;
+  });
+}
+
+// ---- instrumentation ------------------------------------------------------------
+int32_t pars_gpu_profile_enable(pars_gpu_context* ctx, int32_t enable)
+{
+  return guarded(ctx, [&] { flush_profile(*ctx); ctx->profile = enable != 0; });
+}
+
+int32_t pars_gpu_profile_reset(pars_gpu_context* ctx)
+{
+  return guarded(ctx, [&] { flush_profile(*ctx); ctx->profile_totals.clear(); });
+}
+
+int32_t pars_gpu_profile_get(pars_gpu_context* ctx, const char* name, double* milliseconds, int64_t* launches)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(name, "name is required");
+    flush_profile(*ctx);
+    auto it = ctx->profile_totals.find(name);
+    if (milliseconds) *milliseconds = it == ctx->profile_totals.end() ? 0.0 : it->second.milliseconds;
+    if (launches) *launches = it == ctx->profile_totals.end() ? 0 : it->second.launches;
+  });
+}
+
+int32_t pars_gpu_launch_count(pars_gpu_context* ctx, int64_t* launches)
+{
+  return guarded(ctx, [&] { PARS_REQUIRE(launches, "launches is required"); *launches = ctx->launches; });
+}
+
+}
+#pragma GCC visibility pop

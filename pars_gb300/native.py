@@ -1,0 +1,333 @@
+"""ctypes binding of libpars_gpu.so (include/pars_gpu.h).
+
+The product path: every call goes to the sm_103a library.  There is no CPU
+fallback — importing works without a GPU, but using a Context requires the
+built library and a CUDA device, and fails loudly otherwise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBRARY_PATH = os.path.join(HERE, "libpars_gpu.so")
+
+PARTICLE_DTYPE = np.dtype([
+    ("position", np.float32, 4),
+    ("remaining_iterations", np.int32),
+    ("vector_field_index", np.int32),
+    ("original_rank", np.int32),
+    ("original_voxel", np.int32, 3),
+    ("padding", np.int32, 2),
+])
+assert PARTICLE_DTYPE.itemsize == 48
+
+# enum values of include/pars_gpu.h
+EULER, MODIFIED_MIDPOINT, RUNGE_KUTTA_4 = 0, 1, 2
+INTEGRATORS = {"euler": 0, "modified_midpoint": 1, "runge_kutta_4": 2, "runge_kutta_cash_karp_54": 3,
+               "runge_kutta_dormand_prince_5": 4, "runge_kutta_fehlberg_78": 5, "adams_bashforth_2": 6,
+               "adams_bashforth_moulton_2": 7}
+STAGES_FROZEN, STAGES_RESAMPLED = 0, 1
+COLOR_MODES = {"hsl_constant_s": 0, "hsl_constant_l": 1, "hsv_constant_s": 2, "hsv_constant_v": 3, "rgb": 4}
+FTLE_REGULAR, FTLE_FRACTIONAL_ANISOTROPY = 0, 1
+STATUS = {0: "ok", -1: "invalid argument", -2: "cuda error", -3: "out of memory", -4: "unsupported",
+          -5: "not found", -6: "over budget", -7: "cancelled", -8: "timeout", -9: "bad state"}
+
+
+class PartitionInfo(ctypes.Structure):
+    _fields_ = [("grid_size", ctypes.c_int32 * 3), ("block_size", ctypes.c_int32 * 3),
+                ("multi_rank", ctypes.c_int32 * 3), ("offset", ctypes.c_int32 * 3),
+                ("ghosted_block_size", ctypes.c_int32 * 3), ("neighbor_rank", ctypes.c_int32 * 6)]
+
+
+class TraceSummary(ctypes.Structure):
+    _fields_ = [("batches", ctypes.c_int64), ("vertices", ctypes.c_int64), ("steps", ctypes.c_int64),
+                ("rounds", ctypes.c_int32), ("padding", ctypes.c_int32)]
+
+
+class ParsGpuError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS.get(status, status)} ({status}): {message}")
+        self.status = status
+
+
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_F = ctypes.c_float
+
+# name -> argtypes (all return int32 status unless listed in _RESTYPES)
+SIGNATURES = {
+    "pars_gpu_create": [ctypes.POINTER(_P), _I32],
+    "pars_gpu_destroy": [_P],
+    "pars_gpu_last_error": [_P],
+    "pars_gpu_abi_version": [],
+    "pars_gpu_set_stream": [_P, _P],
+    "pars_gpu_synchronize": [_P],
+    "pars_gpu_memory_in_use": [_P, ctypes.POINTER(_I64)],
+    "pars_gpu_field_upload": [_P, _P, _P, _P, _P, _P, ctypes.POINTER(_I32)],
+    "pars_gpu_field_upload_device": [_P, _P, _P, _P, _P, _P, ctypes.POINTER(_I32)],
+    "pars_gpu_field_release": [_P, _I32],
+    "pars_gpu_field_info": [_P, _I32, _P, _P, _P, _P],
+    "pars_gpu_field_download": [_P, _I32, _P],
+    "pars_gpu_field_sample": [_P, _I32, _P, _I64, _P, _P],
+    "pars_gpu_seed_generate": [_P, _P, _P, _P, _I32, _I32, _P, _I64, ctypes.POINTER(_I64)],
+    "pars_gpu_partition": [_I32, _I32, _P, ctypes.POINTER(PartitionInfo)],
+    "pars_gpu_trace": [_P, _I32, _P, _I64, _I32, _I32, _F, ctypes.POINTER(TraceSummary)],
+    "pars_gpu_trace_device": [_P, _I32, _P, _I64, _I32, _I32, _F, ctypes.POINTER(TraceSummary)],
+    "pars_gpu_domain_create": [_P, _P, _P, _P, _I32, ctypes.POINTER(_I32)],
+    "pars_gpu_domain_release": [_P, _I32],
+    "pars_gpu_trace_domain": [_P, _I32, _P, _P, _I32, _I32, _F, ctypes.POINTER(TraceSummary)],
+    "pars_gpu_curves_index": [_P],
+    "pars_gpu_curves_color": [_P, _I32, _F],
+    "pars_gpu_curves_batch_info": [_P, _I64, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I32), ctypes.POINTER(_I32)],
+    "pars_gpu_curves_download": [_P, _I64, _P, _P, _P],
+    "pars_gpu_index_generate": [_P, _P, _I64, _P, ctypes.POINTER(_I64)],
+    "pars_gpu_color_generate": [_P, _P, _I64, _P, _I64, _I32, _F, _P],
+    "pars_gpu_flow_map_generate": [_P, _I32, _I32, _F, _I32, _I32, _F, ctypes.POINTER(_I32), ctypes.POINTER(_I64)],
+    "pars_gpu_ftle_generate": [_P, _I32, _F, _I32, _P],
+    "pars_gpu_ftle_device_pointer": [_P, ctypes.POINTER(_P), ctypes.POINTER(_I64)],
+    "pars_gpu_profile_enable": [_P, _I32],
+    "pars_gpu_profile_reset": [_P],
+    "pars_gpu_profile_get": [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)],
+    "pars_gpu_launch_count": [_P, ctypes.POINTER(_I64)],
+}
+_RESTYPES = {"pars_gpu_last_error": ctypes.c_char_p}
+
+_lib = None
+
+
+def library():
+    """Loads libpars_gpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIBRARY_PATH):
+            raise RuntimeError(f"{LIBRARY_PATH} is missing: build it with pars_gb300.build.build()")
+        lib = ctypes.CDLL(LIBRARY_PATH)
+        for name, args in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = _RESTYPES.get(name, _I32)
+        _lib = lib
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f3(v):
+    return np.ascontiguousarray(np.asarray(v, np.float32).reshape(3))
+
+
+def _i3(v):
+    return np.ascontiguousarray(np.asarray(v, np.int32).reshape(3))
+
+
+def partition(ranks, rank, domain_size):
+    """partitioner::set_domain_size as seen from `rank` (no context needed)."""
+    info = PartitionInfo()
+    d = _i3(domain_size)
+    status = library().pars_gpu_partition(ranks, rank, _ptr(d), ctypes.byref(info))
+    if status:
+        raise ParsGpuError(status, "pars_gpu_partition")
+    return {"grid": np.array(info.grid_size), "block": np.array(info.block_size),
+            "multi_rank": np.array(info.multi_rank), "offset": np.array(info.offset),
+            "ghosted": np.array(info.ghosted_block_size), "neighbors": np.array(info.neighbor_rank)}
+
+
+class Context:
+    """One pars_gpu context (device memory, stream, resident fields/curves)."""
+
+    def __init__(self, device=0):
+        self.lib = library()
+        handle = _P()
+        self._check(self.lib.pars_gpu_create(ctypes.byref(handle), device), "pars_gpu_create", use_context=False)
+        self.handle = handle
+
+    # -- plumbing -------------------------------------------------------------
+    def _check(self, status, what, use_context=True):
+        if status:
+            message = what
+            if use_context and getattr(self, "handle", None):
+                message += ": " + self.lib.pars_gpu_last_error(self.handle).decode()
+            raise ParsGpuError(status, message)
+
+    def _call(self, name, *args):
+        self._check(getattr(self.lib, name)(self.handle, *args), name)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.pars_gpu_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stream(self, stream_ptr):
+        self._call("pars_gpu_set_stream", stream_ptr)
+
+    def synchronize(self):
+        self._call("pars_gpu_synchronize")
+
+    def memory_in_use(self):
+        v = _I64()
+        self._call("pars_gpu_memory_in_use", ctypes.byref(v))
+        return v.value
+
+    # -- fields ------------------------------------------------------------------
+    def upload_field(self, field):
+        h = _I32()
+        self._call("pars_gpu_field_upload", _ptr(field.xyz), _ptr(field.dims), _ptr(field.offset), _ptr(field.size),
+                   _ptr(field.spacing), ctypes.byref(h))
+        return h.value
+
+    def upload_field_device(self, device_xyz_ptr, dims, offset, size, spacing):
+        h = _I32()
+        d, o, s, sp = _i3(dims), _f3(offset), _f3(size), _f3(spacing)
+        self._call("pars_gpu_field_upload_device", device_xyz_ptr, _ptr(d), _ptr(o), _ptr(s), _ptr(sp), ctypes.byref(h))
+        return h.value
+
+    def release_field(self, handle):
+        self._call("pars_gpu_field_release", handle)
+
+    def field_info(self, handle):
+        shape = np.zeros(3, np.int32)
+        offset, size, spacing = (np.zeros(3, np.float32) for _ in range(3))
+        self._call("pars_gpu_field_info", handle, _ptr(shape), _ptr(offset), _ptr(size), _ptr(spacing))
+        return {"shape": shape, "offset": offset, "size": size, "spacing": spacing}
+
+    def download_field(self, handle):
+        shape = self.field_info(handle)["shape"]
+        out = np.zeros(list(shape) + [3], np.float32)
+        self._call("pars_gpu_field_download", handle, _ptr(out))
+        return out
+
+    def sample(self, field, positions):
+        p = np.ascontiguousarray(positions, np.float32).reshape(-1, 4)
+        inside = np.zeros(len(p), np.uint8)
+        vel = np.zeros((len(p), 3), np.float32)
+        self._call("pars_gpu_field_sample", field, _ptr(p), len(p), _ptr(inside), _ptr(vel))
+        return inside.astype(bool), vel
+
+    # -- seeds -----------------------------------------------------------------------
+    def seed_generate(self, offset, size, stride, iterations, rank=0):
+        o, s, st = _f3(offset), _f3(size), _f3(stride)
+        n = _I64()
+        self._call("pars_gpu_seed_generate", _ptr(o), _ptr(s), _ptr(st), iterations, rank, None, 0, ctypes.byref(n))
+        out = np.zeros(n.value, PARTICLE_DTYPE)
+        if n.value:
+            self._call("pars_gpu_seed_generate", _ptr(o), _ptr(s), _ptr(st), iterations, rank, _ptr(out), n.value, ctypes.byref(n))
+        return out
+
+    # -- tracing ---------------------------------------------------------------------
+    def trace(self, field, particles, integrator=RUNGE_KUTTA_4, stage_mode=STAGES_FROZEN, step=0.01):
+        particles = np.ascontiguousarray(particles, PARTICLE_DTYPE)
+        s = TraceSummary()
+        self._call("pars_gpu_trace", field, _ptr(particles), len(particles), integrator, stage_mode, step, ctypes.byref(s))
+        return {"batches": s.batches, "vertices": s.vertices, "steps": s.steps, "rounds": s.rounds}
+
+    def trace_device(self, field, device_ptr, count, integrator=RUNGE_KUTTA_4, stage_mode=STAGES_FROZEN, step=0.01):
+        s = TraceSummary()
+        self._call("pars_gpu_trace_device", field, device_ptr, count, integrator, stage_mode, step, ctypes.byref(s))
+        return {"batches": s.batches, "vertices": s.vertices, "steps": s.steps, "rounds": s.rounds}
+
+    def domain_create(self, field, ranks):
+        h = _I32()
+        self._call("pars_gpu_domain_create", _ptr(field.xyz), _ptr(field.dims), _ptr(field.spacing), ranks, ctypes.byref(h))
+        return h.value
+
+    def domain_release(self, handle):
+        self._call("pars_gpu_domain_release", handle)
+
+    def trace_domain(self, domain, particles, seed_offsets, integrator=RUNGE_KUTTA_4, stage_mode=STAGES_FROZEN, step=0.01):
+        particles = np.ascontiguousarray(particles, PARTICLE_DTYPE)
+        offs = np.ascontiguousarray(seed_offsets, np.int64)
+        s = TraceSummary()
+        self._call("pars_gpu_trace_domain", domain, _ptr(particles), _ptr(offs), integrator, stage_mode, step, ctypes.byref(s))
+        return {"batches": s.batches, "vertices": s.vertices, "steps": s.steps, "rounds": s.rounds}
+
+    def curves_index(self):
+        self._call("pars_gpu_curves_index")
+
+    def curves_color(self, mode="rgb", parameter=0.5):
+        self._call("pars_gpu_curves_color", COLOR_MODES[mode] if isinstance(mode, str) else mode, parameter)
+
+    def batch_info(self, b):
+        nv, ni, r, rd = _I64(), _I64(), _I32(), _I32()
+        self._call("pars_gpu_curves_batch_info", b, ctypes.byref(nv), ctypes.byref(ni), ctypes.byref(r), ctypes.byref(rd))
+        return nv.value, ni.value, r.value, rd.value
+
+    def curves(self, batches, vertices=True, colors=False, indices=False):
+        """Downloads `batches` batches as dicts of numpy arrays."""
+        out = []
+        for b in range(batches):
+            nv, ni, rank, rnd = self.batch_info(b)
+            v = np.zeros((nv, 4), np.float32) if vertices else None
+            c = np.zeros((nv, 4), np.float32) if colors else None
+            i = np.zeros(ni, np.int32) if indices else None
+            self._call("pars_gpu_curves_download", b, _ptr(v), _ptr(c), _ptr(i))
+            out.append({"vertices": v, "colors": c, "indices": i, "rank": rank, "round": rnd})
+        return out
+
+    def index_generate(self, vertices):
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 4)
+        out = np.zeros(max(len(v), 1), np.int32)
+        n = _I64()
+        self._call("pars_gpu_index_generate", _ptr(v), len(v), _ptr(out), ctypes.byref(n))
+        return out[: n.value].copy()
+
+    def color_generate(self, vertices, indices, mode="rgb", parameter=0.5, colors=None):
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 4)
+        i = np.ascontiguousarray(indices, np.int32)
+        c = np.zeros_like(v) if colors is None else np.ascontiguousarray(colors, np.float32).reshape(-1, 4).copy()
+        self._call("pars_gpu_color_generate", _ptr(v), len(v), _ptr(i), len(i),
+                   COLOR_MODES[mode] if isinstance(mode, str) else mode, parameter, _ptr(c))
+        return c
+
+    # -- flow map / FTLE ------------------------------------------------------------------
+    def flow_map_generate(self, field, iterations, scale=1.0, integrator=RUNGE_KUTTA_4, stage_mode=STAGES_RESAMPLED, step=0.01):
+        h, steps = _I32(), _I64()
+        self._call("pars_gpu_flow_map_generate", field, iterations, scale, integrator, stage_mode, step, ctypes.byref(h), ctypes.byref(steps))
+        return h.value, steps.value
+
+    def ftle_generate(self, flow_map, time, mode=FTLE_REGULAR, shape=None, download=True, out=None):
+        """FTLE of a resident flow map; downloads into `out` (or a new array of
+        `shape`) unless download is False."""
+        if download and out is None:
+            out = np.zeros(shape, np.float32)
+        if not download:
+            out = None
+        self._call("pars_gpu_ftle_generate", flow_map, time, mode, _ptr(out))
+        return out
+
+    def ftle_device_pointer(self):
+        p, n = _P(), _I64()
+        self._call("pars_gpu_ftle_device_pointer", ctypes.byref(p), ctypes.byref(n))
+        return p.value, n.value
+
+    # -- instrumentation ----------------------------------------------------------------
+    def profile_enable(self, on=True):
+        self._call("pars_gpu_profile_enable", 1 if on else 0)
+
+    def profile_reset(self):
+        self._call("pars_gpu_profile_reset")
+
+    def profile_get(self, name):
+        ms, n = ctypes.c_double(), _I64()
+        self._call("pars_gpu_profile_get", name.encode(), ctypes.byref(ms), ctypes.byref(n))
+        return ms.value, n.value
+
+    def launch_count(self):
+        n = _I64()
+        self._call("pars_gpu_launch_count", ctypes.byref(n))
+        return n.value

@@ -1,0 +1,242 @@
+"""GPU parity: the sm_103a kernels, called through the C ABI, against the
+reference's golden fixtures and the CPU oracle on the same inputs.
+
+Bars (written out per test):
+* frozen-velocity tracing (the reference's scheme), field sampling, prune,
+  index generation, rgb colours, flow maps: bit-exact;
+* hsl/hsv colours: the reference calls the host libm's FP32 atan2/acos, the GPU
+  rounds FP64 atan2/acos to FP32, so a colour may differ by a few FP32 ulps:
+  |difference| <= 2e-6 (colours lie in [0, 1]).
+"""
+import numpy as np
+import pytest
+
+from conftest import assert_colors_equal, golden, golden_curves, golden_field, particles_from
+
+pytestmark = pytest.mark.gpu
+
+HSX_TOLERANCE = 2e-6
+
+
+def gpu_curves(ctx, summary, color=None, parameter=0.5):
+    ctx.curves_index()
+    if color:
+        ctx.curves_color(color, parameter)
+    return ctx.curves(summary["batches"], vertices=True, colors=bool(color), indices=True)
+
+
+def compare(got, expected, color_tolerance=0.0, check_colors=True):
+    assert len(got) == len(expected)
+    key = lambda b: (b["rank"], b["round"])
+    for a, e in zip(sorted(got, key=key), sorted(expected, key=key)):
+        assert (a["rank"], a["round"]) == (e["rank"], e["round"])
+        assert np.array_equal(a["vertices"], e["vertices"]), "vertices differ"
+        assert np.array_equal(a["indices"], e["indices"]), "indices differ"
+        if check_colors and e.get("colors") is not None:
+            assert_colors_equal(a["colors"], e["colors"], color_tolerance)
+
+
+def test_field_sampling_is_bit_exact(ctx):
+    g = golden("sample_abc24.npz")
+    f = golden_field(g)
+    h = ctx.upload_field(f)
+    inside, vel = ctx.sample(h, g["positions"])
+    assert np.array_equal(inside, g["inside"].astype(bool))
+    assert np.array_equal(vel, g["velocity"])
+    ctx.release_field(h)
+
+
+def test_sampling_near_cell_faces_matches_oracle(ctx, port):
+    """Positions a few ulps either side of every cell face: the floor of the
+    division and the exact fmod remainder decide cell and weight."""
+    from pars_gb300 import workloads as W
+    f = W.abc_field(33)
+    h = np.float32(f.spacing[0])
+    k = np.arange(33, dtype=np.float32)
+    faces = (k * h).astype(np.float32)
+    pts = []
+    for delta in range(-4, 5):
+        pts.append(np.nextafter(faces, np.float32(np.inf) if delta > 0 else np.float32(-np.inf)) if delta else faces)
+        for _ in range(abs(delta) - 1):
+            pts[-1] = np.nextafter(pts[-1], np.float32(np.inf) if delta > 0 else np.float32(-np.inf))
+    axis = np.concatenate(pts)
+    rng = np.random.default_rng(3)
+    n = len(axis)
+    pos = np.zeros((3 * n, 4), np.float32)
+    for a in range(3):
+        block = rng.uniform(0, 6.2, (n, 3)).astype(np.float32)
+        block[:, a] = axis
+        pos[a * n:(a + 1) * n, :3] = block
+    handle = ctx.upload_field(f)
+    gi, gv = ctx.sample(handle, pos)
+    oi, ov = port.field_sample(f, pos)
+    assert np.array_equal(gi, oi)
+    assert np.array_equal(gv, ov)
+    ctx.release_field(handle)
+
+
+def test_seed_generator_is_bit_exact(ctx):
+    g = golden("seeds.npz")
+    f = golden_field(golden("sample_abc24.npz"))
+    lattice = ctx.seed_generate(f.offset, f.size, g["lattice_stride"], 102, rank=3)
+    assert lattice.view(np.uint8).tobytes() == g["lattice"].tobytes()
+    odd = ctx.seed_generate(np.array([0.25, -1.0, 2.0]), np.array([1.0, 2.5, 0.7]), np.array([0.1, 0.3, 0.07]), 7, rank=1)
+    assert odd.view(np.uint8).tobytes() == g["odd"].tobytes()
+
+
+@pytest.mark.parametrize("integrator,name", [(2, "rk4"), (0, "euler")])
+def test_streamlines_match_reference_fixture(ctx, integrator, name):
+    g = golden("trace_abc24.npz")
+    h = ctx.upload_field(golden_field(g))
+    s = ctx.trace(h, particles_from(g, "seeds"), integrator, 0, 0.01)
+    got = gpu_curves(ctx, s, "rgb", 0.75)
+    compare(got, golden_curves(g, f"{name}_rgb_"))
+    ctx.release_field(h)
+
+
+@pytest.mark.parametrize("color", ["hsv_constant_s", "hsl_constant_l"])
+def test_streamline_hsx_colors_match_reference_fixture(ctx, color):
+    g = golden("trace_abc24.npz")
+    h = ctx.upload_field(golden_field(g))
+    s = ctx.trace(h, particles_from(g, "seeds"), 2, 0, 0.01)
+    got = gpu_curves(ctx, s, color, 0.75)
+    expected = golden_curves(g, f"rk4_{color}_")
+    base = golden_curves(g, "rk4_rgb_")
+    for e, b in zip(expected, base):
+        e["vertices"], e["indices"] = b["vertices"], b["indices"]
+    compare(got, expected, color_tolerance=HSX_TOLERANCE)
+    ctx.release_field(h)
+
+
+def test_streamline_edge_cases_match_reference_fixture(ctx):
+    g = golden("trace_abc24.npz")
+    h = ctx.upload_field(golden_field(g))
+    s = ctx.trace(h, particles_from(g, "edge_seeds"), 2, 0, 0.05)
+    compare(gpu_curves(ctx, s, "rgb"), golden_curves(g, "edge_"))
+    ctx.release_field(h)
+
+
+def test_zero_velocity_termination_matches_reference_fixture(ctx):
+    g = golden("trace_abc24.npz")
+    h = ctx.upload_field(golden_field(g, "zero_field_"))
+    s = ctx.trace(h, particles_from(g, "zero_seeds"), 2, 0, 0.02)
+    compare(gpu_curves(ctx, s, "hsv_constant_v", 0.6), golden_curves(g, "zero_"), color_tolerance=HSX_TOLERANCE)
+    ctx.release_field(h)
+
+
+def test_empty_particle_list(ctx):
+    g = golden("trace_abc24.npz")
+    h = ctx.upload_field(golden_field(g))
+    s = ctx.trace(h, particles_from(g, "seeds")[:0], 2, 0, 0.01)
+    assert s["batches"] == 0 and s["steps"] == 0
+    ctx.release_field(h)
+
+
+def test_plain_streamline_workload_matches_oracle(ctx, port):
+    """The 64^3 ABC workload (4096 seeds, 1000 RK4 steps): bit-exact vertices,
+    indices and rgb colours; hsv colours within the stated tolerance."""
+    from pars_gb300 import workloads as W
+    cfg = W.streamline_config()
+    f = cfg["field"]
+    seeds = port.seed_generate(f.offset, f.size, cfg["stride"], cfg["iterations"])
+    h = ctx.upload_field(f)
+    s = ctx.trace(h, seeds, 2, 0, cfg["step"])
+    expected = port.trace_single(f, seeds, 2, cfg["step"], "rgb", 0.75)
+    assert s["steps"] == expected.steps
+    compare(gpu_curves(ctx, s, "rgb"), expected.batches)
+    expected_hsv = port.trace_single(f, seeds, 2, cfg["step"], "hsv_constant_s", 0.75)
+    got = gpu_curves(ctx, s, "hsv_constant_s", 0.75)
+    compare(got, expected_hsv.batches, color_tolerance=HSX_TOLERANCE)
+    ctx.release_field(h)
+
+
+def test_batches_split_like_compute_round_info(ctx, port):
+    """P = 134219 particles with remaining_iterations 1000: 134217 fit a batch
+    ((INT32_MAX / 16) / 1000), so two batches, the second with 2 particles."""
+    from pars_gb300 import workloads as W
+    f = W.abc_field(16)
+    rng = np.random.default_rng(9)
+    n = 134219
+    seeds = np.zeros(n, port_dtype())
+    seeds["position"][:, :3] = rng.uniform(0.5, 5.5, (n, 3)).astype(np.float32)
+    seeds["remaining_iterations"] = 1000
+    seeds["vector_field_index"] = -1
+    h = ctx.upload_field(f)
+    s = ctx.trace(h, seeds, 2, 0, 0.05)
+    assert s["batches"] == 2
+    got = gpu_curves(ctx, s, "rgb")
+    expected = port.trace_single(f, seeds, 2, 0.05, "rgb", 0.5)
+    compare(got, expected.batches)
+    ctx.release_field(h)
+
+
+def port_dtype():
+    import oracle
+    return oracle.PARTICLE_DTYPE
+
+
+def test_partitioned_domain_matches_reference_fixture(ctx):
+    g = golden("multi_abc17.npz")
+    d = ctx.domain_create(golden_field(g), int(g["ranks"]))
+    s = ctx.trace_domain(d, particles_from(g, "seeds"), g["seed_offsets"], 2, 0, 0.01)
+    assert s["rounds"] > 1
+    compare(gpu_curves(ctx, s, "rgb"), golden_curves(g, "multi_"))
+    ctx.domain_release(d)
+
+
+def test_partitioned_domain_matches_oracle_64_blocks(ctx, port):
+    """4x4x4 blocks on one GPU with on-device handoff queues: identical to the
+    oracle's round-by-round exchange (same per-block particle order)."""
+    from pars_gb300 import workloads as W
+    f = W.abc_field(49)
+    ranks = 64
+    info = port.partition(ranks, 0, f.dims)
+    rng = np.random.default_rng(2)
+    n = 6000
+    centres = rng.uniform(1.0, 5.3, (4, 3))
+    p = (centres[rng.integers(0, 4, n)] + rng.normal(0, 0.05 * 2 * np.pi, (n, 3))).clip(0, 6.2).astype(np.float32)
+    extent = (f.spacing * info["block"]).astype(np.float32)
+    multi = np.minimum((p / extent).astype(np.int64), info["grid"] - 1)
+    owner = (multi[:, 0] * info["grid"][1] + multi[:, 1]) * info["grid"][2] + multi[:, 2]
+    order = np.argsort(owner, kind="stable")
+    seeds = np.zeros(n, port_dtype())
+    seeds["position"][:, :3] = p[order]
+    seeds["remaining_iterations"] = 402
+    seeds["vector_field_index"] = -1
+    offsets = np.concatenate([[0], np.cumsum(np.bincount(owner, minlength=ranks))]).astype(np.int64)
+    d = ctx.domain_create(f, ranks)
+    s = ctx.trace_domain(d, seeds, offsets, 2, 0, 0.01)
+    expected = port.trace_multi(f, ranks, offsets, seeds, 2, 0.01, "rgb", 0.5)
+    assert s["steps"] == expected.steps
+    compare(gpu_curves(ctx, s, "rgb"), expected.batches)
+    ctx.domain_release(d)
+
+
+@pytest.mark.parametrize("key,iterations,scale,integrator,step", [
+    ("rk4_s1", 61, 1.0, 2, 0.01), ("euler_s1", 31, 1.0, 0, 0.02), ("rk4_s05", 41, 0.5, 2, 0.01)])
+def test_frozen_flow_map_matches_reference_fixture(ctx, key, iterations, scale, integrator, step):
+    import ctypes
+    g = golden("flow_abc16.npz")
+    h = ctx.upload_field(golden_field(g))
+    fm, steps = ctx.flow_map_generate(h, iterations, scale, integrator, 0, step)
+    expected = g[key]
+    info = ctx.field_info(fm)
+    assert tuple(info["shape"]) == expected.shape[:3]
+    assert np.array_equal(info["spacing"], (golden_field(g).spacing / np.float32(scale)).astype(np.float32))
+    assert np.array_equal(ctx.download_field(fm), expected)
+    assert steps > 0
+    ctx.release_field(fm)
+    ctx.release_field(h)
+
+
+def test_stage_buffers_match_reference_fixture(ctx):
+    g = golden("index_color.npz")
+    v = g["vertices"]
+    idx = ctx.index_generate(v)
+    assert np.array_equal(idx, g["indices"])
+    for mode in ("rgb", "hsv_constant_s", "hsl_constant_l", "hsl_constant_s", "hsv_constant_v"):
+        c = ctx.color_generate(v, idx, mode, 0.3, colors=np.full_like(v, np.nan))
+        assert_colors_equal(c, g["colors_" + mode], 0.0 if mode == "rgb" else HSX_TOLERANCE)
+    assert len(ctx.index_generate(np.tile(np.array([-2, -2, -2, 0], np.float32), (5, 1)))) == 0
+    assert np.array_equal(ctx.index_generate(v[:2]), g["two_indices"])
+    assert len(ctx.index_generate(v[:1])) == 0
