@@ -177,7 +177,7 @@ class Port(_Lib):
         L.orc_flow_map.restype = _LL
         L.orc_flow_map.argtypes = [_P] * 5 + [_I, _F, _I, _F, _LL, _LL, _P]
         L.orc_advect_fp64.restype = None
-        L.orc_advect_fp64.argtypes = [_P] * 5 + [_P, _LL, _I, _I, _D, _LL, _P, _P, _P]
+        L.orc_advect_fp64.argtypes = [_P] * 5 + [_P, _LL, _I, _I, _D, _LL, _P, _P, _P, _D, ctypes.c_ulonglong]
         L.orc_ftle_fp64.restype = None
         L.orc_ftle_fp64.argtypes = [_P, _P, _P, _D, _P]
         L.orc_largest_eigenvalue.restype = None
@@ -202,15 +202,32 @@ class Port(_Lib):
         steps = self.lib.orc_flow_map(*field.ctypes_args(), iterations, scale, integrator, step, first, count, _ptr(flow))
         return flow, steps
 
-    def advect_fp64(self, field, start, max_steps, integrator=2, mode=1, step=0.01, keep_vertices=False):
+    def advect_fp64(self, field, start, max_steps, integrator=2, mode=1, step=0.01, keep_vertices=False, noise=0.0, seed=0):
+        """FP64 advection on the FP32 grid values (mode 1: classical RK4 with
+        re-sampled stages).  noise > 0: per-step relative perturbation of that
+        size (conditioning ensembles)."""
         start = np.ascontiguousarray(start, np.float64).reshape(-1, 3)
         n = len(start)
         end = np.zeros_like(start)
         steps = np.zeros(n, np.int64)
         verts = np.full((n, max_steps + 1, 3), np.nan) if keep_vertices else None
         self.lib.orc_advect_fp64(*field.ctypes_args(), _ptr(start), n, integrator, mode, step, max_steps,
-                                 _ptr(end), _ptr(steps), _ptr(verts))
+                                 _ptr(end), _ptr(steps), _ptr(verts), noise, seed)
         return end, steps, verts
+
+    def conditioning(self, field, start, max_steps, integrator=2, step=0.01, noise=6e-8, members=4):
+        """Per-particle spread of FP64 end points under per-step relative noise
+        `noise` (the size of FP32 rounding): max over `members` runs of the
+        distance to the unperturbed FP64 end point, and whether every member
+        took the unperturbed step count."""
+        clean, steps, _ = self.advect_fp64(field, start, max_steps, integrator, 1, step)
+        spread = np.zeros(len(clean))
+        same = np.ones(len(clean), bool)
+        for m in range(members):
+            e, s, _ = self.advect_fp64(field, start, max_steps, integrator, 1, step, noise=noise, seed=m + 1)
+            spread = np.maximum(spread, np.linalg.norm(e - clean, axis=1))
+            same &= s == steps
+        return clean, steps, spread, same
 
     def ftle_fp64(self, flow, spacing, time):
         flow = np.ascontiguousarray(flow, np.float32)

@@ -465,10 +465,10 @@ long long ravel(const int idx[3], const int dims[3])           // index.hpp:20-2
 // ---------------------------------------------------------------------------
 // FP64 field sampling on the FP32 grid values (true RK4 oracle)
 // ---------------------------------------------------------------------------
-// Same cell/weight convention as the FP32 path, evaluated in FP64.  Stage
-// points outside the grid are sampled with the cell index clamped to
-// [0, shape-2] and the weight clamped to 0 or 1 (constant extension of the
-// boundary values).
+// Trilinear interpolation with a consistent cell / weight pair: the cell is the
+// floor quotient s and the weight (d - s h) / h lies in [0, 1).  Points outside
+// the grid use the cell index clamped to [0, shape-2] and the weight clamped to
+// 0 or 1 (constant extension of the boundary values).
 inline void interpolate_fp64(const field& f, const double* p, double* out)
 {
   long long index[3];
@@ -477,10 +477,13 @@ inline void interpolate_fp64(const field& f, const double* p, double* out)
   {
     const double h = f.spacing[i];
     const double d = p[i] - double(f.offset[i]);
-    const double s = std::floor(d / h);
+    double s = std::floor(d / h);
+    double r = d - s * h;
+    if (r < 0.0) { s -= 1.0; r = d - s * h; }
+    else if (r >= h) { s += 1.0; r = d - s * h; }
     if (!(s >= 0.0)) { index[i] = 0; weight[i] = 0.0; }
     else if (s > double(f.shape[i] - 2)) { index[i] = f.shape[i] - 2; weight[i] = 1.0; }
-    else { index[i] = (long long)s; weight[i] = std::fmod(d, h) / h; }
+    else { index[i] = (long long)s; weight[i] = r / h; }
   }
   const long long x = index[0], y = index[1], z = index[2];
   for (int c = 0; c < 3; ++c)
@@ -843,10 +846,13 @@ long long orc_flow_map(const float* xyz, const int dims[3], const float offset[3
 // steps).  mode 0 = frozen velocity, 1 = re-sampled stages (classical RK4).
 // When `vertices` is not null it receives, per particle, max_steps + 1 slots
 // (xyz, FP64): the start and every step; unused slots are left untouched.
-// steps_out receives the steps each particle took.
+// steps_out receives the steps each particle took.  noise > 0 multiplies each
+// new position coordinate by (1 + noise * N(0,1)) (a seeded per-particle
+// generator): an ensemble of such runs measures how far rounding at that
+// relative level can move an end point, i.e. the problem's conditioning.
 void orc_advect_fp64(const float* xyz, const int dims[3], const float offset[3], const float size[3], const float spacing[3],
                      const double* start, long long n, int integrator, int mode, double step, long long max_steps,
-                     double* end, long long* steps_out, double* vertices)
+                     double* end, long long* steps_out, double* vertices, double noise, unsigned long long seed)
 {
   field f {xyz, {dims[0], dims[1], dims[2]}, {offset[0], offset[1], offset[2]}, {size[0], size[1], size[2]}, {spacing[0], spacing[1], spacing[2]}};
   #pragma omp parallel for schedule(dynamic, 16)
@@ -855,6 +861,15 @@ void orc_advect_fp64(const float* xyz, const int dims[3], const float offset[3],
     double x[3] = {start[3 * i], start[3 * i + 1], start[3 * i + 2]};
     double* track = vertices ? vertices + 3 * (max_steps + 1) * i : nullptr;
     if (track) std::memcpy(track, x, 24);
+    // splitmix64 stream per particle; Box-Muller normals.
+    unsigned long long state = seed * 0x9E3779B97F4A7C15ULL + (unsigned long long)i * 0xD1B54A32D192ED03ULL + 1;
+    auto uniform = [&state]() {
+      unsigned long long z = (state += 0x9E3779B97F4A7C15ULL);
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+      z ^= z >> 31;
+      return (double(z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    };
     long long s = 0;
     for (; s < max_steps; ++s)
     {
@@ -864,6 +879,12 @@ void orc_advect_fp64(const float* xyz, const int dims[3], const float offset[3],
       if (is_zero_fp64(k1)) break;
       double next[3];
       step_fp64(f, integrator, mode, step, x, k1, next);
+      if (noise > 0.0)
+        for (int c = 0; c < 3; ++c)
+        {
+          const double g = std::sqrt(-2.0 * std::log(uniform())) * std::cos(6.283185307179586 * uniform());
+          next[c] *= 1.0 + noise * g;
+        }
       std::memcpy(x, next, 24);
       if (track) std::memcpy(track + 3 * (s + 1), x, 24);
     }

@@ -90,6 +90,7 @@ struct field_entry
     v.ox = offset[0]; v.oy = offset[1]; v.oz = offset[2];
     v.hx = spacing[0]; v.hy = spacing[1]; v.hz = spacing[2];
     v.maxx = offset[0] + size[0]; v.maxy = offset[1] + size[1]; v.maxz = offset[2] + size[2];
+    v.inv_hx = 1.0f / spacing[0]; v.inv_hy = 1.0f / spacing[1]; v.inv_hz = 1.0f / spacing[2];
     return v;
   }
 };

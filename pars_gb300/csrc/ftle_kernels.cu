@@ -31,6 +31,7 @@ struct flow_map_args
   unsigned long long* steps;
 };
 
+template <bool FROZEN>
 __global__ void __launch_bounds__(256) flow_map_kernel(const flow_map_args a)
 {
   const long long total = (long long)a.px * a.py * a.pz;
@@ -44,12 +45,15 @@ __global__ void __launch_bounds__(256) flow_map_kernel(const flow_map_args a)
     float4 pos = make_float4(__fadd_rn(a.ox, __fmul_rn(a.sx, float(ix))), __fadd_rn(a.oy, __fmul_rn(a.sy, float(iy))),
                              __fadd_rn(a.oz, __fmul_rn(a.sz, float(iz))), 0.0f);
     bool finished = false;
+    float3 lo = make_float3(0.0f, 0.0f, 0.0f);
     for (int it = 1; it < a.iterations; ++it)
     {
       float3 v;
-      if (!sample_inside(a.f, pos, v)) { finished = true; break; }
+      const bool inside = FROZEN ? sample_inside(a.f, pos, v) : sample_inside_resampled(a.f, pos, v);
+      if (!inside) { finished = true; break; }
       if (is_zero(v)) { finished = true; break; }
-      pos = take_step(a.f, a.rule, pos, v);
+      if (FROZEN) pos = frozen_step(a.rule, pos, v);
+      else resampled_step(a.f, a.rule, pos, lo, v);
       ++steps;
       if (it + 1 == a.iterations) { finished = true; break; }
     }
@@ -166,7 +170,8 @@ void launch_flow_map(pars_gpu_context& ctx, const field_view& f, const step_rule
   const long long total = (long long)a.px * a.py * a.pz;
   if (total <= 0) return;
   launch_scope scope(ctx, "advect_flow_map");
-  flow_map_kernel<<<(unsigned)((total + 127) / 128), 128, 0, ctx.stream>>>(a);
+  if (rule.frozen) flow_map_kernel<true><<<(unsigned)((total + 127) / 128), 128, 0, ctx.stream>>>(a);
+  else             flow_map_kernel<false><<<(unsigned)((total + 127) / 128), 128, 0, ctx.stream>>>(a);
 }
 
 void launch_ftle(pars_gpu_context& ctx, const field_view& flow, double time, int mode, float* out)

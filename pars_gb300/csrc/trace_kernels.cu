@@ -15,6 +15,10 @@ namespace
 {
 constexpr unsigned full_mask = 0xffffffffu;
 
+// FROZEN = true: the reference's scheme and FP32 operation order (bit-exact).
+// FROZEN = false: re-sampled stages, consistent cell weights, compensated
+// position accumulation.
+template <bool FROZEN>
 __global__ void __launch_bounds__(256) trace_kernel(const trace_launch a)
 {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -36,11 +40,13 @@ __global__ void __launch_bounds__(256) trace_kernel(const trace_launch a)
     int written = 1;
     int kept = is_invalid_vertex(last) ? 0 : 1;
     const float4 term = termination_vertex();
+    float3 lo = make_float3(0.0f, 0.0f, 0.0f);
     for (int it = 1; it < N; ++it)
     {
       if (it == N - 1) { out[it] = term; ++written; ++kept; break; }
       float3 v;
-      if (!sample_inside(f, last, v))
+      const bool inside = FROZEN ? sample_inside(f, last, v) : sample_inside_resampled(f, last, v);
+      if (!inside)
       {
         out[it] = term; ++written; ++kept;
         if (a.route_exits)
@@ -57,7 +63,9 @@ __global__ void __launch_bounds__(256) trace_kernel(const trace_launch a)
         break;
       }
       if (is_zero(v)) { out[it] = term; ++written; ++kept; break; }
-      const float4 next = take_step(f, a.rule, last, v);
+      float4 next;
+      if (FROZEN) next = frozen_step(a.rule, last, v);
+      else { next = last; resampled_step(f, a.rule, next, lo, v); }
       out[it] = next;
       ++written;
       kept += is_invalid_vertex(next) ? 0 : 1;
@@ -193,7 +201,8 @@ void launch_trace(pars_gpu_context& ctx, const trace_launch& a)
   if (a.count <= 152LL * 128) threads = 32;
   else if (a.count <= 152LL * 256) threads = 64;
   launch_scope scope(ctx, "trace_streamlines");
-  trace_kernel<<<grid_for(a.count, threads), threads, 0, ctx.stream>>>(a);
+  if (a.rule.frozen) trace_kernel<true><<<grid_for(a.count, threads), threads, 0, ctx.stream>>>(a);
+  else               trace_kernel<false><<<grid_for(a.count, threads), threads, 0, ctx.stream>>>(a);
 }
 
 void launch_compact_vertices(pars_gpu_context& ctx, const float4* slots, long long slot_stride, const int* written,
