@@ -163,6 +163,12 @@ struct pars_gpu_context
                                           tile_offsets, staging, boundary_positions, boundary_offsets, single_block;
   pars::device_buffer                     ftle;
   long long                               ftle_count = 0;
+  // Released field buffers kept for reuse (bytes -> buffer), so that a caller
+  // that uploads, traces and releases every request does not pay cudaMalloc /
+  // cudaFree (and their device-wide synchronisation) each time.
+  std::multimap<std::size_t, pars::device_buffer> buffer_cache;
+  std::size_t                             buffer_cache_bytes = 0;
+  static constexpr std::size_t            buffer_cache_limit = std::size_t(8) << 30;
   // instrumentation
   bool                                    profile = false;
   std::map<std::string, pars::profile_entry> profile_totals;
@@ -186,6 +192,12 @@ private:
   const char*       name_;
   cudaEvent_t       start_ = nullptr;
 };
+
+// A device buffer of at least `bytes` (at most twice that) from the context's
+// cache, or a new allocation.
+device_buffer acquire_buffer(pars_gpu_context& ctx, std::size_t bytes);
+// Returns a buffer to the cache (freed instead when the cache is full).
+void recycle_buffer(pars_gpu_context& ctx, device_buffer&& buffer);
 
 // Kernel launchers (defined in the *_kernels.cu translation units).
 void launch_pack_field(pars_gpu_context& ctx, const float* xyz, float4* out, long long count);

@@ -26,11 +26,49 @@ long long pars_gpu_context::held_bytes() const
                                     &tile_offsets, &staging, &ftle, &curves.vertices, &curves.colors,
                                     &curves.indices, &boundary_positions, &boundary_offsets};
   for (auto* b : scratch) total += (long long)b->bytes();
-  return total;
+  return total + (long long)buffer_cache_bytes + (long long)single_block.bytes();
 }
 
 namespace pars
 {
+device_buffer acquire_buffer(pars_gpu_context& ctx, std::size_t bytes)
+{
+  auto it = ctx.buffer_cache.lower_bound(bytes);
+  if (it != ctx.buffer_cache.end() && it->first <= 2 * bytes)
+  {
+    device_buffer b = std::move(it->second);
+    ctx.buffer_cache_bytes -= it->first;
+    ctx.buffer_cache.erase(it);
+    return b;
+  }
+  device_buffer b;
+  try { b.reserve(bytes); }
+  catch (const error&)
+  {
+    // Out of memory: give the cache back to the device and try once more.
+    PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+    ctx.buffer_cache.clear();
+    ctx.buffer_cache_bytes = 0;
+    b.reserve(bytes);
+  }
+  return b;
+}
+
+void recycle_buffer(pars_gpu_context& ctx, device_buffer&& buffer)
+{
+  const std::size_t bytes = buffer.bytes();
+  if (bytes == 0) return;
+  if (ctx.buffer_cache_bytes + bytes > pars_gpu_context::buffer_cache_limit)
+  {
+    // Work still queued may read the buffer: free it only after the stream drains.
+    PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+    buffer.release();
+    return;
+  }
+  ctx.buffer_cache_bytes += bytes;
+  ctx.buffer_cache.emplace(bytes, std::move(buffer));
+}
+
 launch_scope::launch_scope(pars_gpu_context& ctx, const char* name) : ctx_(ctx), name_(name)
 {
   ++ctx_.launches;
@@ -480,7 +518,7 @@ int32_t pars_gpu_field_upload(pars_gpu_context* ctx, const float* xyz, const int
     auto entry = make_field(shape, offset, size, spacing);
     const long long count = (long long)shape[0] * shape[1] * shape[2];
     ctx->staging.reserve(sizeof(float) * 3 * count);
-    entry->data.reserve(sizeof(float4) * count);
+    entry->data = acquire_buffer(*ctx, sizeof(float4) * count);
     PARS_CUDA(cudaMemcpyAsync(ctx->staging.get(), xyz, sizeof(float) * 3 * count, cudaMemcpyHostToDevice, ctx->stream));
     launch_pack_field(*ctx, ctx->staging.as<const float>(), entry->data.as<float4>(), count);
     *field = add_field(*ctx, std::move(entry));
@@ -495,7 +533,7 @@ int32_t pars_gpu_field_upload_device(pars_gpu_context* ctx, const float* device_
     check_field_args(shape, spacing);
     auto entry = make_field(shape, offset, size, spacing);
     const long long count = (long long)shape[0] * shape[1] * shape[2];
-    entry->data.reserve(sizeof(float4) * count);
+    entry->data = acquire_buffer(*ctx, sizeof(float4) * count);
     launch_pack_field(*ctx, device_xyz, entry->data.as<float4>(), count);
     *field = add_field(*ctx, std::move(entry));
   });
@@ -506,7 +544,12 @@ int32_t pars_gpu_field_release(pars_gpu_context* ctx, int32_t field)
   return guarded(ctx, [&] {
     auto it = ctx->fields.find(field);
     if (it == ctx->fields.end()) throw error(PARS_ERR_NOT_FOUND, "no field with handle " + std::to_string(field));
-    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (auto& d : ctx->domains)
+      for (int f : d.second->fields)
+        if (f == field) throw error(PARS_ERR_STATE, "field belongs to a domain; release the domain instead");
+    // Work queued on the context's stream may still read the buffer; anything
+    // that reuses it is queued behind that work on the same stream.
+    recycle_buffer(*ctx, std::move(it->second->data));
     ctx->fields.erase(it);
   });
 }
@@ -642,7 +685,7 @@ int32_t pars_gpu_domain_create(pars_gpu_context* ctx, const float* xyz, const in
         f->size[i] = float(info.block_size[i]) * spacing[i];        // data_io.cpp:114
       }
       for (int i = 0; i < 3; ++i) PARS_REQUIRE(f->shape[i] >= 2, "blocks must be at least 2 voxels wide");
-      f->data.reserve(sizeof(float4) * (std::size_t)f->shape[0] * f->shape[1] * f->shape[2]);
+      f->data = acquire_buffer(*ctx, sizeof(float4) * (std::size_t)f->shape[0] * f->shape[1] * f->shape[2]);
       launch_extract_block(*ctx, ctx->staging.as<const float>(), domain_size, info.offset, f->shape, f->data.as<float4>());
       trace_block b;
       b.field = f->view();
@@ -665,7 +708,13 @@ int32_t pars_gpu_domain_release(pars_gpu_context* ctx, int32_t domain)
     auto it = ctx->domains.find(domain);
     if (it == ctx->domains.end()) throw error(PARS_ERR_NOT_FOUND, "no domain with handle " + std::to_string(domain));
     PARS_CUDA(cudaStreamSynchronize(ctx->stream));
-    for (int f : it->second->fields) ctx->fields.erase(f);
+    for (int f : it->second->fields)
+    {
+      auto fit = ctx->fields.find(f);
+      if (fit == ctx->fields.end()) continue;
+      recycle_buffer(*ctx, std::move(fit->second->data));
+      ctx->fields.erase(fit);
+    }
     ctx->domains.erase(it);
   });
 }
@@ -832,9 +881,11 @@ int32_t pars_gpu_flow_map_generate(pars_gpu_context* ctx, int32_t field, int32_t
       PARS_REQUIRE(entry->shape[i] >= 1, "flow map would be empty");
     }
     const long long voxels = (long long)entry->shape[0] * entry->shape[1] * entry->shape[2];
-    entry->data.reserve(sizeof(float4) * voxels);
-    // Voxels no seed reaches stay NaN (the reference leaves them unassigned).
-    PARS_CUDA(cudaMemsetAsync(entry->data.get(), 0xff, sizeof(float4) * voxels, ctx->stream));
+    entry->data = acquire_buffer(*ctx, sizeof(float4) * voxels);
+    // Voxels no seed reaches stay NaN (the reference leaves them unassigned);
+    // when the seed lattice covers the flow map every voxel is written.
+    if (seeds[0] < entry->shape[0] || seeds[1] < entry->shape[1] || seeds[2] < entry->shape[2])
+      PARS_CUDA(cudaMemsetAsync(entry->data.get(), 0xff, sizeof(float4) * voxels, ctx->stream));
     ctx->counters.reserve(sizeof(unsigned long long) * 2);
     auto* counter = ctx->counters.as<unsigned long long>();
     PARS_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
