@@ -232,6 +232,34 @@ int32_t pars_gpu_flow_map_generate(pars_gpu_context* context, int32_t field, int
 int32_t pars_gpu_ftle_generate    (pars_gpu_context* context, int32_t flow_map, float time, int32_t mode, float* ftle);
 int32_t pars_gpu_ftle_device_pointer(pars_gpu_context* context, const float** device_ftle, int64_t* count);
 
+/* ---- allocation-free FTLE --------------------------------------------------------
+ * No counterpart in the reference.  For callers that may not allocate device
+ * memory: plugins running inside a host application that owns the GPU's
+ * memory budget (an in-situ simulation, a renderer), and paths where the
+ * implicit synchronisation of cudaMalloc / cudaFree is not acceptable.  It
+ * needs no context and calls no cudaMalloc, cudaFree or allocating library
+ * routine: the flow map and the float4 copy of the field live in one static
+ * device array of this library (8 MiB, held on every GPU that loads the
+ * library until the process exits).
+ *
+ * Computes what pars_gpu_field_upload_device + pars_gpu_flow_map_generate
+ * (resolution scale 1) + pars_gpu_ftle_generate compute, on the CURRENT CUDA
+ * device and `stream` (a cudaStream_t, NULL = default stream): device_xyz is
+ * the field in DEVICE memory ([shape0][shape1][shape2][3] FP32), device_ftle
+ * receives shape0*shape1*shape2 FP32 values in DEVICE memory, and
+ * device_steps (DEVICE int64, may be NULL) the particle-steps taken.
+ * Limit: shape0*shape1*shape2 <= 262144 (64^3); larger fields return
+ * PARS_ERR_BUDGET.  size / spacing must give at least shape seeds per axis.
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU
+ * (different streams or threads without ordering between them) race and
+ * corrupt each other's results; order them on one stream. */
+int32_t pars_gpu_ftle_no_alloc(const float* device_xyz, const int32_t shape[3], const float offset[3], const float size[3],
+                               const float spacing[3], int32_t iterations, int32_t integrator, int32_t stage_mode,
+                               float step_size, float time, int32_t mode, float* device_ftle, int64_t* device_steps,
+                               void* stream);
+
 /* ---- instrumentation ---------------------------------------------------------- */
 /* When enabled, each kernel launch is bracketed by CUDA events on the launch
  * stream and its time is accumulated per kernel name. */

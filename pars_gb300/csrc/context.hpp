@@ -199,6 +199,10 @@ device_buffer acquire_buffer(pars_gpu_context& ctx, std::size_t bytes);
 // Returns a buffer to the cache (freed instead when the cache is full).
 void recycle_buffer(pars_gpu_context& ctx, device_buffer&& buffer);
 
+// Integrator parameters for (integrator, stage mode, step size); throws
+// pars::error for integrators the kernels do not implement.
+step_rule make_step_rule(int integrator, int stage_mode, float h);
+
 // Kernel launchers (defined in the *_kernels.cu translation units).
 void launch_pack_field(pars_gpu_context& ctx, const float* xyz, float4* out, long long count);
 void launch_unpack_field(pars_gpu_context& ctx, const float4* data, float* xyz, long long count);

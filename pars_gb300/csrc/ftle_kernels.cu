@@ -187,4 +187,124 @@ void launch_ftle(pars_gpu_context& ctx, const field_view& flow, double time, int
   launch_scope scope(ctx, "ftle_fused");
   ftle_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx.stream>>>(a);
 }
+
+// ---- Allocation-free FTLE ------------------------------------------------------
+// pars_gpu_ftle_no_alloc (declared in pars_gpu.h) runs the same pack, flow-map
+// and FTLE kernels as the context path, but keeps its scratch — the float4
+// copy of the field, the flow map, and the step counter — in the one
+// file-scope device array below instead of allocating it.  Every GPU that
+// loads this library holds the array (no_alloc_max_voxels * 32 bytes + 256,
+// 8 MiB) until the process exits.
+namespace
+{
+constexpr long long no_alloc_max_voxels = 1LL << 18;   // 64^3
+constexpr long long no_alloc_entries = 2 * no_alloc_max_voxels + 16;   // field | flow map | counter
+static __device__ __align__(256) float4 no_alloc_scratch[no_alloc_entries];
+
+__global__ void pack_into_scratch_kernel(const float* __restrict__ xyz, float4* __restrict__ out, long long count)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) out[i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.0f);
 }
+
+__global__ void steps_to_int64_kernel(const unsigned long long* __restrict__ counter, int64_t* __restrict__ out)
+{
+  *out = (int64_t)*counter;
+}
+
+// Host code must not use the array's name as a device address: it is a host
+// stand-in.  The device address is looked up once per device, with that device
+// current, and cached; later calls on the device reuse it.
+constexpr int no_alloc_max_devices = 64;
+std::mutex no_alloc_mutex;
+float4* no_alloc_address[no_alloc_max_devices] = {};
+
+int32_t no_alloc_scratch_address(int device, float4** out)
+{
+  if (device < 0 || device >= no_alloc_max_devices) return PARS_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(no_alloc_mutex);
+  if (!no_alloc_address[device])
+  {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, no_alloc_scratch) != cudaSuccess) { (void)cudaGetLastError(); return PARS_ERR_CUDA; }
+    no_alloc_address[device] = static_cast<float4*>(p);
+  }
+  *out = no_alloc_address[device];
+  return PARS_OK;
+}
+}
+}
+
+#pragma GCC visibility push(default)
+extern "C" int32_t pars_gpu_ftle_no_alloc(const float* device_xyz, const int32_t shape[3], const float offset[3], const float size[3],
+                                          const float spacing[3], int32_t iterations, int32_t integrator, int32_t stage_mode,
+                                          float step_size, float time, int32_t mode, float* device_ftle, int64_t* device_steps,
+                                          void* stream)
+{
+  using namespace pars;
+  if (!device_xyz || !shape || !offset || !size || !spacing || !device_ftle) return PARS_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < 3; ++i)
+    if (shape[i] < 2 || !(spacing[i] > 0.0f)) return PARS_ERR_INVALID_ARGUMENT;
+  if (mode != PARS_FTLE_REGULAR && mode != PARS_FTLE_FRACTIONAL_ANISOTROPY) return PARS_ERR_INVALID_ARGUMENT;
+  if (time == 0.0f) return PARS_ERR_INVALID_ARGUMENT;
+  const long long voxels = (long long)shape[0] * shape[1] * shape[2];
+  if (voxels > no_alloc_max_voxels) return PARS_ERR_BUDGET;   // larger than the static scratch
+  step_rule rule;
+  try { rule = make_step_rule(integrator, stage_mode, step_size); }
+  catch (const error& e) { return e.status; }
+  // Flow map at the field's own resolution (resolution scale 1): one seed per
+  // vertex (seed_generator.cpp:11), so every flow-map voxel is written and the
+  // flow-map part of the scratch needs no clearing.
+  int seeds[3];
+  for (int i = 0; i < 3; ++i)
+  {
+    const float q = size[i] / spacing[i];
+    seeds[i] = (q > 0.0f && q < 2147483647.0f) ? int(q) : 0;
+    if (seeds[i] < shape[i]) return PARS_ERR_INVALID_ARGUMENT;
+  }
+
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) { (void)cudaGetLastError(); return PARS_ERR_CUDA; }
+  float4* scratch = nullptr;
+  const int32_t status = no_alloc_scratch_address(device, &scratch);
+  if (status != PARS_OK) return status;
+  float4* field_data = scratch;
+  float4* flow = scratch + no_alloc_max_voxels;
+  auto* counter = reinterpret_cast<unsigned long long*>(scratch + 2 * no_alloc_max_voxels);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+  field_view f;
+  f.data = field_data;
+  f.nx = shape[0]; f.ny = shape[1]; f.nz = shape[2];
+  f.ox = offset[0]; f.oy = offset[1]; f.oz = offset[2];
+  f.hx = spacing[0]; f.hy = spacing[1]; f.hz = spacing[2];
+  f.maxx = offset[0] + size[0]; f.maxy = offset[1] + size[1]; f.maxz = offset[2] + size[2];
+  f.inv_hx = 1.0f / spacing[0]; f.inv_hy = 1.0f / spacing[1]; f.inv_hz = 1.0f / spacing[2];
+
+  // The counter keeps the previous call's value: clear it first.
+  if (cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s) != cudaSuccess) { (void)cudaGetLastError(); return PARS_ERR_CUDA; }
+  pack_into_scratch_kernel<<<(unsigned)((voxels + 255) / 256), 256, 0, s>>>(device_xyz, field_data, voxels);
+
+  flow_map_args a;
+  a.f = f; a.rule = rule; a.iterations = iterations;
+  a.ox = offset[0]; a.oy = offset[1]; a.oz = offset[2];
+  a.sx = spacing[0]; a.sy = spacing[1]; a.sz = spacing[2];
+  a.px = seeds[0]; a.py = seeds[1]; a.pz = seeds[2];
+  a.fx = shape[0]; a.fy = shape[1]; a.fz = shape[2];
+  a.flow = flow; a.steps = counter;
+  const long long total = (long long)a.px * a.py * a.pz;
+  if (rule.frozen) flow_map_kernel<true><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(a);
+  else             flow_map_kernel<false><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(a);
+
+  ftle_args t;
+  t.flow = flow; t.nx = shape[0]; t.ny = shape[1]; t.nz = shape[2];
+  t.hx = spacing[0]; t.hy = spacing[1]; t.hz = spacing[2];
+  t.inverse_time = 1.0 / fabs(double(time));
+  t.mode = mode;
+  t.out = device_ftle;
+  ftle_kernel<<<(unsigned)((voxels + 255) / 256), 256, 0, s>>>(t);
+  if (device_steps) steps_to_int64_kernel<<<1, 1, 0, s>>>(counter, device_steps);
+  if (cudaGetLastError() != cudaSuccess) return PARS_ERR_CUDA;
+  return PARS_OK;
+}
+#pragma GCC visibility pop

@@ -435,6 +435,8 @@ std::size_t checked_bytes(long long count, std::size_t element)
   return (std::size_t)count * element;
 }
 }
+
+step_rule make_step_rule(int integrator, int stage_mode, float h) { return make_rule(integrator, stage_mode, h); }
 }
 
 using namespace pars;

@@ -87,6 +87,7 @@ SIGNATURES = {
     "pars_gpu_flow_map_generate": [_P, _I32, _I32, _F, _I32, _I32, _F, ctypes.POINTER(_I32), ctypes.POINTER(_I64)],
     "pars_gpu_ftle_generate": [_P, _I32, _F, _I32, _P],
     "pars_gpu_ftle_device_pointer": [_P, ctypes.POINTER(_P), ctypes.POINTER(_I64)],
+    "pars_gpu_ftle_no_alloc": [_P, _P, _P, _P, _P, _I32, _I32, _I32, _F, _F, _I32, _P, _P, _P],
     "pars_gpu_profile_enable": [_P, _I32],
     "pars_gpu_profile_reset": [_P],
     "pars_gpu_profile_get": [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)],
