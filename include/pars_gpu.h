@@ -232,6 +232,54 @@ int32_t pars_gpu_flow_map_generate(pars_gpu_context* context, int32_t field, int
 int32_t pars_gpu_ftle_generate    (pars_gpu_context* context, int32_t flow_map, float time, int32_t mode, float* ftle);
 int32_t pars_gpu_ftle_device_pointer(pars_gpu_context* context, const float** device_ftle, int64_t* count);
 
+/* ---- unsteady fields and batched advection ------------------------------------------
+ * No counterpart in the reference (its fields are steady and its integrator
+ * ignores time, particle_tracer.cpp:315-318).  An unsteady field holds
+ * `slices` time slices of one grid, [slices][shape0][shape1][shape2][3] FP32;
+ * slice k is the velocity at time t0 + k * slice_dt, linear in time between
+ * slices and constant beyond the first and last slice. */
+int32_t pars_gpu_unsteady_field_upload       (pars_gpu_context* context, const float* xyz, const int32_t shape[3], int32_t slices,
+                                              const float offset[3], const float size[3], const float spacing[3],
+                                              double t0, double slice_dt, int32_t* field);
+int32_t pars_gpu_unsteady_field_upload_device(pars_gpu_context* context, const float* device_xyz, const int32_t shape[3],
+                                              int32_t slices, const float offset[3], const float size[3],
+                                              const float spacing[3], double t0, double slice_dt, int32_t* field);
+
+/* One job of a batched advection: seeds on a (steady or unsteady) field,
+ * advected with the flow-map rules of particle_advector
+ * (particle_advector.cpp:74-139: stop on leaving the grid, on a zero velocity,
+ * or after max_steps steps).  Pathlines on unsteady fields use classical RK4
+ * in space-time with the time of step n = time_begin + n * step_size in FP64. */
+typedef struct pars_gpu_batch_job
+{
+  int32_t      field;               /* field handle (steady or unsteady) */
+  int32_t      integrator;          /* PARS_EULER or PARS_RUNGE_KUTTA_4 */
+  int32_t      stage_mode;          /* PARS_STAGES_RESAMPLED (PARS_STAGES_FROZEN: velocity of the step start) */
+  int32_t      max_steps;
+  float        step_size;
+  int32_t      padding0;
+  double       time_begin;          /* unsteady fields: start time */
+  const float* seeds;               /* DEVICE float4 positions, or NULL for the lattice below */
+  int64_t      seed_count;          /* seeds != NULL: number of seeds */
+  float        lattice_offset[3];   /* seeds == NULL: offset + stride * index, C order (seed_generator.cpp:14-19) */
+  float        lattice_stride[3];
+  int32_t      lattice_count[3];
+  int32_t      padding1;
+  float*       end_positions;       /* DEVICE float4 per seed (last position), may be NULL */
+  int32_t*     end_steps;           /* DEVICE int32 per seed (steps taken), may be NULL */
+  int64_t      steps;               /* out: particle-steps of this job */
+} pars_gpu_batch_job;
+
+/* Advects every job in one persistent launch that drains a device queue of
+ * seed chunks.  variant selects the launch shape (threads per CTA, register
+ * budget) among pars_gpu_batch_variants(); -1 = autotuned: the first call of
+ * each job class (steady / unsteady) times every variant on a probe of the
+ * batch and keeps the fastest for the context. */
+int32_t pars_gpu_batch_advect  (pars_gpu_context* context, pars_gpu_batch_job* jobs, int32_t count, int32_t variant);
+int32_t pars_gpu_batch_variants(pars_gpu_context* context, int32_t* count);
+/* The tuned variant of a job class (0 steady, 1 unsteady), -1 if not tuned yet. */
+int32_t pars_gpu_batch_tuned   (pars_gpu_context* context, int32_t job_class, int32_t* variant, int32_t* threads);
+
 /* ---- allocation-free FTLE --------------------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device
  * memory: plugins running inside a host application that owns the GPU's

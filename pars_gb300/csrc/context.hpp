@@ -79,9 +79,20 @@ private:
 
 struct field_entry
 {
-  device_buffer data;          // float4 [X][Y][Z]
+  device_buffer data;          // float4 [slices][X][Y][Z]
   int           shape[3];
   float         offset[3], size[3], spacing[3];
+  int           slices = 1;    // time slices (1 = steady)
+  double        t0 = 0.0, slice_dt = 1.0;
+  time_axis time() const
+  {
+    time_axis t;
+    t.nt = slices;
+    t.slice_stride = (long long)shape[0] * shape[1] * shape[2];
+    t.t0 = t0;
+    t.inv_slice_dt = 1.0 / slice_dt;
+    return t;
+  }
   field_view view() const
   {
     field_view v;
@@ -168,6 +179,10 @@ struct pars_gpu_context
   // cudaFree (and their device-wide synchronisation) each time.
   std::multimap<std::size_t, pars::device_buffer> buffer_cache;
   std::size_t                             buffer_cache_bytes = 0;
+  // batched advection: job table, counters, and the autotuned launch variant
+  // per job class (0 = steady, 1 = unsteady); -1 = not tuned yet
+  pars::device_buffer                     batch_jobs, batch_counters;
+  int                                     batch_variant[2] = {-1, -1};
   static constexpr std::size_t            buffer_cache_limit = std::size_t(8) << 30;
   // instrumentation
   bool                                    profile = false;
@@ -252,6 +267,29 @@ void launch_extract_block(pars_gpu_context& ctx, const float* domain_xyz, const 
 long long launch_index_generate(pars_gpu_context& ctx, const float4* vertices, long long n, int* indices);
 void launch_color_generate(pars_gpu_context& ctx, const float4* vertices, const int* indices, long long index_count,
                            int mode, float parameter, float4* colors);
+
+// One job of a batched advection launch, as the persistent kernel reads it.
+struct batch_job_device
+{
+  field_view          field;
+  time_axis           time;
+  step_rule           rule;
+  int                 max_steps;
+  double              time_begin;
+  long long           seed_count;
+  const float4*       seeds;          // explicit seeds, or nullptr for the lattice
+  float               ox, oy, oz, sx, sy, sz;
+  int                 px, py, pz;
+  float4*             end_positions;  // may be nullptr
+  int*                end_steps;      // may be nullptr
+  long long           first_chunk;    // chunks of all earlier jobs
+  unsigned long long* steps;          // per-job step counter
+};
+int  batch_variant_count();
+int  batch_variant_threads(int variant);
+// job_class 0: all jobs steady; 1: some job unsteady.
+void launch_batch_advect(pars_gpu_context& ctx, int job_class, int variant, const batch_job_device* jobs, int njobs,
+                         long long total_chunks, unsigned long long* counter);
 
 void launch_flow_map(pars_gpu_context& ctx, const field_view& f, const step_rule& rule, int iterations,
                      const float offset[3], const float fm_spacing[3], const int seeds_per_dimension[3],

@@ -46,14 +46,21 @@ __global__ void __launch_bounds__(256) flow_map_kernel(const flow_map_args a)
                              __fadd_rn(a.oz, __fmul_rn(a.sz, float(iz))), 0.0f);
     bool finished = false;
     float3 lo = make_float3(0.0f, 0.0f, 0.0f);
+    cell_cache cache;
     for (int it = 1; it < a.iterations; ++it)
     {
       float3 v;
-      const bool inside = FROZEN ? sample_inside(a.f, pos, v) : sample_inside_resampled(a.f, pos, v);
+      bool inside;
+      if (FROZEN) inside = sample_inside(a.f, pos, v);
+      else
+      {
+        inside = contains_reference(a.f, pos);
+        if (inside) v = sample_cached(a.f, cache, pos.x, pos.y, pos.z);
+      }
       if (!inside) { finished = true; break; }
       if (is_zero(v)) { finished = true; break; }
       if (FROZEN) pos = frozen_step(a.rule, pos, v);
-      else resampled_step(a.f, a.rule, pos, lo, v);
+      else resampled_step_cached(a.f, cache, a.rule, pos, lo, v);
       ++steps;
       if (it + 1 == a.iterations) { finished = true; break; }
     }

@@ -24,7 +24,8 @@ long long pars_gpu_context::held_bytes() const
                                     &block_of_next, &exits, &exit_keys, &exit_keys_sorted, &exit_order,
                                     &exit_order_sorted, &counters, &block_max, &cub_temp, &scan_input, &tile_counts,
                                     &tile_offsets, &staging, &ftle, &curves.vertices, &curves.colors,
-                                    &curves.indices, &boundary_positions, &boundary_offsets};
+                                    &curves.indices, &boundary_positions, &boundary_offsets, &batch_jobs,
+                                    &batch_counters};
   for (auto* b : scratch) total += (long long)b->bytes();
   return total + (long long)buffer_cache_bytes + (long long)single_block.bytes();
 }
@@ -541,6 +542,42 @@ int32_t pars_gpu_field_upload_device(pars_gpu_context* ctx, const float* device_
   });
 }
 
+int32_t pars_gpu_unsteady_field_upload(pars_gpu_context* ctx, const float* xyz, const int32_t shape[3], int32_t slices,
+                                       const float offset[3], const float size[3], const float spacing[3], double t0,
+                                       double slice_dt, int32_t* field)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(xyz && field, "xyz and field are required");
+    PARS_REQUIRE(slices >= 1 && slice_dt > 0.0, "slices must be >= 1 and slice_dt positive");
+    check_field_args(shape, spacing);
+    auto entry = make_field(shape, offset, size, spacing);
+    entry->slices = slices; entry->t0 = t0; entry->slice_dt = slice_dt;
+    const long long count = (long long)shape[0] * shape[1] * shape[2] * slices;
+    ctx->staging.reserve(sizeof(float) * 3 * count);
+    entry->data = acquire_buffer(*ctx, sizeof(float4) * count);
+    PARS_CUDA(cudaMemcpyAsync(ctx->staging.get(), xyz, sizeof(float) * 3 * count, cudaMemcpyHostToDevice, ctx->stream));
+    launch_pack_field(*ctx, ctx->staging.as<const float>(), entry->data.as<float4>(), count);
+    *field = add_field(*ctx, std::move(entry));
+  });
+}
+
+int32_t pars_gpu_unsteady_field_upload_device(pars_gpu_context* ctx, const float* device_xyz, const int32_t shape[3], int32_t slices,
+                                              const float offset[3], const float size[3], const float spacing[3], double t0,
+                                              double slice_dt, int32_t* field)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(device_xyz && field, "device_xyz and field are required");
+    PARS_REQUIRE(slices >= 1 && slice_dt > 0.0, "slices must be >= 1 and slice_dt positive");
+    check_field_args(shape, spacing);
+    auto entry = make_field(shape, offset, size, spacing);
+    entry->slices = slices; entry->t0 = t0; entry->slice_dt = slice_dt;
+    const long long count = (long long)shape[0] * shape[1] * shape[2] * slices;
+    entry->data = acquire_buffer(*ctx, sizeof(float4) * count);
+    launch_pack_field(*ctx, device_xyz, entry->data.as<float4>(), count);
+    *field = add_field(*ctx, std::move(entry));
+  });
+}
+
 int32_t pars_gpu_field_release(pars_gpu_context* ctx, int32_t field)
 {
   return guarded(ctx, [&] {
@@ -918,6 +955,117 @@ int32_t pars_gpu_ftle_generate(pars_gpu_context* ctx, int32_t flow_map, float ti
       PARS_CUDA(cudaMemcpyAsync(ftle, ctx->ftle.get(), sizeof(float) * voxels, cudaMemcpyDeviceToHost, ctx->stream));
       PARS_CUDA(cudaStreamSynchronize(ctx->stream));
     }
+  });
+}
+
+int32_t pars_gpu_batch_variants(pars_gpu_context* ctx, int32_t* count)
+{
+  return guarded(ctx, [&] { PARS_REQUIRE(count, "count is required"); *count = batch_variant_count(); });
+}
+
+int32_t pars_gpu_batch_tuned(pars_gpu_context* ctx, int32_t job_class, int32_t* variant, int32_t* threads)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(job_class == 0 || job_class == 1, "job_class is 0 (steady) or 1 (unsteady)");
+    const int v = ctx->batch_variant[job_class];
+    if (variant) *variant = v;
+    if (threads) *threads = v >= 0 ? batch_variant_threads(v) : 0;
+  });
+}
+
+int32_t pars_gpu_batch_advect(pars_gpu_context* ctx, pars_gpu_batch_job* jobs, int32_t count, int32_t variant)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(count >= 0 && (count == 0 || jobs), "jobs are required");
+    PARS_REQUIRE(variant >= -1 && variant < batch_variant_count(), "unknown launch variant");
+    if (count == 0) return;
+    std::vector<batch_job_device> device_jobs(count);
+    bool unsteady = false;
+    for (int j = 0; j < count; ++j)
+    {
+      const pars_gpu_batch_job& in = jobs[j];
+      auto& f = find_field(*ctx, in.field);
+      batch_job_device& d = device_jobs[j];
+      d.field = f.view();
+      d.time = f.time();
+      d.rule = make_rule(in.integrator, in.stage_mode, in.step_size);
+      PARS_REQUIRE(in.max_steps >= 0, "max_steps must be >= 0");
+      d.max_steps = in.max_steps;
+      d.time_begin = in.time_begin;
+      d.seeds = reinterpret_cast<const float4*>(in.seeds);
+      if (in.seeds) { PARS_REQUIRE(in.seed_count >= 0, "seed_count must be >= 0"); d.seed_count = in.seed_count; }
+      else
+      {
+        for (int i = 0; i < 3; ++i) PARS_REQUIRE(in.lattice_count[i] >= 0, "lattice counts must be >= 0");
+        d.seed_count = (long long)in.lattice_count[0] * in.lattice_count[1] * in.lattice_count[2];
+      }
+      d.ox = in.lattice_offset[0]; d.oy = in.lattice_offset[1]; d.oz = in.lattice_offset[2];
+      d.sx = in.lattice_stride[0]; d.sy = in.lattice_stride[1]; d.sz = in.lattice_stride[2];
+      d.px = in.lattice_count[0]; d.py = in.lattice_count[1]; d.pz = in.lattice_count[2];
+      d.end_positions = reinterpret_cast<float4*>(in.end_positions);
+      d.end_steps = in.end_steps;
+      unsteady = unsteady || f.slices > 1;
+    }
+    const int job_class = unsteady ? 1 : 0;
+    ctx->batch_jobs.reserve(sizeof(batch_job_device) * count);
+    ctx->batch_counters.reserve(sizeof(unsigned long long) * (count + 1));
+    auto* counters = ctx->batch_counters.as<unsigned long long>();
+
+    // Chunk prefixes depend on the launch shape (seeds per chunk = threads).
+    auto run = [&](int v) {
+      const int threads = batch_variant_threads(v);
+      long long chunks = 0;
+      for (int j = 0; j < count; ++j)
+      {
+        device_jobs[j].first_chunk = chunks;
+        device_jobs[j].steps = counters + 1 + j;
+        chunks += (device_jobs[j].seed_count + threads - 1) / threads;
+      }
+      PARS_CUDA(cudaMemcpyAsync(ctx->batch_jobs.get(), device_jobs.data(), sizeof(batch_job_device) * count, cudaMemcpyHostToDevice, ctx->stream));
+      PARS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (count + 1), ctx->stream));
+      launch_batch_advect(*ctx, job_class, v, ctx->batch_jobs.as<const batch_job_device>(), count, chunks, counters);
+    };
+
+    if (variant < 0 && ctx->batch_variant[job_class] < 0)
+    {
+      // Autotune on a probe: every job capped at 16384 seeds, each variant
+      // timed twice with CUDA events, the fastest kept for this job class.
+      std::vector<long long> full(count);
+      for (int j = 0; j < count; ++j) { full[j] = device_jobs[j].seed_count; device_jobs[j].seed_count = std::min(full[j], 16384LL); }
+      std::vector<float4*> outputs(count);
+      std::vector<int*> step_outputs(count);
+      for (int j = 0; j < count; ++j) { outputs[j] = device_jobs[j].end_positions; step_outputs[j] = device_jobs[j].end_steps; }
+      cudaEvent_t a, b;
+      PARS_CUDA(cudaEventCreate(&a));
+      PARS_CUDA(cudaEventCreate(&b));
+      float best = 0.0f;
+      int best_v = 1;
+      for (int v = 0; v < batch_variant_count(); ++v)
+      {
+        float fastest = 0.0f;
+        for (int rep = 0; rep < 2; ++rep)
+        {
+          PARS_CUDA(cudaEventRecord(a, ctx->stream));
+          run(v);
+          PARS_CUDA(cudaEventRecord(b, ctx->stream));
+          PARS_CUDA(cudaEventSynchronize(b));
+          float ms = 0.0f;
+          PARS_CUDA(cudaEventElapsedTime(&ms, a, b));
+          fastest = rep == 0 ? ms : std::min(fastest, ms);
+        }
+        if (v == 0 || fastest < best) { best = fastest; best_v = v; }
+      }
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      ctx->batch_variant[job_class] = best_v;
+      for (int j = 0; j < count; ++j) device_jobs[j].seed_count = full[j];
+    }
+    const int chosen = variant >= 0 ? variant : ctx->batch_variant[job_class];
+    run(chosen);
+    std::vector<unsigned long long> steps(count + 1);
+    PARS_CUDA(cudaMemcpyAsync(steps.data(), counters, sizeof(unsigned long long) * (count + 1), cudaMemcpyDeviceToHost, ctx->stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int j = 0; j < count; ++j) jobs[j].steps = (int64_t)steps[1 + j];
   });
 }
 

@@ -41,11 +41,18 @@ __global__ void __launch_bounds__(256) trace_kernel(const trace_launch a)
     int kept = is_invalid_vertex(last) ? 0 : 1;
     const float4 term = termination_vertex();
     float3 lo = make_float3(0.0f, 0.0f, 0.0f);
+    cell_cache cache;
     for (int it = 1; it < N; ++it)
     {
       if (it == N - 1) { out[it] = term; ++written; ++kept; break; }
       float3 v;
-      const bool inside = FROZEN ? sample_inside(f, last, v) : sample_inside_resampled(f, last, v);
+      bool inside;
+      if (FROZEN) inside = sample_inside(f, last, v);
+      else
+      {
+        inside = contains_reference(f, last);
+        if (inside) v = sample_cached(f, cache, last.x, last.y, last.z);
+      }
       if (!inside)
       {
         out[it] = term; ++written; ++kept;
@@ -65,7 +72,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const trace_launch a)
       if (is_zero(v)) { out[it] = term; ++written; ++kept; break; }
       float4 next;
       if (FROZEN) next = frozen_step(a.rule, last, v);
-      else { next = last; resampled_step(f, a.rule, next, lo, v); }
+      else { next = last; resampled_step_cached(f, cache, a.rule, next, lo, v); }
       out[it] = next;
       ++written;
       kept += is_invalid_vertex(next) ? 0 : 1;
