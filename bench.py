@@ -68,7 +68,7 @@ def measured_peaks():
 def committed_traffic(steps_per_launch):
     """DRAM bytes per launch of the flow-map kernel from the committed ncu
     summary (bytes per particle-step measured there, scaled to this launch)."""
-    path = os.path.join(ROOT, "profiles", "advect_flow_map_traffic.txt")
+    path = os.path.join(ROOT, "profiles", "batch_advect_traffic.txt")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -213,7 +213,7 @@ def main():
     launches = ctx.launch_count() - launches0
     ctx.profile_enable(False)
     elapsed_ms = start.elapsed_time(stop)
-    advect_ms, advect_n = ctx.profile_get("advect_flow_map")
+    advect_ms, advect_n = ctx.profile_get("batch_advect")
     ftle_ms, ftle_n = ctx.profile_get("ftle_fused")
 
     if dist:
@@ -289,7 +289,7 @@ def main():
                 "ftle_voxels_per_s": ftle_voxels_per_s,
                 "frozen_velocity_steps_per_s": frozen_value,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                             "traffic": committed_traffic(steps_per_launch), "kernel": "advect_flow_map",
+                             "traffic": committed_traffic(steps_per_launch), "kernel": "batch_advect",
                              "bytes_per_unit": BYTES_PER_RK4_STEP, "units_per_launch": steps_per_launch,
                              "avg_launch_ms": advect_avg_s * 1e3, "peak_source": peak_kind,
                              "ftle_kernel": {"avg_launch_ms": ftle_avg_s * 1e3,

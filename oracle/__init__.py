@@ -184,6 +184,22 @@ class Port(_Lib):
         L.orc_largest_eigenvalue.argtypes = [_P, _LL, _P]
         L.orc_largest_eigenvalue_closed_form.restype = None
         L.orc_largest_eigenvalue_closed_form.argtypes = [_P, _LL, _P]
+        L.orc_advect_unsteady_fp64.restype = None
+        L.orc_advect_unsteady_fp64.argtypes = [_P, _P, _I, _P, _P, _D, _D, _P, _LL, _D, _D, _LL, _P, _P]
+
+    def advect_unsteady_fp64(self, xyz, offset, spacing, t0, slice_dt, start, time_begin, step, max_steps):
+        """FP64 pathlines (classical RK4 in space-time) on an unsteady field
+        xyz [slices, X, Y, Z, 3]."""
+        xyz = np.ascontiguousarray(xyz, np.float32)
+        dims = np.array(xyz.shape[1:4], np.int32)
+        o = np.ascontiguousarray(offset, np.float32)
+        sp = np.ascontiguousarray(spacing, np.float32)
+        start = np.ascontiguousarray(start, np.float64).reshape(-1, 3)
+        end = np.zeros_like(start)
+        steps = np.zeros(len(start), np.int64)
+        self.lib.orc_advect_unsteady_fp64(_ptr(xyz), _ptr(dims), xyz.shape[0], _ptr(o), _ptr(sp), t0, slice_dt, _ptr(start),
+                                          len(start), time_begin, step, max_steps, _ptr(end), _ptr(steps))
+        return end, steps
 
     def max_threads(self):
         return self.lib.orc_max_threads()

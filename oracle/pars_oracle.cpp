@@ -893,6 +893,70 @@ void orc_advect_fp64(const float* xyz, const int dims[3], const float offset[3],
   }
 }
 
+// ---- FP64 pathline oracle on an unsteady field ----------------------------------
+// `slices` grids [slices][X][Y][Z][3] (FP32), slice k at time t0 + k*slice_dt,
+// linear in time between slices, constant outside [t0, t_last].  Classical RK4
+// in space-time from (start, time_begin) with step h: the step stops when the
+// particle leaves the grid (floor quotient outside [0, shape-2]), when |v_i| <=
+// 1e-5 at the step start, or after max_steps steps.  Time of step n:
+// time_begin + n*h.
+void orc_advect_unsteady_fp64(const float* xyz, const int dims[3], int slices, const float offset[3], const float spacing[3],
+                              double t0, double slice_dt, const double* start, long long n, double time_begin, double h,
+                              long long max_steps, double* end, long long* steps_out)
+{
+  const long long slice_stride = 3LL * dims[0] * dims[1] * dims[2];
+  auto sample = [&](const double* p, double t, double* out) {
+    int k = 0;
+    double wt = 0.0;
+    if (slices > 1)
+    {
+      const double s = (t - t0) / slice_dt;
+      const double fs = std::floor(s);
+      if (!(fs >= 0.0)) { k = 0; wt = 0.0; }
+      else if (fs >= double(slices - 1)) { k = slices - 2; wt = 1.0; }
+      else { k = int(fs); wt = s - fs; }
+    }
+    field f0 {xyz + k * slice_stride, {dims[0], dims[1], dims[2]}, {offset[0], offset[1], offset[2]}, {0, 0, 0},
+              {spacing[0], spacing[1], spacing[2]}};
+    double a[3];
+    interpolate_fp64(f0, p, a);
+    if (slices > 1 && wt != 0.0)
+    {
+      field f1 = f0;
+      f1.xyz = xyz + (k + 1) * slice_stride;
+      double b[3];
+      interpolate_fp64(f1, p, b);
+      for (int c = 0; c < 3; ++c) a[c] = (1.0 - wt) * a[c] + wt * b[c];
+    }
+    for (int c = 0; c < 3; ++c) out[c] = a[c];
+  };
+  field shape_only {xyz, {dims[0], dims[1], dims[2]}, {offset[0], offset[1], offset[2]}, {0, 0, 0},
+                    {spacing[0], spacing[1], spacing[2]}};
+  #pragma omp parallel for schedule(dynamic, 16)
+  for (long long i = 0; i < n; ++i)
+  {
+    double x[3] = {start[3 * i], start[3 * i + 1], start[3 * i + 2]};
+    long long s = 0;
+    for (; s < max_steps; ++s)
+    {
+      if (!contains_fp64(shape_only, x)) break;
+      const double t = time_begin + double(s) * h;
+      double k1[3], k2[3], k3[3], k4[3], tmp[3];
+      sample(x, t, k1);
+      if (is_zero_fp64(k1)) break;
+      for (int c = 0; c < 3; ++c) tmp[c] = x[c] + 0.5 * h * k1[c];
+      sample(tmp, t + 0.5 * h, k2);
+      for (int c = 0; c < 3; ++c) tmp[c] = x[c] + 0.5 * h * k2[c];
+      sample(tmp, t + 0.5 * h, k3);
+      for (int c = 0; c < 3; ++c) tmp[c] = x[c] + h * k3[c];
+      sample(tmp, t + h, k4);
+      for (int c = 0; c < 3; ++c) x[c] += h / 6.0 * (k1[c] + 2.0 * k2[c] + 2.0 * k3[c] + k4[c]);
+    }
+    std::memcpy(end + 3 * i, x, 24);
+    steps_out[i] = s;
+  }
+}
+
 // ---- FTLE, FP64 intended mathematics -------------------------------------------
 // J_ij = d phi_i / d x_j by central differences with denominator 2h_j, one-sided
 // at the grid borders (0 along an axis of extent 1); C = J^T J; FTLE =

@@ -1,105 +1,218 @@
 // Batched advection: many jobs (seed sets on steady or unsteady fields of
-// different sizes) in ONE persistent launch.
+// different sizes) in ONE persistent launch that drains a device work queue.
 //
-// The grid holds as many CTAs as fit on the GPU at once.  Each CTA repeatedly
-// takes the next chunk of seeds from a device counter (one atomic per chunk),
-// finds the chunk's job by binary search over the jobs' chunk prefixes, and
-// advects one seed per thread with the flow-map rules of particle_advector
-// (particle_advector.cpp:74-139): stop when the particle leaves the grid,
-// meets a zero velocity, or has taken max_steps steps; its last position is
-// written to the job's output.  Uneven jobs balance themselves: a CTA that
-// finishes early takes the next chunk, whatever job it belongs to.
+// The grid holds as many CTAs as fit on the GPU at once.  Work is a queue of
+// pools (POOL consecutive seeds of one job); a warp takes pools with one
+// atomic and hands their seeds to its lanes.  A lane whose particle retires
+// takes the next seed of the pool at once (warp ballot + prefix), so lanes do
+// not idle while the rest of the warp finishes long particles.  All lanes of a
+// warp work on the same job; a warp moves to another job only when its lanes
+// have drained, so job parameters stay warp-uniform.
+//
+// Each particle follows the flow-map rules of particle_advector
+// (particle_advector.cpp:74-139): before every step it stops when it has
+// taken max_steps steps, left the grid (the reference's contains(), floor of
+// the IEEE quotient) or meets a zero velocity (|v_i| <= 1e-5); its last
+// position (and optionally its step count) is written to the job's output.
 #include "context.hpp"
 
 namespace pars
 {
 namespace
 {
-__device__ __forceinline__ int find_job(const batch_job_device* __restrict__ jobs, int njobs, long long chunk)
+constexpr unsigned full_mask = 0xffffffffu;
+constexpr int pool_seeds = 256;
+
+__device__ __forceinline__ int find_job(const batch_job_device* __restrict__ jobs, int njobs, long long pool)
 {
   int lo = 0, hi = njobs - 1;
   while (lo < hi)
   {
     const int mid = (lo + hi + 1) >> 1;
-    if (jobs[mid].first_chunk <= chunk) lo = mid;
+    if (jobs[mid].first_pool <= pool) lo = mid;
     else hi = mid - 1;
   }
   return lo;
 }
 
+// Cell of one axis for the step-start test and the first sample: the
+// consistent pair (s, w) and whether the reference's floor(rn(d / h)) puts the
+// point inside.  rn(d / h) can differ from the consistent s only when d / h is
+// within an ulp of s + 1, i.e. w is within 1e-4 of 1; only then is the IEEE
+// division evaluated.
+__device__ __forceinline__ bool start_cell(float p, float o, float h, float inv_h, int n, axis_cell& c)
+{
+  c = cell_consistent(p, o, h, inv_h);
+  float s_ref = c.s;
+  if (c.w >= 0.9999f) s_ref = floorf(__fdiv_rn(__fsub_rn(p, o), h));
+  return cell_inside(s_ref, n);
+}
+
+__device__ __forceinline__ float3 sample_cell(const field_view& f, cell_cache& k, axis_cell cx, axis_cell cy, axis_cell cz)
+{
+  clamp_cell(cx, f.nx); clamp_cell(cy, f.ny); clamp_cell(cz, f.nz);
+  const int ix = int(cx.s), iy = int(cy.s), iz = int(cz.s);
+  if (ix != k.ix || iy != k.iy || iz != k.iz) cache_load(f, k, ix, iy, iz);
+  return make_float3(cache_eval1(k.a.x, k.b.x, k.c.x, k.d.x, k.e.x, k.f.x, k.g.x, k.h.x, cx.w, cy.w, cz.w),
+                     cache_eval1(k.a.y, k.b.y, k.c.y, k.d.y, k.e.y, k.f.y, k.g.y, k.h.y, cx.w, cy.w, cz.w),
+                     cache_eval1(k.a.z, k.b.z, k.c.z, k.d.z, k.e.z, k.f.z, k.g.z, k.h.z, cx.w, cy.w, cz.w));
+}
+
+template <bool UNSTEADY>
+struct lane_cache;
+template <> struct lane_cache<false> { cell_cache k; };
+template <> struct lane_cache<true>  { cell_cache2 k; };
+
 // UNSTEADY = false: every job is on a steady field (one slice).
 // UNSTEADY = true: jobs may have several time slices (a steady job works too).
 template <int THREADS, int MIN_BLOCKS, bool UNSTEADY>
 __global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
-batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long long total_chunks,
-                    unsigned long long* __restrict__ chunk_counter)
+batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long long total_pools,
+                    unsigned long long* __restrict__ pool_counter)
 {
-  __shared__ long long s_chunk;
-  __shared__ int s_job;
+  const int lane = threadIdx.x & 31;
+  const unsigned lanes_below = (1u << lane) - 1u;
+
+  // warp-uniform work state
+  int job = -1;
+  long long pool_next = 0, pool_end = 0, pending = -1;
+  bool exhausted = false;
+  unsigned int job_steps = 0;       // this lane's steps on the current job
+  // lane state
+  bool alive = false;
+  long long seed = 0;
+  int steps = 0;
+  float4 pos = make_float4(0.f, 0.f, 0.f, 0.f);
+  float3 lo = make_float3(0.f, 0.f, 0.f);
+  lane_cache<UNSTEADY> cache;
+  // current job's parameters (warp-uniform)
+  field_view f {};
+  time_axis ta {};
+  float h = 0.0f;
+  int rk4 = 1, max_steps = 0;
+  double time_begin = 0.0;
+
   for (;;)
   {
-    if (threadIdx.x == 0)
+    // ---- refill idle lanes ---------------------------------------------------
+    unsigned need = __ballot_sync(full_mask, !alive);
+    while (need)
     {
-      const long long c = (long long)atomicAdd(chunk_counter, 1ULL);
-      s_chunk = c;
-      s_job = c < total_chunks ? find_job(jobs, njobs, c) : 0;
+      if (pool_next < pool_end)
+      {
+        const long long s = pool_next + __popc(need & lanes_below);
+        if (!alive && s < pool_end)
+        {
+          const batch_job_device& J = jobs[job];
+          seed = s;
+          if (J.seeds) pos = J.seeds[s];
+          else
+          {
+            const int iz = int(s % J.pz);
+            const int iy = int((s / J.pz) % J.py);
+            const int ix = int(s / ((long long)J.pz * J.py));
+            pos = make_float4(__fadd_rn(J.ox, __fmul_rn(J.sx, float(ix))), __fadd_rn(J.oy, __fmul_rn(J.sy, float(iy))),
+                              __fadd_rn(J.oz, __fmul_rn(J.sz, float(iz))), 0.0f);
+          }
+          lo = make_float3(0.f, 0.f, 0.f);
+          steps = 0;
+          alive = true;
+        }
+        pool_next = min(pool_end, pool_next + (long long)__popc(need));
+        need = __ballot_sync(full_mask, !alive);
+        continue;
+      }
+      if (exhausted) break;
+      long long p = pending;
+      if (p < 0)
+      {
+        if (lane == 0) p = (long long)atomicAdd(pool_counter, 1ULL);
+        p = __shfl_sync(full_mask, p, 0);
+      }
+      if (p >= total_pools) { exhausted = true; break; }
+      const int pj = find_job(jobs, njobs, p);
+      if (pj != job)
+      {
+        if (__any_sync(full_mask, alive)) { pending = p; break; }   // drain the current job first
+        // switch job: flush this lane's step count, load the new parameters
+        if (job >= 0)
+        {
+          const unsigned int total = __reduce_add_sync(full_mask, job_steps);
+          if (lane == 0 && total) atomicAdd(jobs[job].steps, (unsigned long long)total);
+        }
+        job_steps = 0;
+        job = pj;
+        const batch_job_device& J = jobs[job];
+        f = J.field; ta = J.time; h = J.rule.h; rk4 = J.rule.rk4; max_steps = J.max_steps; time_begin = J.time_begin;
+        cache = lane_cache<UNSTEADY>();
+      }
+      pending = -1;
+      pool_next = (p - jobs[job].first_pool) * pool_seeds;
+      pool_end = min(pool_next + pool_seeds, jobs[job].seed_count);
     }
-    __syncthreads();
-    const long long chunk = s_chunk;
-    const int j = s_job;
-    __syncthreads();
-    if (chunk >= total_chunks) return;
+    if (!__any_sync(full_mask, alive))
+    {
+      if (exhausted) break;
+      continue;   // switch to the pending job
+    }
 
-    const batch_job_device& job = jobs[j];
-    const long long seed = (chunk - job.first_chunk) * THREADS + threadIdx.x;
-    unsigned int steps = 0;
-    if (seed < job.seed_count)
+    // ---- one step of every live lane -------------------------------------------
+    if (alive)
     {
-      float4 pos;
-      if (job.seeds) pos = job.seeds[seed];
-      else
+      bool retire = steps >= max_steps;
+      axis_cell cx, cy, cz;
+      if (!retire)
       {
-        // lattice seed (seed_generator.cpp:14-19), C order
-        const int iz = int(seed % job.pz);
-        const int iy = int((seed / job.pz) % job.py);
-        const int ix = int(seed / ((long long)job.pz * job.py));
-        pos = make_float4(__fadd_rn(job.ox, __fmul_rn(job.sx, float(ix))), __fadd_rn(job.oy, __fmul_rn(job.sy, float(iy))),
-                          __fadd_rn(job.oz, __fmul_rn(job.sz, float(iz))), 0.0f);
+        const bool in_x = start_cell(pos.x, f.ox, f.hx, f.inv_hx, f.nx, cx);
+        const bool in_y = start_cell(pos.y, f.oy, f.hy, f.inv_hy, f.ny, cy);
+        const bool in_z = start_cell(pos.z, f.oz, f.hz, f.inv_hz, f.nz, cz);
+        retire = !(in_x && in_y && in_z);
       }
-      const field_view f = job.field;
-      const step_rule rule = job.rule;
-      float3 lo = make_float3(0.0f, 0.0f, 0.0f);
-      if (!UNSTEADY)
+      if (!retire)
       {
-        cell_cache cache;
-        for (int it = 0; it < job.max_steps; ++it)
+        step_rule r;
+        r.frozen = 0; r.rk4 = rk4; r.h = h; r.count = 0;
+        if constexpr (UNSTEADY)
         {
-          if (!contains_reference(f, pos)) break;
-          const float3 v = sample_cached(f, cache, pos.x, pos.y, pos.z);
-          if (is_zero(v)) break;
-          resampled_step_cached(f, cache, rule, pos, lo, v);
-          ++steps;
-        }
-      }
-      else
-      {
-        cell_cache2 cache;
-        for (int it = 0; it < job.max_steps; ++it)
-        {
-          if (!contains_reference(f, pos)) break;
           // FP64 time of this step: start + n h (no accumulated rounding)
-          const double t = job.time_begin + double(it) * double(rule.h);
-          const float3 v = sample_unsteady_cached(f, job.time, cache, pos.x, pos.y, pos.z, t);
-          if (is_zero(v)) break;
-          unsteady_step(f, job.time, cache, rule, pos, lo, v, t);
-          ++steps;
+          const double t = time_begin + double(steps) * double(h);
+          const float3 k1 = sample_unsteady_cached(f, ta, cache.k, pos.x, pos.y, pos.z, t);
+          if (is_zero(k1)) retire = true;
+          else unsteady_step(f, ta, cache.k, r, pos, lo, k1, t);
         }
+        else
+        {
+          const float3 k1 = sample_cell(f, cache.k, cx, cy, cz);
+          if (is_zero(k1)) retire = true;
+          else resampled_step_cached(f, cache.k, r, pos, lo, k1);
+        }
+        if (!retire) { ++steps; ++job_steps; }
       }
-      if (job.end_positions) job.end_positions[seed] = pos;
-      if (job.end_steps) job.end_steps[seed] = int(steps);
+      if (retire)
+      {
+        const batch_job_device& J = jobs[job];
+        if (J.end_positions)
+        {
+          long long out = seed;
+          bool write = true;
+          if (!J.seeds && J.ux > 0)
+          {
+            // lattice seed -> output voxel of the flow map's own shape
+            const int iz = int(seed % J.pz), iy = int((seed / J.pz) % J.py), ix = int(seed / ((long long)J.pz * J.py));
+            write = ix < J.ux && iy < J.uy && iz < J.uz;
+            out = ((long long)ix * J.uy + iy) * J.uz + iz;
+          }
+          if (write) J.end_positions[out] = pos;
+        }
+        if (J.end_steps) J.end_steps[seed] = steps;
+        alive = false;
+      }
     }
-    const unsigned int warp_steps = __reduce_add_sync(0xffffffffu, steps);
-    if ((threadIdx.x & 31) == 0 && warp_steps) atomicAdd(job.steps, (unsigned long long)warp_steps);
+  }
+  if (job >= 0)
+  {
+    const unsigned int total = __reduce_add_sync(full_mask, job_steps);
+    if (lane == 0 && total) atomicAdd(jobs[job].steps, (unsigned long long)total);
   }
 }
 
@@ -109,13 +222,12 @@ struct variant
   const void* kernel;
 };
 
-// Launch shapes the autotuner chooses from, per job class: threads per CTA
-// (= seeds per chunk) and the minimum resident CTAs per SM the register
-// allocation must allow.
+// Launch shapes the autotuner chooses from, per job class: threads per CTA and
+// the minimum resident CTAs per SM that the register allocation must allow.
 const variant variants[2][4] = {
   {{64, 1, (const void*)batch_advect_kernel<64, 1, false>},
    {128, 1, (const void*)batch_advect_kernel<128, 1, false>},
-   {128, 4, (const void*)batch_advect_kernel<128, 4, false>},
+   {128, 6, (const void*)batch_advect_kernel<128, 6, false>},
    {256, 1, (const void*)batch_advect_kernel<256, 1, false>}},
   {{64, 1, (const void*)batch_advect_kernel<64, 1, true>},
    {128, 1, (const void*)batch_advect_kernel<128, 1, true>},
@@ -126,19 +238,21 @@ const variant variants[2][4] = {
 
 int batch_variant_count() { return 4; }
 int batch_variant_threads(int v) { return variants[0][v].threads; }
+int batch_pool_seeds() { return pool_seeds; }
 
 void launch_batch_advect(pars_gpu_context& ctx, int job_class, int v, const batch_job_device* jobs, int njobs,
-                         long long total_chunks, unsigned long long* counter)
+                         long long total_pools, unsigned long long* counter)
 {
-  if (total_chunks <= 0) return;
+  if (total_pools <= 0) return;
   const variant& var = variants[job_class][v];
   int per_sm = 0, sms = 0;
   PARS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, var.kernel, var.threads, 0));
   PARS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
   const long long persistent = (long long)std::max(per_sm, 1) * sms;
-  const unsigned grid = (unsigned)std::min<long long>(persistent, total_chunks);
+  const long long warps_needed = total_pools;   // at least one pool per warp
+  const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>(persistent, (warps_needed * 32 + var.threads - 1) / var.threads));
   launch_scope scope(ctx, "batch_advect");
-  void* args[] = {(void*)&jobs, (void*)&njobs, (void*)&total_chunks, (void*)&counter};
+  void* args[] = {(void*)&jobs, (void*)&njobs, (void*)&total_pools, (void*)&counter};
   PARS_CUDA(cudaLaunchKernel(var.kernel, grid, var.threads, args, 0, ctx.stream));
 }
 }

@@ -280,13 +280,15 @@ struct batch_job_device
   const float4*       seeds;          // explicit seeds, or nullptr for the lattice
   float               ox, oy, oz, sx, sy, sz;
   int                 px, py, pz;
+  int                 ux, uy, uz;     // lattice seeds: output voxel shape (0 = output per seed)
   float4*             end_positions;  // may be nullptr
   int*                end_steps;      // may be nullptr
-  long long           first_chunk;    // chunks of all earlier jobs
+  long long           first_pool;     // pools of all earlier jobs
   unsigned long long* steps;          // per-job step counter
 };
 int  batch_variant_count();
 int  batch_variant_threads(int variant);
+int  batch_pool_seeds();
 // job_class 0: all jobs steady; 1: some job unsteady.
 void launch_batch_advect(pars_gpu_context& ctx, int job_class, int variant, const batch_job_device* jobs, int njobs,
                          long long total_chunks, unsigned long long* counter);

@@ -430,6 +430,69 @@ void trace_single(pars_gpu_context& ctx, int32_t field, long long count, int32_t
   run_rounds(ctx, blocks, device_blocks, count, block_count, block_max, rule, false, summary);
 }
 
+// Runs batched jobs in one persistent launch and returns each job's steps.
+// variant < 0 uses the context's tuned launch shape for the job class, tuning
+// it first if needed: every job capped at 16384 seeds, each shape timed twice
+// with CUDA events, the fastest kept.
+std::vector<unsigned long long> execute_batch(pars_gpu_context& ctx, std::vector<batch_job_device>& jobs, int job_class, int variant)
+{
+  const int count = int(jobs.size());
+  ctx.batch_jobs.reserve(sizeof(batch_job_device) * count);
+  ctx.batch_counters.reserve(sizeof(unsigned long long) * (count + 1));
+  auto* counters = ctx.batch_counters.as<unsigned long long>();
+
+  // The device queue: each job's seeds in pools of batch_pool_seeds(); counter
+  // 0 hands out pools, counters 1.. count each job's steps.
+  auto run = [&](int v) {
+    const int pool = batch_pool_seeds();
+    long long pools = 0;
+    for (int j = 0; j < count; ++j)
+    {
+      jobs[j].first_pool = pools;
+      jobs[j].steps = counters + 1 + j;
+      pools += (jobs[j].seed_count + pool - 1) / pool;
+    }
+    PARS_CUDA(cudaMemcpyAsync(ctx.batch_jobs.get(), jobs.data(), sizeof(batch_job_device) * count, cudaMemcpyHostToDevice, ctx.stream));
+    PARS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (count + 1), ctx.stream));
+    launch_batch_advect(ctx, job_class, v, ctx.batch_jobs.as<const batch_job_device>(), count, pools, counters);
+  };
+
+  if (variant < 0 && ctx.batch_variant[job_class] < 0)
+  {
+    std::vector<long long> full(count);
+    for (int j = 0; j < count; ++j) { full[j] = jobs[j].seed_count; jobs[j].seed_count = std::min(full[j], 16384LL); }
+    cudaEvent_t a, b;
+    PARS_CUDA(cudaEventCreate(&a));
+    PARS_CUDA(cudaEventCreate(&b));
+    float best = 0.0f;
+    int best_v = 1;
+    for (int v = 0; v < batch_variant_count(); ++v)
+    {
+      float fastest = 0.0f;
+      for (int rep = 0; rep < 2; ++rep)
+      {
+        PARS_CUDA(cudaEventRecord(a, ctx.stream));
+        run(v);
+        PARS_CUDA(cudaEventRecord(b, ctx.stream));
+        PARS_CUDA(cudaEventSynchronize(b));
+        float ms = 0.0f;
+        PARS_CUDA(cudaEventElapsedTime(&ms, a, b));
+        fastest = rep == 0 ? ms : std::min(fastest, ms);
+      }
+      if (v == 0 || fastest < best) { best = fastest; best_v = v; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    ctx.batch_variant[job_class] = best_v;
+    for (int j = 0; j < count; ++j) jobs[j].seed_count = full[j];
+  }
+  run(variant >= 0 ? variant : ctx.batch_variant[job_class]);
+  std::vector<unsigned long long> steps(count + 1);
+  PARS_CUDA(cudaMemcpyAsync(steps.data(), counters, sizeof(unsigned long long) * (count + 1), cudaMemcpyDeviceToHost, ctx.stream));
+  PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+  return std::vector<unsigned long long>(steps.begin() + 1, steps.end());
+}
+
 std::size_t checked_bytes(long long count, std::size_t element)
 {
   PARS_REQUIRE(count >= 0, "negative count");
@@ -925,16 +988,42 @@ int32_t pars_gpu_flow_map_generate(pars_gpu_context* ctx, int32_t field, int32_t
     // when the seed lattice covers the flow map every voxel is written.
     if (seeds[0] < entry->shape[0] || seeds[1] < entry->shape[1] || seeds[2] < entry->shape[2])
       PARS_CUDA(cudaMemsetAsync(entry->data.get(), 0xff, sizeof(float4) * voxels, ctx->stream));
-    ctx->counters.reserve(sizeof(unsigned long long) * 2);
-    auto* counter = ctx->counters.as<unsigned long long>();
-    PARS_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
-    launch_flow_map(*ctx, f.view(), rule, iterations, f.offset, entry->spacing, seeds, entry->shape, entry->data.as<float4>(), counter);
-    if (steps)
+    if (rule.frozen || iterations <= 1)
     {
-      unsigned long long s = 0;
-      PARS_CUDA(cudaMemcpyAsync(&s, counter, sizeof(s), cudaMemcpyDeviceToHost, ctx->stream));
-      PARS_CUDA(cudaStreamSynchronize(ctx->stream));
-      *steps = (int64_t)s;
+      // The reference's scheme, bit for bit (and the iterations <= 1 case,
+      // where every voxel keeps its seed position).
+      ctx->counters.reserve(sizeof(unsigned long long) * 2);
+      auto* counter = ctx->counters.as<unsigned long long>();
+      PARS_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
+      launch_flow_map(*ctx, f.view(), rule, iterations, f.offset, entry->spacing, seeds, entry->shape, entry->data.as<float4>(), counter);
+      if (steps)
+      {
+        unsigned long long s = 0;
+        PARS_CUDA(cudaMemcpyAsync(&s, counter, sizeof(s), cudaMemcpyDeviceToHost, ctx->stream));
+        PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+        *steps = (int64_t)s;
+      }
+    }
+    else
+    {
+      // Re-sampled stages: one job of the persistent batched engine.
+      std::vector<batch_job_device> job(1);
+      batch_job_device& d = job[0];
+      d.field = f.view();
+      d.time = f.time();
+      d.rule = rule;
+      d.max_steps = iterations - 1;
+      d.time_begin = f.t0;
+      d.seeds = nullptr;
+      d.seed_count = (long long)seeds[0] * seeds[1] * seeds[2];
+      d.ox = f.offset[0]; d.oy = f.offset[1]; d.oz = f.offset[2];
+      d.sx = entry->spacing[0]; d.sy = entry->spacing[1]; d.sz = entry->spacing[2];
+      d.px = seeds[0]; d.py = seeds[1]; d.pz = seeds[2];
+      d.ux = entry->shape[0]; d.uy = entry->shape[1]; d.uz = entry->shape[2];
+      d.end_positions = entry->data.as<float4>();
+      d.end_steps = nullptr;
+      const auto s = execute_batch(*ctx, job, f.slices > 1 ? 1 : 0, -1);
+      if (steps) *steps = (int64_t)s[0];
     }
     *flow_map = add_field(*ctx, std::move(entry));
   });
@@ -989,6 +1078,9 @@ int32_t pars_gpu_batch_advect(pars_gpu_context* ctx, pars_gpu_batch_job* jobs, i
       d.field = f.view();
       d.time = f.time();
       d.rule = make_rule(in.integrator, in.stage_mode, in.step_size);
+      if (d.rule.frozen)
+        throw error(PARS_ERR_UNSUPPORTED, "batched advection integrates with re-sampled stages (PARS_STAGES_RESAMPLED)");
+      d.ux = d.uy = d.uz = 0;
       PARS_REQUIRE(in.max_steps >= 0, "max_steps must be >= 0");
       d.max_steps = in.max_steps;
       d.time_begin = in.time_begin;
@@ -1006,66 +1098,8 @@ int32_t pars_gpu_batch_advect(pars_gpu_context* ctx, pars_gpu_batch_job* jobs, i
       d.end_steps = in.end_steps;
       unsteady = unsteady || f.slices > 1;
     }
-    const int job_class = unsteady ? 1 : 0;
-    ctx->batch_jobs.reserve(sizeof(batch_job_device) * count);
-    ctx->batch_counters.reserve(sizeof(unsigned long long) * (count + 1));
-    auto* counters = ctx->batch_counters.as<unsigned long long>();
-
-    // Chunk prefixes depend on the launch shape (seeds per chunk = threads).
-    auto run = [&](int v) {
-      const int threads = batch_variant_threads(v);
-      long long chunks = 0;
-      for (int j = 0; j < count; ++j)
-      {
-        device_jobs[j].first_chunk = chunks;
-        device_jobs[j].steps = counters + 1 + j;
-        chunks += (device_jobs[j].seed_count + threads - 1) / threads;
-      }
-      PARS_CUDA(cudaMemcpyAsync(ctx->batch_jobs.get(), device_jobs.data(), sizeof(batch_job_device) * count, cudaMemcpyHostToDevice, ctx->stream));
-      PARS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (count + 1), ctx->stream));
-      launch_batch_advect(*ctx, job_class, v, ctx->batch_jobs.as<const batch_job_device>(), count, chunks, counters);
-    };
-
-    if (variant < 0 && ctx->batch_variant[job_class] < 0)
-    {
-      // Autotune on a probe: every job capped at 16384 seeds, each variant
-      // timed twice with CUDA events, the fastest kept for this job class.
-      std::vector<long long> full(count);
-      for (int j = 0; j < count; ++j) { full[j] = device_jobs[j].seed_count; device_jobs[j].seed_count = std::min(full[j], 16384LL); }
-      std::vector<float4*> outputs(count);
-      std::vector<int*> step_outputs(count);
-      for (int j = 0; j < count; ++j) { outputs[j] = device_jobs[j].end_positions; step_outputs[j] = device_jobs[j].end_steps; }
-      cudaEvent_t a, b;
-      PARS_CUDA(cudaEventCreate(&a));
-      PARS_CUDA(cudaEventCreate(&b));
-      float best = 0.0f;
-      int best_v = 1;
-      for (int v = 0; v < batch_variant_count(); ++v)
-      {
-        float fastest = 0.0f;
-        for (int rep = 0; rep < 2; ++rep)
-        {
-          PARS_CUDA(cudaEventRecord(a, ctx->stream));
-          run(v);
-          PARS_CUDA(cudaEventRecord(b, ctx->stream));
-          PARS_CUDA(cudaEventSynchronize(b));
-          float ms = 0.0f;
-          PARS_CUDA(cudaEventElapsedTime(&ms, a, b));
-          fastest = rep == 0 ? ms : std::min(fastest, ms);
-        }
-        if (v == 0 || fastest < best) { best = fastest; best_v = v; }
-      }
-      cudaEventDestroy(a);
-      cudaEventDestroy(b);
-      ctx->batch_variant[job_class] = best_v;
-      for (int j = 0; j < count; ++j) device_jobs[j].seed_count = full[j];
-    }
-    const int chosen = variant >= 0 ? variant : ctx->batch_variant[job_class];
-    run(chosen);
-    std::vector<unsigned long long> steps(count + 1);
-    PARS_CUDA(cudaMemcpyAsync(steps.data(), counters, sizeof(unsigned long long) * (count + 1), cudaMemcpyDeviceToHost, ctx->stream));
-    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
-    for (int j = 0; j < count; ++j) jobs[j].steps = (int64_t)steps[1 + j];
+    const std::vector<unsigned long long> steps = execute_batch(*ctx, device_jobs, unsteady ? 1 : 0, variant);
+    for (int j = 0; j < count; ++j) jobs[j].steps = (int64_t)steps[j];
   });
 }
 

@@ -45,6 +45,16 @@ class TraceSummary(ctypes.Structure):
                 ("rounds", ctypes.c_int32), ("padding", ctypes.c_int32)]
 
 
+class BatchJob(ctypes.Structure):
+    """pars_gpu_batch_job (include/pars_gpu.h)."""
+    _fields_ = [("field", ctypes.c_int32), ("integrator", ctypes.c_int32), ("stage_mode", ctypes.c_int32),
+                ("max_steps", ctypes.c_int32), ("step_size", ctypes.c_float), ("padding0", ctypes.c_int32),
+                ("time_begin", ctypes.c_double), ("seeds", ctypes.c_void_p), ("seed_count", ctypes.c_int64),
+                ("lattice_offset", ctypes.c_float * 3), ("lattice_stride", ctypes.c_float * 3),
+                ("lattice_count", ctypes.c_int32 * 3), ("padding1", ctypes.c_int32),
+                ("end_positions", ctypes.c_void_p), ("end_steps", ctypes.c_void_p), ("steps", ctypes.c_int64)]
+
+
 class ParsGpuError(RuntimeError):
     def __init__(self, status, message):
         super().__init__(f"{STATUS.get(status, status)} ({status}): {message}")
@@ -88,6 +98,11 @@ SIGNATURES = {
     "pars_gpu_ftle_generate": [_P, _I32, _F, _I32, _P],
     "pars_gpu_ftle_device_pointer": [_P, ctypes.POINTER(_P), ctypes.POINTER(_I64)],
     "pars_gpu_ftle_no_alloc": [_P, _P, _P, _P, _P, _I32, _I32, _I32, _F, _F, _I32, _P, _P, _P],
+    "pars_gpu_unsteady_field_upload": [_P, _P, _P, _I32, _P, _P, _P, ctypes.c_double, ctypes.c_double, ctypes.POINTER(_I32)],
+    "pars_gpu_unsteady_field_upload_device": [_P, _P, _P, _I32, _P, _P, _P, ctypes.c_double, ctypes.c_double, ctypes.POINTER(_I32)],
+    "pars_gpu_batch_advect": [_P, _P, _I32, _I32],
+    "pars_gpu_batch_variants": [_P, ctypes.POINTER(_I32)],
+    "pars_gpu_batch_tuned": [_P, _I32, ctypes.POINTER(_I32), ctypes.POINTER(_I32)],
     "pars_gpu_profile_enable": [_P, _I32],
     "pars_gpu_profile_reset": [_P],
     "pars_gpu_profile_get": [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)],
@@ -315,6 +330,36 @@ class Context:
         p, n = _P(), _I64()
         self._call("pars_gpu_ftle_device_pointer", ctypes.byref(p), ctypes.byref(n))
         return p.value, n.value
+
+    # -- unsteady fields / batched advection -------------------------------------------
+    def upload_unsteady_field(self, xyz, offset, spacing, t0, slice_dt, size=None):
+        """xyz: [slices, X, Y, Z, 3] FP32 host array."""
+        xyz = np.ascontiguousarray(xyz, np.float32)
+        dims = np.array(xyz.shape[1:4], np.int32)
+        o, sp = _f3(offset), _f3(spacing)
+        s = _f3(size) if size is not None else (dims.astype(np.float32) * sp).astype(np.float32)
+        h = _I32()
+        self._call("pars_gpu_unsteady_field_upload", _ptr(xyz), _ptr(dims), xyz.shape[0], _ptr(o), _ptr(s), _ptr(sp),
+                   t0, slice_dt, ctypes.byref(h))
+        return h.value
+
+    def upload_unsteady_field_device(self, device_ptr, dims, slices, offset, size, spacing, t0, slice_dt):
+        h = _I32()
+        d, o, s, sp = _i3(dims), _f3(offset), _f3(size), _f3(spacing)
+        self._call("pars_gpu_unsteady_field_upload_device", device_ptr, _ptr(d), slices, _ptr(o), _ptr(s), _ptr(sp),
+                   t0, slice_dt, ctypes.byref(h))
+        return h.value
+
+    def batch_advect(self, jobs, variant=-1):
+        """jobs: list of BatchJob; returns the per-job step counts."""
+        arr = (BatchJob * len(jobs))(*jobs)
+        self._call("pars_gpu_batch_advect", ctypes.cast(arr, ctypes.c_void_p), len(jobs), variant)
+        return [arr[i].steps for i in range(len(jobs))]
+
+    def batch_tuned(self, job_class):
+        v, t = _I32(), _I32()
+        self._call("pars_gpu_batch_tuned", job_class, ctypes.byref(v), ctypes.byref(t))
+        return v.value, t.value
 
     # -- instrumentation ----------------------------------------------------------------
     def profile_enable(self, on=True):

@@ -82,6 +82,44 @@ def uniform_field(n, velocity, spacing=0.25):
     return Field(xyz, np.zeros(3, np.float32), np.full(3, np.float32(spacing), np.float32))
 
 
+def double_gyre_slices(n, slices, period=10.0, A=0.1, eps=0.25):
+    """Unsteady 3-D double gyre on [0,2] x [0,1] x [0,1] sampled at n^3
+    vertices and `slices` times spanning one period (t_k = k * period /
+    (slices - 1)); omega = 2 pi / period, w = 0:
+        f(x,t) = eps sin(wt) x^2 + (1 - 2 eps sin(wt)) x
+        u = -pi A sin(pi f) cos(pi y),  v = pi A cos(pi f) sin(pi y) df/dx.
+    Returns (xyz [slices, n, n, n, 3] FP32, offset, spacing, t0, slice_dt)."""
+    omega = 2.0 * np.pi / period
+    x = np.linspace(0.0, 2.0, n)
+    y = np.linspace(0.0, 1.0, n)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    out = np.zeros((slices, n, n, n, 3), np.float32)
+    dt = period / (slices - 1)
+    for k in range(slices):
+        t = k * dt
+        a = eps * np.sin(omega * t)
+        b = 1.0 - 2.0 * a
+        f = a * X * X + b * X
+        dfdx = 2.0 * a * X + b
+        u = -np.pi * A * np.sin(np.pi * f) * np.cos(np.pi * Y)
+        v = np.pi * A * np.cos(np.pi * f) * np.sin(np.pi * Y) * dfdx
+        out[k, :, :, :, 0] = u[:, :, None]
+        out[k, :, :, :, 1] = v[:, :, None]
+    spacing = np.array([2.0 / (n - 1), 1.0 / (n - 1), 1.0 / (n - 1)], np.float32)
+    return out, np.zeros(3, np.float32), spacing, 0.0, dt
+
+
+def pathline_batch_config(seed=3, fields=32):
+    """The batched-pathline workload: `fields` double-gyre fields with edge
+    log-uniform in [32, 256], 16-64 slices, seed counts log-uniform in
+    [1k, 512k], drawn with numpy's PCG64 from `seed`."""
+    rng = np.random.default_rng(seed)
+    edges = np.exp(rng.uniform(np.log(32), np.log(256), fields)).astype(int)
+    slices = rng.integers(16, 65, fields)
+    seeds = np.exp(rng.uniform(np.log(1000), np.log(512 * 1024), fields)).astype(int)
+    return [{"edge": int(e), "slices": int(s), "seeds": int(c)} for e, s, c in zip(edges, slices, seeds)]
+
+
 def streamline_config():
     """The plain streamline workload: 64^3 ABC, seeds on a stride-4 lattice
     (16^3), RK4 h = 0.01, 1000 steps (remaining_iterations = 1002: seed, at most
