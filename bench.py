@@ -46,6 +46,8 @@ def parse_args():
     p.add_argument("--size", type=int, default=256)
     p.add_argument("--iterations", type=int, default=501)
     p.add_argument("--cpu-sample", type=int, default=1048576, help="seeds in the CPU baseline's bounded sample")
+    p.add_argument("--workload", choices=["ftle", "streamlines", "domain", "pathlines"], default="ftle",
+                   help="ftle: the headline line; the others print one line for the other workloads")
     return p.parse_args()
 
 
@@ -136,8 +138,148 @@ def cpu_reference_run(field, iterations, sample, steps, warmup):
     return total / dt, threads, dt
 
 
+def _events_time(torch, stream, fn):
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    out = fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return out, a.elapsed_time(b) * 1e-3
+
+
+def run_streamlines(args):
+    """The plain streamline workload: 64^3 ABC, 4096 seeds (stride 4), RK4
+    h = 0.01, 1000 steps, rgb colours and indices; frozen (the reference's
+    scheme) and re-sampled RK4."""
+    import torch
+    import oracle
+    from pars_gb300 import native, workloads
+    cfg = workloads.streamline_config()
+    f = cfg["field"]
+    ctx = native.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    seeds = ctx.seed_generate(f.offset, f.size, cfg["stride"], cfg["iterations"])
+    h = ctx.upload_field(f)
+    out = {}
+    for name, mode in (("frozen", native.STAGES_FROZEN), ("resampled", native.STAGES_RESAMPLED)):
+        def once():
+            s = ctx.trace(h, seeds, native.RUNGE_KUTTA_4, mode, cfg["step"])
+            ctx.curves_index()
+            ctx.curves_color("rgb")
+            return s
+        for _ in range(max(args.warmup, 3)):
+            once()
+        total, t = 0, 0.0
+        for _ in range(args.steps):
+            s, dt = _events_time(torch, stream, once)
+            total += s["steps"]
+            t += dt
+        out[name] = total / t
+        out[name + "_ms"] = 1e3 * t / args.steps
+    port = oracle.port()
+    t0 = time.perf_counter()
+    ref = port.trace_single(f, seeds, 2, cfg["step"], "rgb", 0.5)
+    cpu = ref.steps / (time.perf_counter() - t0)
+    print(json.dumps({"workload": "streamlines_64: 64^3 ABC, 4096 seeds, RK4 h=0.01, <=1000 steps, index + rgb colour",
+                      "metric": METRIC, "unit": UNIT, "value": out["resampled"], "ms_per_call_resampled": out["resampled_ms"],
+                      "frozen_velocity_steps_per_s": out["frozen"], "ms_per_call_frozen": out["frozen_ms"],
+                      "steps_per_call": ref.steps, "cpu_port_steps_per_s": cpu, "cpu_threads": port.max_threads()}))
+    ctx.close()
+
+
+def run_domain(args):
+    """The partitioned workload: 512^3 Arnold-Beltrami field + 8 Fourier modes
+    (seed 1) split 4x4x4 into 64 blocks on one GPU; 1M seeds from a 4-centre
+    Gaussian mixture (sigma = 0.05 of the domain, seed 2); RK4 h = 0.005,
+    2000 steps; particles handed between blocks each round on the device."""
+    import torch
+    from pars_gb300 import native, workloads
+    n = args.size if args.size != 256 else 512
+    ctx = native.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    xyz, spacing = workloads.beltrami_fourier_device(torch, n, seed=1)
+    ranks = 64
+    d = ctx.domain_create_device(xyz.data_ptr(), (n, n, n), spacing, ranks)
+    del xyz
+    torch.cuda.empty_cache()
+    info = native.partition(ranks, 0, (n, n, n))
+    seeds, offsets = workloads.gaussian_mixture_seeds(1_000_000, n, spacing, info, remaining=2002, seed=2)
+    s, dt = None, 0.0
+    for _ in range(max(args.warmup, 1)):
+        ctx.trace_domain(d, seeds, offsets, native.RUNGE_KUTTA_4, native.STAGES_RESAMPLED, 0.005)
+    total, t = 0, 0.0
+    for _ in range(args.steps):
+        s, dt = _events_time(torch, stream, lambda: ctx.trace_domain(d, seeds, offsets, native.RUNGE_KUTTA_4,
+                                                                     native.STAGES_RESAMPLED, 0.005))
+        total += s["steps"]
+        t += dt
+    print(json.dumps({"workload": f"domain_{n}: {n}^3 Arnold-Beltrami + 8 Fourier modes, 64 blocks (4x4x4) on one GPU, "
+                                  "1M Gaussian-mixture seeds, RK4 h=0.005, <=2000 steps, device handoff queues",
+                      "metric": METRIC, "unit": UNIT, "value": total / t, "ms_per_step": 1e3 * t / args.steps,
+                      "steps_per_run": s["steps"], "rounds": s["rounds"], "batches": s["batches"],
+                      "vertices": s["vertices"]}))
+    ctx.domain_release(d)
+    ctx.close()
+
+
+def run_pathlines(args):
+    """The batched-pathline workload: 32 unsteady double-gyre fields (edge
+    log-uniform 32-256, 16-64 slices, seed counts log-uniform 1k-512k; seed 3),
+    classical RK4 in space-time, h = 0.01 over one period (1000 steps), all
+    fields in one persistent launch with the autotuned launch shape."""
+    import torch
+    from pars_gb300 import native, workloads
+    ctx = native.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    specs = workloads.pathline_batch_config(seed=3)
+    jobs, keep = [], []
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(3)
+    field_bytes = 0
+    for spec in specs:
+        xyz, offset, spacing, t0, dt = workloads.double_gyre_device(torch, spec["edge"], spec["slices"])
+        n = spec["edge"]
+        h = ctx.upload_unsteady_field_device(xyz.data_ptr(), (n, n, n), spec["slices"], offset,
+                                              (np.array([n, n, n], np.float32) * spacing), spacing, t0, dt)
+        field_bytes += n ** 3 * spec["slices"] * 16
+        del xyz
+        c = spec["seeds"]
+        seeds = torch.zeros((c, 4), dtype=torch.float32, device="cuda")
+        seeds[:, 0] = 0.05 + 1.9 * torch.rand(c, device="cuda", generator=gen)
+        seeds[:, 1] = 0.05 + 0.9 * torch.rand(c, device="cuda", generator=gen)
+        seeds[:, 2] = 0.05 + 0.9 * torch.rand(c, device="cuda", generator=gen)
+        end = torch.empty((c, 4), dtype=torch.float32, device="cuda")
+        j = native.BatchJob()
+        j.field, j.integrator, j.stage_mode, j.max_steps, j.step_size = h, native.RUNGE_KUTTA_4, native.STAGES_RESAMPLED, 1000, 0.01
+        j.time_begin, j.seeds, j.seed_count, j.end_positions = 0.0, seeds.data_ptr(), c, end.data_ptr()
+        jobs.append(j)
+        keep.append((seeds, end))
+    torch.cuda.empty_cache()
+    ctx.batch_advect(jobs)   # tunes the launch shape on first use
+    for _ in range(max(args.warmup - 1, 1)):
+        ctx.batch_advect(jobs)
+    total, t = 0, 0.0
+    for _ in range(args.steps):
+        steps, dt = _events_time(torch, stream, lambda: ctx.batch_advect(jobs))
+        total += sum(steps)
+        t += dt
+    variant, threads = ctx.batch_tuned(1)
+    print(json.dumps({"workload": "pathlines_32: 32 unsteady double-gyre fields (edge 32-256 log-uniform, 16-64 slices, "
+                                  "1k-512k seeds log-uniform, seed 3), RK4 in space-time h=0.01, <=1000 steps, one persistent launch",
+                      "metric": METRIC, "unit": UNIT, "value": total / t, "ms_per_step": 1e3 * t / args.steps,
+                      "steps_per_run": total // args.steps, "seeds": sum(s["seeds"] for s in specs),
+                      "field_bytes": field_bytes, "tuned_variant": variant, "threads_per_cta": threads}))
+    ctx.close()
+
+
 def main():
     args = parse_args()
+    if args.workload != "ftle":
+        {"streamlines": run_streamlines, "domain": run_domain, "pathlines": run_pathlines}[args.workload](args)
+        return
     rank, world, local = dist_env()
     from pars_gb300 import workloads
 

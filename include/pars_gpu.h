@@ -186,6 +186,9 @@ int32_t pars_gpu_trace_device(pars_gpu_context* context, int32_t field, const pa
  * size = block_size * spacing (data_io.cpp:91-115).  *domain receives a handle. */
 int32_t pars_gpu_domain_create (pars_gpu_context* context, const float* xyz, const int32_t domain_size[3],
                                 const float spacing[3], int32_t ranks, int32_t* domain);
+/* Same, from a DEVICE copy of the domain field. */
+int32_t pars_gpu_domain_create_device(pars_gpu_context* context, const float* device_xyz, const int32_t domain_size[3],
+                                      const float spacing[3], int32_t ranks, int32_t* domain);
 int32_t pars_gpu_domain_release(pars_gpu_context* context, int32_t domain);
 /* Traces seeds over a partitioned domain: rank r's seeds are
  * particles[seed_offsets[r] .. seed_offsets[r+1]).  Every round each block

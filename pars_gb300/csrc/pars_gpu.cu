@@ -761,6 +761,56 @@ int32_t pars_gpu_trace_device(pars_gpu_context* ctx, int32_t field, const pars_p
   });
 }
 
+namespace
+{
+// Splits a DEVICE [X][Y][Z][3] domain field into the partitioner's ghosted
+// blocks (data_io.cpp:91-115 without the file) and registers the domain.
+int32_t build_domain(pars_gpu_context* ctx, const float* device_xyz, const int32_t domain_size[3], const float spacing[3], int32_t ranks)
+{
+  auto entry = std::make_unique<domain_entry>();
+  entry->ranks = ranks;
+  entry->first = partition_of(ranks, 0, domain_size);
+  for (int i = 0; i < 3; ++i) PARS_REQUIRE(entry->first.block_size[i] >= 1, "more blocks than voxels along an axis");
+  for (int r = 0; r < ranks; ++r)
+  {
+    const pars_partition_info info = partition_of(ranks, r, domain_size);
+    auto f = std::make_unique<field_entry>();
+    for (int i = 0; i < 3; ++i)
+    {
+      f->shape[i] = info.ghosted_block_size[i];
+      f->spacing[i] = spacing[i];
+      f->offset[i] = float(info.offset[i]) * spacing[i];          // data_io.cpp:113
+      f->size[i] = float(info.block_size[i]) * spacing[i];        // data_io.cpp:114
+    }
+    for (int i = 0; i < 3; ++i) PARS_REQUIRE(f->shape[i] >= 2, "blocks must be at least 2 voxels wide");
+    f->data = acquire_buffer(*ctx, sizeof(float4) * (std::size_t)f->shape[0] * f->shape[1] * f->shape[2]);
+    launch_extract_block(*ctx, device_xyz, domain_size, info.offset, f->shape, f->data.as<float4>());
+    trace_block b;
+    b.field = f->view();
+    for (int face = 0; face < 6; ++face) b.neighbor[face] = info.neighbor_rank[face];
+    entry->blocks.push_back(b);
+    entry->fields.push_back(add_field(*ctx, std::move(f)));
+  }
+  entry->device_blocks.reserve(sizeof(trace_block) * ranks);
+  PARS_CUDA(cudaMemcpyAsync(entry->device_blocks.get(), entry->blocks.data(), sizeof(trace_block) * ranks, cudaMemcpyHostToDevice, ctx->stream));
+  PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int32_t handle = ctx->next_handle++;
+  ctx->domains[handle] = std::move(entry);
+  return handle;
+}
+}
+
+int32_t pars_gpu_domain_create_device(pars_gpu_context* ctx, const float* device_xyz, const int32_t domain_size[3], const float spacing[3],
+                                      int32_t ranks, int32_t* domain)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(device_xyz && domain_size && spacing && domain, "device_xyz, domain_size, spacing and domain are required");
+    PARS_REQUIRE(ranks >= 1, "ranks must be >= 1");
+    check_field_args(domain_size, spacing);
+    *domain = build_domain(ctx, device_xyz, domain_size, spacing, ranks);
+  });
+}
+
 int32_t pars_gpu_domain_create(pars_gpu_context* ctx, const float* xyz, const int32_t domain_size[3], const float spacing[3],
                                int32_t ranks, int32_t* domain)
 {
@@ -768,39 +818,10 @@ int32_t pars_gpu_domain_create(pars_gpu_context* ctx, const float* xyz, const in
     PARS_REQUIRE(xyz && domain_size && spacing && domain, "xyz, domain_size, spacing and domain are required");
     PARS_REQUIRE(ranks >= 1, "ranks must be >= 1");
     check_field_args(domain_size, spacing);
-    auto entry = std::make_unique<domain_entry>();
-    entry->ranks = ranks;
-    entry->first = partition_of(ranks, 0, domain_size);
-    for (int i = 0; i < 3; ++i) PARS_REQUIRE(entry->first.block_size[i] >= 1, "more blocks than voxels along an axis");
     const long long total = (long long)domain_size[0] * domain_size[1] * domain_size[2];
     ctx->staging.reserve(sizeof(float) * 3 * total);
     PARS_CUDA(cudaMemcpyAsync(ctx->staging.get(), xyz, sizeof(float) * 3 * total, cudaMemcpyHostToDevice, ctx->stream));
-    for (int r = 0; r < ranks; ++r)
-    {
-      const pars_partition_info info = partition_of(ranks, r, domain_size);
-      auto f = std::make_unique<field_entry>();
-      for (int i = 0; i < 3; ++i)
-      {
-        f->shape[i] = info.ghosted_block_size[i];
-        f->spacing[i] = spacing[i];
-        f->offset[i] = float(info.offset[i]) * spacing[i];          // data_io.cpp:113
-        f->size[i] = float(info.block_size[i]) * spacing[i];        // data_io.cpp:114
-      }
-      for (int i = 0; i < 3; ++i) PARS_REQUIRE(f->shape[i] >= 2, "blocks must be at least 2 voxels wide");
-      f->data = acquire_buffer(*ctx, sizeof(float4) * (std::size_t)f->shape[0] * f->shape[1] * f->shape[2]);
-      launch_extract_block(*ctx, ctx->staging.as<const float>(), domain_size, info.offset, f->shape, f->data.as<float4>());
-      trace_block b;
-      b.field = f->view();
-      for (int face = 0; face < 6; ++face) b.neighbor[face] = info.neighbor_rank[face];
-      entry->blocks.push_back(b);
-      entry->fields.push_back(add_field(*ctx, std::move(f)));
-    }
-    entry->device_blocks.reserve(sizeof(trace_block) * ranks);
-    PARS_CUDA(cudaMemcpyAsync(entry->device_blocks.get(), entry->blocks.data(), sizeof(trace_block) * ranks, cudaMemcpyHostToDevice, ctx->stream));
-    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
-    const int32_t handle = ctx->next_handle++;
-    ctx->domains[handle] = std::move(entry);
-    *domain = handle;
+    *domain = build_domain(ctx, ctx->staging.as<const float>(), domain_size, spacing, ranks);
   });
 }
 

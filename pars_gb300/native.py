@@ -87,6 +87,7 @@ SIGNATURES = {
     "pars_gpu_trace_device": [_P, _I32, _P, _I64, _I32, _I32, _F, ctypes.POINTER(TraceSummary)],
     "pars_gpu_domain_create": [_P, _P, _P, _P, _I32, ctypes.POINTER(_I32)],
     "pars_gpu_domain_release": [_P, _I32],
+    "pars_gpu_domain_create_device": [_P, _P, _P, _P, _I32, ctypes.POINTER(_I32)],
     "pars_gpu_trace_domain": [_P, _I32, _P, _P, _I32, _I32, _F, ctypes.POINTER(TraceSummary)],
     "pars_gpu_curves_index": [_P],
     "pars_gpu_curves_color": [_P, _I32, _F],
@@ -260,6 +261,12 @@ class Context:
     def domain_create(self, field, ranks):
         h = _I32()
         self._call("pars_gpu_domain_create", _ptr(field.xyz), _ptr(field.dims), _ptr(field.spacing), ranks, ctypes.byref(h))
+        return h.value
+
+    def domain_create_device(self, device_ptr, dims, spacing, ranks):
+        h = _I32()
+        d, sp = _i3(dims), _f3(spacing)
+        self._call("pars_gpu_domain_create_device", device_ptr, _ptr(d), _ptr(sp), ranks, ctypes.byref(h))
         return h.value
 
     def domain_release(self, handle):

@@ -120,6 +120,95 @@ def pathline_batch_config(seed=3, fields=32):
     return [{"edge": int(e), "slices": int(s), "seeds": int(c)} for e, s, c in zip(edges, slices, seeds)]
 
 
+def double_gyre_device(torch, n, slices, period=10.0, A=0.1, eps=0.25):
+    """double_gyre_slices computed on the GPU with torch (the 32-field
+    workload holds ~48 GB of slices; building them on the host would dominate
+    the run).  Returns (xyz device tensor [slices, n, n, n, 3] FP32, offset,
+    spacing, t0, slice_dt)."""
+    omega = 2.0 * np.pi / period
+    x = torch.linspace(0.0, 2.0, n, dtype=torch.float64, device="cuda")
+    y = torch.linspace(0.0, 1.0, n, dtype=torch.float64, device="cuda")
+    X, Y = torch.meshgrid(x, y, indexing="ij")
+    out = torch.zeros((slices, n, n, n, 3), dtype=torch.float32, device="cuda")
+    dt = period / (slices - 1)
+    for k in range(slices):
+        t = k * dt
+        a = eps * np.sin(omega * t)
+        b = 1.0 - 2.0 * a
+        f = a * X * X + b * X
+        dfdx = 2.0 * a * X + b
+        u = -np.pi * A * torch.sin(np.pi * f) * torch.cos(np.pi * Y)
+        v = np.pi * A * torch.cos(np.pi * f) * torch.sin(np.pi * Y) * dfdx
+        out[k, :, :, :, 0] = u.float()[:, :, None]
+        out[k, :, :, :, 1] = v.float()[:, :, None]
+    spacing = np.array([2.0 / (n - 1), 1.0 / (n - 1), 1.0 / (n - 1)], np.float32)
+    return out, np.zeros(3, np.float32), spacing, 0.0, dt
+
+
+def fourier_modes(seed=1, modes=8, amplitude=0.1):
+    """Random Fourier perturbation: integer wave vectors in [-4, 4]^3 (non-zero),
+    random unit directions and phases; each mode has amplitude
+    amplitude / sqrt(modes), so the sum has RMS amplitude about amplitude/sqrt(2)."""
+    rng = np.random.default_rng(seed)
+    k = rng.integers(-4, 5, (modes, 3))
+    k[np.all(k == 0, axis=1)] = (1, 0, 0)
+    d = rng.normal(size=(modes, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    phase = rng.uniform(0.0, 2.0 * np.pi, modes)
+    return k.astype(np.float64), d, phase, amplitude / np.sqrt(modes)
+
+
+def beltrami_fourier_device(torch, n, seed=1):
+    """ABC (Arnold-Beltrami) flow on the n^3 vertices of [0, 2pi]^3 plus
+    fourier_modes(seed), computed slab by slab on the GPU.  Returns (xyz device
+    tensor [n, n, n, 3] FP32, spacing)."""
+    h = 2.0 * np.pi / (n - 1)
+    c = torch.arange(n, dtype=torch.float64, device="cuda") * h
+    Y, Z = torch.meshgrid(c, c, indexing="ij")
+    k, d, phase, amp = fourier_modes(seed)
+    out = torch.empty((n, n, n, 3), dtype=torch.float32, device="cuda")
+    for i in range(n):
+        x = float(c[i])
+        u = ABC_A * torch.sin(Z) + ABC_C * torch.cos(Y)
+        v = ABC_B * np.sin(x) + ABC_A * torch.cos(Z)
+        w = ABC_C * torch.sin(Y) + ABC_B * np.cos(x)
+        for m in range(len(k)):
+            s = amp * torch.sin(k[m, 0] * x + k[m, 1] * Y + k[m, 2] * Z + phase[m])
+            u = u + d[m, 0] * s
+            v = v + d[m, 1] * s
+            w = w + d[m, 2] * s
+        out[i, :, :, 0] = u.float()
+        out[i, :, :, 1] = v.float()
+        out[i, :, :, 2] = w.float()
+    return out, np.full(3, np.float32(h), np.float32)
+
+
+def gaussian_mixture_seeds(count, n, spacing, partition, remaining, seed=2, centres=4, sigma_fraction=0.05):
+    """`count` seeds from a `centres`-centre Gaussian mixture in [0, L)^3,
+    L = (n - 1) * spacing, sigma = sigma_fraction * L, clipped into the
+    domain; grouped by owning block of `partition` (the partitioner's grid).
+    Returns (particles sorted by owner, seed_offsets per block)."""
+    from .native import PARTICLE_DTYPE
+    rng = np.random.default_rng(seed)
+    L = float((n - 1) * spacing[0])
+    centre = rng.uniform(0.2 * L, 0.8 * L, (centres, 3))
+    which = rng.integers(0, centres, count)
+    p = centre[which] + rng.normal(0.0, sigma_fraction * L, (count, 3))
+    p = np.clip(p, 0.0, np.nextafter(L, 0.0)).astype(np.float32)
+    grid = partition["grid"]
+    extent = (spacing * partition["block"]).astype(np.float32)
+    multi = np.minimum((p / extent).astype(np.int64), grid - 1)
+    owner = (multi[:, 0] * grid[1] + multi[:, 1]) * grid[2] + multi[:, 2]
+    order = np.argsort(owner, kind="stable")
+    particles = np.zeros(count, PARTICLE_DTYPE)
+    particles["position"][:, :3] = p[order]
+    particles["remaining_iterations"] = remaining
+    particles["vector_field_index"] = -1
+    ranks = int(np.prod(grid))
+    offsets = np.concatenate([[0], np.cumsum(np.bincount(owner, minlength=ranks))]).astype(np.int64)
+    return particles, offsets
+
+
 def streamline_config():
     """The plain streamline workload: 64^3 ABC, seeds on a stride-4 lattice
     (16^3), RK4 h = 0.01, 1000 steps (remaining_iterations = 1002: seed, at most
