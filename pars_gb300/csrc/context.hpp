@@ -236,6 +236,7 @@ struct trace_launch
   int*                 written;
   int*                 kept;
   step_rule            rule;
+  const step_rule*     block_rules;   // per-block rules (same stage mode as `rule`), or nullptr
   int                  route_exits;   // 0: particles leaving the block are dropped
   pars_particle*       exit_particles;
   unsigned long long*  exit_keys;     // (destination block << 40) | particle index
@@ -292,6 +293,17 @@ int  batch_pool_seeds();
 // job_class 0: all jobs steady; 1: some job unsteady.
 void launch_batch_advect(pars_gpu_context& ctx, int job_class, int variant, const batch_job_device* jobs, int njobs,
                          long long total_chunks, unsigned long long* counter);
+
+// The tracing round loop over particles already in ctx.particles_in (grouped
+// by block, ctx.block_of when there are several blocks); fills ctx.curves.
+// device_block_rules (optional, one per block) override `rule`'s step size and
+// integrator per block; the stage mode of `rule` applies to every block.
+void trace_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, const trace_block* device_blocks, long long count,
+                  std::vector<long long> block_count, std::vector<int> block_max, const step_rule& rule, bool route_exits,
+                  pars_gpu_trace_summary* summary, const step_rule* device_block_rules = nullptr);
+// Batched advection of `jobs` in one persistent launch; returns each job's steps.
+std::vector<unsigned long long> run_batch(pars_gpu_context& ctx, std::vector<batch_job_device>& jobs, int job_class, int variant);
+pars_partition_info partition(int ranks, int rank, const int32_t domain[3]);
 
 void launch_flow_map(pars_gpu_context& ctx, const field_view& f, const step_rule& rule, int iterations,
                      const float offset[3], const float fm_spacing[3], const int seeds_per_dimension[3],

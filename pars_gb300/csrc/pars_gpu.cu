@@ -257,7 +257,8 @@ void grow_curves(pars_gpu_context& ctx, long long needed_vertices)
 // block_max give each block's particle count and maximum remaining_iterations.
 void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, const trace_block* device_blocks,
                 long long count, std::vector<long long> block_count, std::vector<int> block_max,
-                const step_rule& rule, bool route_exits, pars_gpu_trace_summary* summary)
+                const step_rule& rule, bool route_exits, pars_gpu_trace_summary* summary,
+                const step_rule* device_block_rules = nullptr)
 {
   auto& curves = ctx.curves;
   curves.batches.clear();
@@ -298,6 +299,7 @@ void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, c
     a.written = ctx.written.as<int>();
     a.kept = ctx.kept.as<int>();
     a.rule = rule;
+    a.block_rules = device_block_rules;
     a.route_exits = route_exits ? 1 : 0;
     a.exit_particles = route_exits ? ctx.exits.as<pars_particle>() : nullptr;
     a.exit_keys = route_exits ? ctx.exit_keys.as<unsigned long long>() : nullptr;
@@ -501,6 +503,21 @@ std::size_t checked_bytes(long long count, std::size_t element)
 }
 
 step_rule make_step_rule(int integrator, int stage_mode, float h) { return make_rule(integrator, stage_mode, h); }
+
+void trace_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, const trace_block* device_blocks, long long count,
+                  std::vector<long long> block_count, std::vector<int> block_max, const step_rule& rule, bool route_exits,
+                  pars_gpu_trace_summary* summary, const step_rule* device_block_rules)
+{
+  run_rounds(ctx, blocks, device_blocks, count, std::move(block_count), std::move(block_max), rule, route_exits, summary,
+             device_block_rules);
+}
+
+std::vector<unsigned long long> run_batch(pars_gpu_context& ctx, std::vector<batch_job_device>& jobs, int job_class, int variant)
+{
+  return execute_batch(ctx, jobs, job_class, variant);
+}
+
+pars_partition_info partition(int ranks, int rank, const int32_t domain[3]) { return partition_of(ranks, rank, domain); }
 }
 
 using namespace pars;

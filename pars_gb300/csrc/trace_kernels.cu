@@ -32,6 +32,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const trace_launch a)
   {
     const int block = a.block_of ? a.block_of[i] : 0;
     const field_view f = a.blocks[block].field;
+    const step_rule rule = a.block_rules ? a.block_rules[block] : a.rule;
     const float4* record = reinterpret_cast<const float4*>(a.particles + i);
     float4 last = record[0];
     const int N = __float_as_int(record[1].x);   // remaining_iterations
@@ -71,8 +72,8 @@ __global__ void __launch_bounds__(256) trace_kernel(const trace_launch a)
       }
       if (is_zero(v)) { out[it] = term; ++written; ++kept; break; }
       float4 next;
-      if (FROZEN) next = frozen_step(a.rule, last, v);
-      else { next = last; resampled_step_cached(f, cache, a.rule, next, lo, v); }
+      if (FROZEN) next = frozen_step(rule, last, v);
+      else { next = last; resampled_step_cached(f, cache, rule, next, lo, v); }
       out[it] = next;
       ++written;
       kept += is_invalid_vertex(next) ? 0 : 1;
