@@ -283,6 +283,75 @@ int32_t pars_gpu_batch_variants(pars_gpu_context* context, int32_t* count);
 /* The tuned variant of a job class (0 steady, 1 unsteady), -1 if not tuned yet. */
 int32_t pars_gpu_batch_tuned   (pars_gpu_context* context, int32_t job_class, int32_t* variant, int32_t* threads);
 
+/* ---- request service (pars_service, pars/source/service.cpp:20-69) ----------------
+ * Requests are the reference's binary proto3 `settings` messages
+ * (pars/proto/settings.proto).  `mode` is read as the reference reads it:
+ * containing "ftle" selects the FTLE pipeline (pipeline::execute_ftle),
+ * anything else streamlines (pipeline::execute: trace, prune, index, colour);
+ * "fractional_anisotropy" selects the FA measure.  Integration uses
+ * re-sampled RK4 stages; a mode containing "reference" traces streamlines
+ * with the reference's frozen-velocity scheme instead.  `dataset_filepath`
+ * names a dataset registered with pars_gpu_service_add_dataset.
+ *
+ * The service queues requests as they arrive.  `lanes` worker threads, each
+ * with its own CUDA stream, take batches of queued requests of one kind that
+ * fit into the device-memory budget (requests arriving while others run are
+ * admitted as memory frees up) and run each batch as one launch; results are
+ * copied to host memory before the batch's memory is returned. */
+typedef struct pars_gpu_service pars_gpu_service;
+
+/* The scalar fields of a decoded `settings` message (strings truncated). */
+typedef struct pars_gpu_settings_summary
+{
+  char    mode[64];
+  char    dataset_filepath[256];
+  char    particle_tracing_integrator[64];
+  char    color_generation_mode[64];
+  int32_t seed_generation_stride[3];
+  int32_t seed_generation_iterations;
+  float   particle_tracing_step_size;
+  int32_t particle_tracing_load_balance;
+  float   color_generation_free_parameter;
+  float   raytracing_camera_position[3];
+  int32_t raytracing_image_size[2];
+  float   raytracing_streamline_radius;
+  int32_t raytracing_iterations;
+} pars_gpu_settings_summary;
+
+typedef struct pars_gpu_request_info
+{
+  int32_t state;          /* 0 queued, 1 running, 2 done */
+  int32_t status;         /* PARS_OK or the failure */
+  int32_t kind;           /* 0 streamlines, 1 FTLE */
+  int32_t ftle_shape[3];
+  int64_t batches;        /* streamlines: integral_curves batches */
+  int64_t steps;          /* particle-steps taken */
+  double  queue_ms;       /* submit -> start */
+  double  run_ms;         /* start -> finish */
+  double  latency_ms;     /* submit -> finish */
+} pars_gpu_request_info;
+
+/* Decodes a `settings` message (host-only; no device needed). */
+int32_t pars_gpu_settings_decode     (const uint8_t* message, int64_t length, pars_gpu_settings_summary* settings);
+int32_t pars_gpu_service_create      (pars_gpu_service** service, int32_t device, int64_t budget_bytes, int32_t lanes,
+                                      int32_t max_batch);
+int32_t pars_gpu_service_destroy     (pars_gpu_service* service);
+/* Registers a dataset (HOST xyz [X][Y][Z][3], as pars_gpu_field_upload) under `name`. */
+int32_t pars_gpu_service_add_dataset (pars_gpu_service* service, const char* name, const float* xyz, const int32_t shape[3],
+                                      const float offset[3], const float size[3], const float spacing[3]);
+int32_t pars_gpu_service_submit      (pars_gpu_service* service, const uint8_t* message, int64_t length, int64_t* ticket);
+/* Waits up to timeout_ms (negative: no limit, 0: poll) and reports the state;
+ * returns the request's failure status once it has failed. */
+int32_t pars_gpu_service_wait        (pars_gpu_service* service, int64_t ticket, int32_t timeout_ms, int32_t* state);
+int32_t pars_gpu_service_result_info (pars_gpu_service* service, int64_t ticket, pars_gpu_request_info* info);
+/* Streamline results, per batch: counts, then HOST copies (any pointer may be NULL). */
+int32_t pars_gpu_service_result_batch(pars_gpu_service* service, int64_t ticket, int64_t batch, int64_t* vertices,
+                                      int64_t* indices, float* vertex_data, float* color_data, int32_t* index_data);
+/* FTLE results: ftle_shape[0]*ftle_shape[1]*ftle_shape[2] floats to HOST `values`. */
+int32_t pars_gpu_service_result_ftle (pars_gpu_service* service, int64_t ticket, float* values);
+/* Forgets a request (cancels it if it is still queued). */
+int32_t pars_gpu_service_release     (pars_gpu_service* service, int64_t ticket);
+
 /* ---- allocation-free FTLE --------------------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device
  * memory: plugins running inside a host application that owns the GPU's

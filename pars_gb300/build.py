@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBRARY = os.path.join(HERE, "libpars_gpu.so")
 
-SOURCES = ["pars_gpu.cu", "trace_kernels.cu", "curve_kernels.cu", "ftle_kernels.cu", "field_kernels.cu", "batch_kernels.cu"]
+SOURCES = ["pars_gpu.cu", "trace_kernels.cu", "curve_kernels.cu", "ftle_kernels.cu", "field_kernels.cu", "batch_kernels.cu",
+           "service.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]

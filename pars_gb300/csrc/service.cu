@@ -16,7 +16,10 @@
 // Datasets (the requests' dataset_filepath) are fields registered with the
 // service and kept resident across requests.
 #include <algorithm>
+#include <array>
 #include <chrono>
+#include <cstdio>
+#include <cstring>
 #include <condition_variable>
 #include <deque>
 #include <map>
@@ -187,14 +190,12 @@ void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std:
     field_view fv {};
     fv.data = flows[k].as<const float4>();
     fv.nx = r.ftle_shape[0]; fv.ny = r.ftle_shape[1]; fv.nz = r.ftle_shape[2];
-    const float scale = jobs[k].sx > 0.0f ? svc.datasets[r.dataset].spacing[0] / jobs[k].sx : 1.0f;
-    (void)scale;
     fv.hx = jobs[k].sx; fv.hy = jobs[k].sy; fv.hz = jobs[k].sz;
     const long long voxels = (long long)fv.nx * fv.ny * fv.nz;
     values.reserve(sizeof(float) * voxels);
-    // time = step * iterations, as pipeline.cpp:403 sets it
-    const double time = double(r.s.particle_tracing_step_size) * double(r.s.seed_generation_iterations);
-    launch_ftle(c, fv, time == 0.0 ? 1.0 : time, r.ftle_mode, values.as<float>());
+    // time = step * iterations in FP32, as pipeline.cpp:403 sets it
+    const float time = r.s.particle_tracing_step_size * float(r.s.seed_generation_iterations);
+    launch_ftle(c, fv, time == 0.0f ? 1.0 : double(time), r.ftle_mode, values.as<float>());
     r.ftle_values.resize(voxels);
     PARS_CUDA(cudaMemcpyAsync(r.ftle_values.data(), values.get(), sizeof(float) * voxels, cudaMemcpyDeviceToHost, c.stream));
   }
@@ -207,6 +208,7 @@ void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std:
 void run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std::shared_ptr<request>>& batch, int stage_mode)
 {
   std::vector<trace_block> blocks;
+  std::vector<step_rule> rules;
   std::vector<long long> block_count;
   std::vector<int> block_max;
   long long total = 0;
@@ -229,8 +231,8 @@ void run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vecto
     trace_block b;
     b.field = d.view;
     for (int f = 0; f < 6; ++f) b.neighbor[f] = -1;
-    b.rule = make_step_rule(r.integrator, stage_mode, r.s.particle_tracing_step_size);
     blocks.push_back(b);
+    rules.push_back(make_step_rule(r.integrator, stage_mode, r.s.particle_tracing_step_size));
     block_count.push_back(n);
     block_max.push_back(n > 0 ? r.s.seed_generation_iterations : 0);
     total += n;
@@ -256,12 +258,14 @@ void run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vecto
   }
   if (total > 0)
     PARS_CUDA(cudaMemcpyAsync(c.block_of.get(), block_of.data(), sizeof(int) * total, cudaMemcpyHostToDevice, c.stream));
-  device_buffer device_blocks;
+  device_buffer device_blocks, device_rules;
   device_blocks.reserve(sizeof(trace_block) * blocks.size());
+  device_rules.reserve(sizeof(step_rule) * rules.size());
   PARS_CUDA(cudaMemcpyAsync(device_blocks.get(), blocks.data(), sizeof(trace_block) * blocks.size(), cudaMemcpyHostToDevice, c.stream));
-  // one block alone runs without the block table (block_of = nullptr)
+  PARS_CUDA(cudaMemcpyAsync(device_rules.get(), rules.data(), sizeof(step_rule) * rules.size(), cudaMemcpyHostToDevice, c.stream));
   pars_gpu_trace_summary summary {};
-  trace_rounds(c, blocks, device_blocks.as<const trace_block>(), total, block_count, block_max, blocks[0].rule, false, &summary);
+  trace_rounds(c, blocks, device_blocks.as<const trace_block>(), total, block_count, block_max, rules[0], false, &summary,
+               device_rules.as<const step_rule>());
 
   auto& curves = c.curves;
   curves.indices.reserve(sizeof(int) * (std::size_t)std::max<long long>(curves.vertex_total, 1));
@@ -296,8 +300,14 @@ void run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vecto
                                 cudaMemcpyDeviceToHost, c.stream));
   }
   PARS_CUDA(cudaStreamSynchronize(c.stream));
-  // steps per request: vertices minus seed and termination vertex per curve
-  for (std::size_t k = 0; k < batch.size(); ++k) batch[k]->steps = 0;
+  // Steps per request: each curve holds its seed, one vertex per step and the
+  // termination vertex (remaining_iterations >= 2; one block, one round).
+  for (std::size_t k = 0; k < batch.size(); ++k)
+  {
+    long long vertices = 0;
+    for (auto& v : batch[k]->vertices) vertices += (long long)v.size();
+    batch[k]->steps = batch[k]->s.seed_generation_iterations >= 2 ? std::max(0LL, vertices - 2 * block_count[k]) : 0;
+  }
   (void)summary;
 }
 

@@ -55,6 +55,22 @@ class BatchJob(ctypes.Structure):
                 ("end_positions", ctypes.c_void_p), ("end_steps", ctypes.c_void_p), ("steps", ctypes.c_int64)]
 
 
+class SettingsSummary(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_char * 64), ("dataset_filepath", ctypes.c_char * 256),
+                ("particle_tracing_integrator", ctypes.c_char * 64), ("color_generation_mode", ctypes.c_char * 64),
+                ("seed_generation_stride", ctypes.c_int32 * 3), ("seed_generation_iterations", ctypes.c_int32),
+                ("particle_tracing_step_size", ctypes.c_float), ("particle_tracing_load_balance", ctypes.c_int32),
+                ("color_generation_free_parameter", ctypes.c_float), ("raytracing_camera_position", ctypes.c_float * 3),
+                ("raytracing_image_size", ctypes.c_int32 * 2), ("raytracing_streamline_radius", ctypes.c_float),
+                ("raytracing_iterations", ctypes.c_int32)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int32), ("status", ctypes.c_int32), ("kind", ctypes.c_int32),
+                ("ftle_shape", ctypes.c_int32 * 3), ("batches", ctypes.c_int64), ("steps", ctypes.c_int64),
+                ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+
+
 class ParsGpuError(RuntimeError):
     def __init__(self, status, message):
         super().__init__(f"{STATUS.get(status, status)} ({status}): {message}")
@@ -104,6 +120,16 @@ SIGNATURES = {
     "pars_gpu_batch_advect": [_P, _P, _I32, _I32],
     "pars_gpu_batch_variants": [_P, ctypes.POINTER(_I32)],
     "pars_gpu_batch_tuned": [_P, _I32, ctypes.POINTER(_I32), ctypes.POINTER(_I32)],
+    "pars_gpu_settings_decode": [_P, _I64, ctypes.POINTER(SettingsSummary)],
+    "pars_gpu_service_create": [ctypes.POINTER(_P), _I32, _I64, _I32, _I32],
+    "pars_gpu_service_destroy": [_P],
+    "pars_gpu_service_add_dataset": [_P, ctypes.c_char_p, _P, _P, _P, _P, _P],
+    "pars_gpu_service_submit": [_P, _P, _I64, ctypes.POINTER(_I64)],
+    "pars_gpu_service_wait": [_P, _I64, _I32, ctypes.POINTER(_I32)],
+    "pars_gpu_service_result_info": [_P, _I64, ctypes.POINTER(RequestInfo)],
+    "pars_gpu_service_result_batch": [_P, _I64, _I64, ctypes.POINTER(_I64), ctypes.POINTER(_I64), _P, _P, _P],
+    "pars_gpu_service_result_ftle": [_P, _I64, _P],
+    "pars_gpu_service_release": [_P, _I64],
     "pars_gpu_profile_enable": [_P, _I32],
     "pars_gpu_profile_reset": [_P],
     "pars_gpu_profile_get": [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)],
@@ -384,3 +410,87 @@ class Context:
         n = _I64()
         self._call("pars_gpu_launch_count", ctypes.byref(n))
         return n.value
+
+
+def decode_settings(message):
+    """pars_gpu_settings_decode: the scalar fields of a `settings` message."""
+    data = np.frombuffer(bytes(message), np.uint8)
+    out = SettingsSummary()
+    status = library().pars_gpu_settings_decode(data.ctypes.data if len(data) else None, len(data), ctypes.byref(out))
+    if status:
+        raise ParsGpuError(status, "pars_gpu_settings_decode")
+    return out
+
+
+class Service:
+    """The request service (pars_gpu_service_*): submit `settings` messages,
+    wait, collect results."""
+
+    def __init__(self, device=0, budget_bytes=64 << 30, lanes=2, max_batch=64):
+        self.lib = library()
+        handle = _P()
+        status = self.lib.pars_gpu_service_create(ctypes.byref(handle), device, budget_bytes, lanes, max_batch)
+        if status:
+            raise ParsGpuError(status, "pars_gpu_service_create")
+        self.handle = handle
+
+    def _check(self, status, what):
+        if status:
+            raise ParsGpuError(status, what)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.pars_gpu_service_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_dataset(self, name, field):
+        self._check(self.lib.pars_gpu_service_add_dataset(self.handle, name.encode(), _ptr(field.xyz), _ptr(field.dims),
+                                                          _ptr(field.offset), _ptr(field.size), _ptr(field.spacing)),
+                    "pars_gpu_service_add_dataset")
+
+    def submit(self, message):
+        data = np.frombuffer(bytes(message), np.uint8)
+        t = _I64()
+        self._check(self.lib.pars_gpu_service_submit(self.handle, data.ctypes.data, len(data), ctypes.byref(t)),
+                    "pars_gpu_service_submit")
+        return t.value
+
+    def wait(self, ticket, timeout_ms=-1):
+        s = _I32()
+        self._check(self.lib.pars_gpu_service_wait(self.handle, ticket, timeout_ms, ctypes.byref(s)), "pars_gpu_service_wait")
+        return s.value
+
+    def info(self, ticket):
+        i = RequestInfo()
+        self._check(self.lib.pars_gpu_service_result_info(self.handle, ticket, ctypes.byref(i)), "pars_gpu_service_result_info")
+        return i
+
+    def streamlines(self, ticket):
+        """List of (vertices, colors, indices) per batch."""
+        out = []
+        for b in range(self.info(ticket).batches):
+            nv, ni = _I64(), _I64()
+            self._check(self.lib.pars_gpu_service_result_batch(self.handle, ticket, b, ctypes.byref(nv), ctypes.byref(ni),
+                                                               None, None, None), "pars_gpu_service_result_batch")
+            v = np.zeros((nv.value, 4), np.float32)
+            c = np.zeros((nv.value, 4), np.float32)
+            i = np.zeros(ni.value, np.int32)
+            self._check(self.lib.pars_gpu_service_result_batch(self.handle, ticket, b, ctypes.byref(nv), ctypes.byref(ni),
+                                                               _ptr(v), _ptr(c), _ptr(i)), "pars_gpu_service_result_batch")
+            out.append((v, c, i))
+        return out
+
+    def ftle(self, ticket):
+        shape = tuple(self.info(ticket).ftle_shape)
+        out = np.zeros(shape, np.float32)
+        self._check(self.lib.pars_gpu_service_result_ftle(self.handle, ticket, _ptr(out)), "pars_gpu_service_result_ftle")
+        return out
+
+    def release(self, ticket):
+        self._check(self.lib.pars_gpu_service_release(self.handle, ticket), "pars_gpu_service_release")

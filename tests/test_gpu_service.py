@@ -1,0 +1,133 @@
+"""The request service (pars_gpu_service_*): reference `settings` messages in,
+curve buffers / FTLE fields out, with admission, batching and two lanes.
+
+Bars:
+* every result is the same alone and in the mix: a batch of mixed requests
+  submitted together gives, request by request, exactly (bit for bit) what the
+  same request gives when it is alone in the service;
+* a streamline request with mode "streamlines_reference" (the reference's
+  frozen-velocity scheme) returns the reference's buffers: bit-exact vertices,
+  indices and rgb colours against the oracle;
+* an FTLE request equals the context path (flow map + FTLE) on the same
+  dataset, bit for bit.
+"""
+import numpy as np
+import pytest
+
+from conftest import assert_colors_equal
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests():
+    base = {"particle_tracing_integrator": "runge_kutta_4", "color_generation_free_parameter": 0.75}
+    reqs = []
+    for k, (stride, iters, color, step) in enumerate([(3, 302, "rgb", 0.01), (2, 152, "hsv_constant_s", 0.02),
+                                                      (4, 502, "hsl_constant_l", 0.01), (5, 82, "rgb", 0.05),
+                                                      (2, 202, "hsv_constant_v", 0.01), (6, 1002, "rgb", 0.01)]):
+        reqs.append(dict(base, mode="streamlines", dataset_filepath="abc40" if k % 2 == 0 else "abc28",
+                         seed_generation_stride=[stride] * 3, seed_generation_iterations=iters,
+                         color_generation_mode=color, particle_tracing_step_size=step))
+    for k, (stride, iters) in enumerate([(1, 101), (2, 201), (1, 61), (3, 301)]):
+        reqs.append(dict(base, mode="ftle", dataset_filepath="abc40" if k % 2 else "abc28",
+                         seed_generation_stride=[stride] * 3, seed_generation_iterations=iters,
+                         particle_tracing_step_size=0.01))
+    return reqs
+
+
+def _result(svc, ticket, kind):
+    return svc.streamlines(ticket) if kind == "streamlines" else svc.ftle(ticket)
+
+
+def _same(a, b, kind):
+    if kind == "ftle":
+        return np.array_equal(a, b, equal_nan=True)
+    return len(a) == len(b) and all(np.array_equal(x[0], y[0]) and np.array_equal(x[1], y[1], equal_nan=True)
+                                    and np.array_equal(x[2], y[2]) for x, y in zip(a, b))
+
+
+@pytest.fixture(scope="module")
+def service():
+    from pars_gb300 import native, workloads as W
+    svc = native.Service(0, budget_bytes=24 << 30, lanes=2, max_batch=16)
+    svc.add_dataset("abc40", W.abc_field(40, noise_sigma=0.01, seed=4))
+    svc.add_dataset("abc28", W.abc_field(28))
+    yield svc
+    svc.close()
+
+
+def test_results_are_the_same_alone_and_in_the_mix(service):
+    from pars_gb300.requests import encode_settings
+    reqs = _requests()
+    tickets = [service.submit(encode_settings(r)) for r in reqs]
+    for t in tickets:
+        assert service.wait(t) == 2
+    mixed = [_result(service, t, "ftle" if "ftle" in r["mode"] else "streamlines") for t, r in zip(tickets, reqs)]
+    infos = [service.info(t) for t in tickets]
+    assert all(i.status == 0 for i in infos)
+    assert all(i.latency_ms >= i.run_ms >= 0 for i in infos)
+    for t in tickets:
+        service.release(t)
+    for r, m in zip(reqs, mixed):
+        kind = "ftle" if "ftle" in r["mode"] else "streamlines"
+        t = service.submit(encode_settings(r))
+        assert service.wait(t) == 2
+        alone = _result(service, t, kind)
+        service.release(t)
+        assert _same(alone, m, kind), r
+
+
+def test_reference_mode_streamlines_match_the_oracle(service, port):
+    from pars_gb300 import workloads as W
+    from pars_gb300.requests import encode_settings
+    f = W.abc_field(28)
+    req = {"mode": "streamlines_reference", "dataset_filepath": "abc28", "seed_generation_stride": [3, 3, 3],
+           "seed_generation_iterations": 202, "particle_tracing_integrator": "runge_kutta_4",
+           "particle_tracing_step_size": 0.01, "color_generation_mode": "rgb"}
+    t = service.submit(encode_settings(req))
+    assert service.wait(t) == 2
+    got = service.streamlines(t)
+    service.release(t)
+    seeds = port.seed_generate(f.offset, f.size, (f.spacing * np.float32(3)).astype(np.float32), 202)
+    expected = port.trace_single(f, seeds, 2, 0.01, "rgb", 0.5)
+    assert len(got) == len(expected.batches)
+    for (v, c, i), e in zip(got, expected.batches):
+        assert np.array_equal(v, e["vertices"])
+        assert np.array_equal(i, e["indices"])
+        assert_colors_equal(c, e["colors"])
+
+
+def test_ftle_request_equals_the_context_path(service, ctx):
+    from pars_gb300 import native, workloads as W
+    from pars_gb300.requests import encode_settings
+    f = W.abc_field(40, noise_sigma=0.01, seed=4)
+    req = {"mode": "ftle", "dataset_filepath": "abc40", "seed_generation_stride": [1, 1, 1],
+           "seed_generation_iterations": 151, "particle_tracing_integrator": "runge_kutta_4",
+           "particle_tracing_step_size": 0.01}
+    t = service.submit(encode_settings(req))
+    assert service.wait(t) == 2
+    got = service.ftle(t)
+    steps = service.info(t).steps
+    service.release(t)
+    h = ctx.upload_field(f)
+    fm, s = ctx.flow_map_generate(h, 151, 1.0, native.RUNGE_KUTTA_4, native.STAGES_RESAMPLED, 0.01)
+    expected = ctx.ftle_generate(fm, np.float32(0.01) * 151, 0, shape=tuple(f.dims))
+    assert steps == s
+    assert np.array_equal(got, expected)
+    ctx.release_field(fm)
+    ctx.release_field(h)
+
+
+def test_unknown_dataset_and_oversized_requests_are_rejected(service):
+    from pars_gb300 import native
+    from pars_gb300.requests import encode_settings
+    with pytest.raises(native.ParsGpuError) as e:
+        service.submit(encode_settings({"mode": "ftle", "dataset_filepath": "missing", "seed_generation_stride": [1, 1, 1],
+                                        "seed_generation_iterations": 11, "particle_tracing_integrator": "runge_kutta_4",
+                                        "particle_tracing_step_size": 0.01}))
+    assert e.value.status == -5
+    with pytest.raises(native.ParsGpuError) as e:
+        service.submit(encode_settings({"mode": "streamlines", "dataset_filepath": "abc40", "seed_generation_stride": [1, 1, 1],
+                                        "seed_generation_iterations": 2_000_000, "particle_tracing_integrator": "runge_kutta_4",
+                                        "particle_tracing_step_size": 0.01}))
+    assert e.value.status == -6
