@@ -46,7 +46,8 @@ def parse_args():
     p.add_argument("--size", type=int, default=256)
     p.add_argument("--iterations", type=int, default=501)
     p.add_argument("--cpu-sample", type=int, default=1048576, help="seeds in the CPU baseline's bounded sample")
-    p.add_argument("--workload", choices=["ftle", "streamlines", "domain", "pathlines"], default="ftle",
+    p.add_argument("--requests", type=int, default=300, help="served workload: number of requests")
+    p.add_argument("--workload", choices=["ftle", "streamlines", "domain", "pathlines", "serve"], default="ftle",
                    help="ftle: the headline line; the others print one line for the other workloads")
     return p.parse_args()
 
@@ -275,10 +276,96 @@ def run_pathlines(args):
     ctx.close()
 
 
+def run_serve(args):
+    """The served mixed stream: requests (reference `settings` messages) into
+    the service, Poisson arrivals; throughput and p50/p99 latency of the
+    batched service (2 lanes, batches up to 64) against the plain path (one
+    request at a time, no batching), at saturation and at offered loads below
+    each path's saturation throughput."""
+    import threading as th
+    import torch
+    from pars_gb300 import native, workloads
+    from pars_gb300.requests import encode_settings
+    ds, reqs = workloads.served_stream_config(seed=4, requests=args.requests)
+    messages = []
+    for r in reqs:
+        d = ds[r["dataset"]]
+        step = 0.01 if d["kind"] == "abc" else 0.05
+        messages.append(encode_settings({
+            "mode": r["kind"], "dataset_filepath": d["name"], "seed_generation_stride": [r["stride"]] * 3,
+            "seed_generation_iterations": r["steps"] + (2 if r["kind"] == "streamlines" else 1),
+            "particle_tracing_integrator": "runge_kutta_4", "particle_tracing_step_size": step,
+            "color_generation_mode": "hsv_constant_s", "color_generation_free_parameter": 0.75}))
+
+    def make(lanes, max_batch):
+        svc = native.Service(0, budget_bytes=160 << 30, lanes=lanes, max_batch=max_batch)
+        for d in ds:
+            gen = workloads.abc_device if d["kind"] == "abc" else workloads.gyre_snapshot_device
+            xyz, offset, size, spacing = gen(torch, d["edge"])
+            svc.add_dataset_device(d["name"], xyz.data_ptr(), (d["edge"],) * 3, offset, size, spacing)
+            del xyz
+            torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        return svc
+
+    def run(svc, rate):
+        """Submits every request at its Poisson arrival time (rate None: all at
+        once); returns (makespan s, latencies ms, particle-steps)."""
+        tickets = [None] * len(messages)
+        t0 = time.perf_counter()
+
+        def submitter():
+            at = 0.0
+            for k, m in enumerate(messages):
+                if rate:
+                    at += reqs[k]["gap"] / rate
+                    delay = t0 + at - time.perf_counter()
+                    if delay > 0:
+                        time.sleep(delay)
+                tickets[k] = svc.submit(m)
+
+        thread = th.Thread(target=submitter)
+        thread.start()
+        lat, steps = [], 0
+        for k in range(len(messages)):
+            while tickets[k] is None:
+                time.sleep(0.0002)
+            svc.wait(tickets[k])
+            info = svc.info(tickets[k])
+            lat.append(info.latency_ms)
+            steps += info.steps
+            svc.release(tickets[k])
+        thread.join()
+        return time.perf_counter() - t0, np.array(lat), steps
+
+    results = {}
+    for name, lanes, batch in (("plain", 1, 1), ("batched", 2, 64)):
+        svc = make(lanes, batch)
+        for m in messages[:8]:                       # warm-up (autotuning, allocations)
+            svc.wait(svc.submit(m))
+        span, lat, steps = run(svc, None)
+        saturation = len(messages) / span
+        out = {"saturation_requests_per_s": saturation, "saturation_particle_steps_per_s": steps / span,
+               "saturation_p50_ms": float(np.percentile(lat, 50)), "saturation_p99_ms": float(np.percentile(lat, 99))}
+        for load in (0.5, 0.9):
+            span, lat, _ = run(svc, load * saturation)
+            out[f"load{int(load * 100)}"] = {"offered_requests_per_s": load * saturation,
+                                             "achieved_requests_per_s": len(messages) / span,
+                                             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
+        results[name] = out
+        svc.close()
+    print(json.dumps({"workload": f"served_{len(messages)}: {len(messages)} requests (seed 4), 70% streamlines / 30% FTLE on "
+                                  f"{len(ds)} resident ABC / double-gyre fields (edge 64-512), seeds 1k-2M, 200-2000 RK4 steps, "
+                                  "Poisson arrivals",
+                      "datasets": ds, "plain": results["plain"], "batched": results["batched"],
+                      "throughput_ratio_at_saturation": results["batched"]["saturation_requests_per_s"] /
+                                                        results["plain"]["saturation_requests_per_s"]}))
+
+
 def main():
     args = parse_args()
     if args.workload != "ftle":
-        {"streamlines": run_streamlines, "domain": run_domain, "pathlines": run_pathlines}[args.workload](args)
+        {"streamlines": run_streamlines, "domain": run_domain, "pathlines": run_pathlines, "serve": run_serve}[args.workload](args)
         return
     rank, world, local = dist_env()
     from pars_gb300 import workloads

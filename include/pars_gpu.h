@@ -339,6 +339,10 @@ int32_t pars_gpu_service_destroy     (pars_gpu_service* service);
 /* Registers a dataset (HOST xyz [X][Y][Z][3], as pars_gpu_field_upload) under `name`. */
 int32_t pars_gpu_service_add_dataset (pars_gpu_service* service, const char* name, const float* xyz, const int32_t shape[3],
                                       const float offset[3], const float size[3], const float spacing[3]);
+/* Same, from DEVICE xyz. */
+int32_t pars_gpu_service_add_dataset_device(pars_gpu_service* service, const char* name, const float* device_xyz,
+                                            const int32_t shape[3], const float offset[3], const float size[3],
+                                            const float spacing[3]);
 int32_t pars_gpu_service_submit      (pars_gpu_service* service, const uint8_t* message, int64_t length, int64_t* ticket);
 /* Waits up to timeout_ms (negative: no limit, 0: poll) and reports the state;
  * returns the request's failure status once it has failed. */

@@ -479,6 +479,27 @@ int32_t pars_gpu_service_add_dataset(pars_gpu_service* svc, const char* name, co
   });
 }
 
+int32_t pars_gpu_service_add_dataset_device(pars_gpu_service* svc, const char* name, const float* device_xyz, const int32_t shape[3],
+                                            const float offset[3], const float size[3], const float spacing[3])
+{
+  return service_guard(svc, [&] {
+    PARS_REQUIRE(name && device_xyz, "name and device_xyz are required");
+    int32_t handle = -1;
+    const int32_t status = pars_gpu_field_upload_device(svc->owner, device_xyz, shape, offset, size, spacing, &handle);
+    if (status != PARS_OK) throw error(status, pars_gpu_last_error(svc->owner));
+    pars_gpu_synchronize(svc->owner);
+    dataset d;
+    d.name = name;
+    d.field = handle;
+    auto& f = *svc->owner->fields.at(handle);
+    d.view = f.view();
+    for (int i = 0; i < 3; ++i) { d.shape[i] = f.shape[i]; d.offset[i] = f.offset[i]; d.size[i] = f.size[i]; d.spacing[i] = f.spacing[i]; }
+    std::lock_guard<std::mutex> lock(svc->mutex);
+    svc->dataset_index[d.name] = int(svc->datasets.size());
+    svc->datasets.push_back(d);
+  });
+}
+
 int32_t pars_gpu_service_submit(pars_gpu_service* svc, const uint8_t* message, int64_t length, int64_t* ticket)
 {
   return service_guard(svc, [&] {

@@ -124,6 +124,7 @@ SIGNATURES = {
     "pars_gpu_service_create": [ctypes.POINTER(_P), _I32, _I64, _I32, _I32],
     "pars_gpu_service_destroy": [_P],
     "pars_gpu_service_add_dataset": [_P, ctypes.c_char_p, _P, _P, _P, _P, _P],
+    "pars_gpu_service_add_dataset_device": [_P, ctypes.c_char_p, _P, _P, _P, _P, _P],
     "pars_gpu_service_submit": [_P, _P, _I64, ctypes.POINTER(_I64)],
     "pars_gpu_service_wait": [_P, _I64, _I32, ctypes.POINTER(_I32)],
     "pars_gpu_service_result_info": [_P, _I64, ctypes.POINTER(RequestInfo)],
@@ -453,6 +454,11 @@ class Service:
         self._check(self.lib.pars_gpu_service_add_dataset(self.handle, name.encode(), _ptr(field.xyz), _ptr(field.dims),
                                                           _ptr(field.offset), _ptr(field.size), _ptr(field.spacing)),
                     "pars_gpu_service_add_dataset")
+
+    def add_dataset_device(self, name, device_ptr, dims, offset, size, spacing):
+        d, o, s, sp = _i3(dims), _f3(offset), _f3(size), _f3(spacing)
+        self._check(self.lib.pars_gpu_service_add_dataset_device(self.handle, name.encode(), device_ptr, _ptr(d), _ptr(o),
+                                                                 _ptr(s), _ptr(sp)), "pars_gpu_service_add_dataset_device")
 
     def submit(self, message):
         data = np.frombuffer(bytes(message), np.uint8)

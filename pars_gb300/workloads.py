@@ -209,6 +209,65 @@ def gaussian_mixture_seeds(count, n, spacing, partition, remaining, seed=2, cent
     return particles, offsets
 
 
+def abc_device(torch, n):
+    """abc_field(n) computed on the GPU; returns (xyz device tensor, offset, size, spacing)."""
+    h = 2.0 * np.pi / (n - 1)
+    c = torch.arange(n, dtype=torch.float64, device="cuda") * h
+    Y, Z = torch.meshgrid(c, c, indexing="ij")
+    out = torch.empty((n, n, n, 3), dtype=torch.float32, device="cuda")
+    for i in range(n):
+        x = float(c[i])
+        out[i, :, :, 0] = (ABC_A * torch.sin(Z) + ABC_C * torch.cos(Y)).float()
+        out[i, :, :, 1] = (ABC_B * np.sin(x) + ABC_A * torch.cos(Z)).float()
+        out[i, :, :, 2] = (ABC_C * torch.sin(Y) + ABC_B * np.cos(x)).float()
+    spacing = np.full(3, np.float32(h), np.float32)
+    return out, np.zeros(3, np.float32), (spacing * np.float32(n)).astype(np.float32), spacing
+
+
+def gyre_snapshot_device(torch, n, t=2.5):
+    """One time slice (time t) of the double gyre on n^3 vertices of
+    [0,2] x [0,1] x [0,1], as a steady field."""
+    xyz, offset, spacing, t0, dt = double_gyre_device(torch, n, 2, period=10.0)
+    # double_gyre_device gives slices at t = 0 and t = period; rebuild at t
+    omega = 2.0 * np.pi / 10.0
+    x = torch.linspace(0.0, 2.0, n, dtype=torch.float64, device="cuda")
+    y = torch.linspace(0.0, 1.0, n, dtype=torch.float64, device="cuda")
+    X, Y = torch.meshgrid(x, y, indexing="ij")
+    a = 0.25 * np.sin(omega * t)
+    b = 1.0 - 2.0 * a
+    f = a * X * X + b * X
+    out = xyz[0]
+    out[:, :, :, 0] = (-np.pi * 0.1 * torch.sin(np.pi * f) * torch.cos(np.pi * Y)).float()[:, :, None]
+    out[:, :, :, 1] = (np.pi * 0.1 * torch.cos(np.pi * f) * torch.sin(np.pi * Y) * (2.0 * a * X + b)).float()[:, :, None]
+    out = out.contiguous()
+    return out, offset, (spacing * np.float32(n)).astype(np.float32), spacing
+
+
+def served_stream_config(seed=4, requests=1000, datasets=8, streamline_seed_cap=65536):
+    """The served mixed stream: `datasets` resident fields (ABC or a
+    double-gyre snapshot, edge log-uniform in [64, 512]) and `requests`
+    requests, 70 % streamline / 30 % FTLE, seed counts log-uniform in
+    [1k, 2M] (streamline requests capped at streamline_seed_cap, since every
+    step of every curve is returned to the host), step counts uniform in
+    [200, 2000], Poisson arrivals (unit-rate exponential gaps, scaled by the
+    offered rate).  The seed count is met with the smallest lattice stride
+    that does not exceed it.  PCG64 from `seed`."""
+    rng = np.random.default_rng(seed)
+    ds = [{"name": f"field{k}", "kind": "abc" if rng.random() < 0.5 else "gyre",
+           "edge": int(np.exp(rng.uniform(np.log(64), np.log(512))))} for k in range(datasets)]
+    reqs = []
+    for _ in range(requests):
+        kind = "streamlines" if rng.random() < 0.7 else "ftle"
+        d = int(rng.integers(0, datasets))
+        seeds = float(np.exp(rng.uniform(np.log(1000), np.log(2_000_000))))
+        if kind == "streamlines":
+            seeds = min(seeds, streamline_seed_cap)
+        steps = int(rng.integers(200, 2001))
+        stride = max(1, int(np.ceil(ds[d]["edge"] / seeds ** (1.0 / 3.0))))
+        reqs.append({"kind": kind, "dataset": d, "stride": stride, "steps": steps, "gap": float(rng.exponential())})
+    return ds, reqs
+
+
 def streamline_config():
     """The plain streamline workload: 64^3 ABC, seeds on a stride-4 lattice
     (16^3), RK4 h = 0.01, 1000 steps (remaining_iterations = 1002: seed, at most
