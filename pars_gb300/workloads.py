@@ -243,7 +243,7 @@ def gyre_snapshot_device(torch, n, t=2.5):
     return out, offset, (spacing * np.float32(n)).astype(np.float32), spacing
 
 
-def served_stream_config(seed=4, requests=1000, datasets=8, streamline_seed_cap=65536):
+def served_stream_config(seed=4, requests=1000, datasets=8, streamline_seed_cap=16384):
     """The served mixed stream: `datasets` resident fields (ABC or a
     double-gyre snapshot, edge log-uniform in [64, 512]) and `requests`
     requests, 70 % streamline / 30 % FTLE, seed counts log-uniform in
