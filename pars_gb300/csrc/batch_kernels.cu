@@ -82,8 +82,9 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
   bool alive = false;
   long long seed = 0;
   int steps = 0;
-  float4 pos = make_float4(0.f, 0.f, 0.f, 0.f);
-  float3 lo = make_float3(0.f, 0.f, 0.f);
+  float4 pos = make_float4(0.f, 0.f, 0.f, 0.f);   // unsteady: absolute position
+  float3 lo = make_float3(0.f, 0.f, 0.f);         // unsteady: its compensation term
+  local_position local {0, 0, 0, 0.f, 0.f, 0.f};  // steady: cell + offset
   lane_cache<UNSTEADY> cache;
   // current job's parameters (warp-uniform)
   field_view f {};
@@ -115,6 +116,7 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
                               __fadd_rn(J.oz, __fmul_rn(J.sz, float(iz))), 0.0f);
           }
           lo = make_float3(0.f, 0.f, 0.f);
+          if constexpr (!UNSTEADY) local = to_local(f, pos);
           steps = 0;
           alive = true;
         }
@@ -160,33 +162,38 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
     if (alive)
     {
       bool retire = steps >= max_steps;
-      axis_cell cx, cy, cz;
-      if (!retire)
+      if constexpr (UNSTEADY)
       {
-        const bool in_x = start_cell(pos.x, f.ox, f.hx, f.inv_hx, f.nx, cx);
-        const bool in_y = start_cell(pos.y, f.oy, f.hy, f.inv_hy, f.ny, cy);
-        const bool in_z = start_cell(pos.z, f.oz, f.hz, f.inv_hz, f.nz, cz);
-        retire = !(in_x && in_y && in_z);
-      }
-      if (!retire)
-      {
-        step_rule r;
-        r.frozen = 0; r.rk4 = rk4; r.h = h; r.count = 0;
-        if constexpr (UNSTEADY)
+        axis_cell cx, cy, cz;
+        if (!retire)
         {
+          const bool in_x = start_cell(pos.x, f.ox, f.hx, f.inv_hx, f.nx, cx);
+          const bool in_y = start_cell(pos.y, f.oy, f.hy, f.inv_hy, f.ny, cy);
+          const bool in_z = start_cell(pos.z, f.oz, f.hz, f.inv_hz, f.nz, cz);
+          retire = !(in_x && in_y && in_z);
+        }
+        if (!retire)
+        {
+          step_rule r;
+          r.frozen = 0; r.rk4 = rk4; r.h = h; r.count = 0;
           // FP64 time of this step: start + n h (no accumulated rounding)
           const double t = time_begin + double(steps) * double(h);
           const float3 k1 = sample_unsteady_cached(f, ta, cache.k, pos.x, pos.y, pos.z, t);
           if (is_zero(k1)) retire = true;
-          else unsteady_step(f, ta, cache.k, r, pos, lo, k1, t);
+          else { unsteady_step(f, ta, cache.k, r, pos, lo, k1, t); ++steps; ++job_steps; }
         }
-        else
+      }
+      else
+      {
+        // the step-start test: the particle's cell inside the grid
+        if (!retire) retire = !local_inside(f, local);
+        if (!retire)
         {
-          const float3 k1 = sample_cell(f, cache.k, cx, cy, cz);
-          if (is_zero(k1)) retire = true;
-          else resampled_step_cached(f, cache.k, r, pos, lo, k1);
+          const float3 k1 = sample_local(f, cache.k, local.ix, local.iy, local.iz, local.ux, local.uy, local.uz);
+          if (is_zero_local(f, k1)) retire = true;
+          else { local_step(f, cache.k, rk4, h, local, k1); ++steps; ++job_steps; }
         }
-        if (!retire) { ++steps; ++job_steps; }
+        if (retire) pos = to_absolute(f, local, 0.0f);
       }
       if (retire)
       {

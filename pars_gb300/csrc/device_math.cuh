@@ -448,6 +448,111 @@ __device__ __forceinline__ void unsteady_step(const field_view& f, const time_ax
   compensated_add(x.z, lo.z, h6 * (k1.z + 2.0f * (k2.z + k3.z) + k4.z));
 }
 
+// ---- Local cell coordinates (batched engine) -----------------------------------
+// A particle is carried as its cell (ix, iy, iz) and its offset u in [0, 1)^3
+// within that cell, in units of the cell; position = offset + (i + u) * h.
+// The cached cell polynomial is scaled by 1/h per component, so it returns the
+// velocity in cells per unit time and a stage point is u + c * h * k.  A
+// sample inside the current cell needs no floor, division or conversion; the
+// offset keeps 24 bits of precision within its cell however far the cell is
+// from the origin.
+struct local_position
+{
+  int   ix, iy, iz;
+  float ux, uy, uz;
+};
+
+__device__ __forceinline__ void scale3(float3& v, float sx, float sy, float sz) { v.x *= sx; v.y *= sy; v.z *= sz; }
+__device__ __forceinline__ void scale_cache(cell_cache& k, float sx, float sy, float sz)
+{
+  scale3(k.a, sx, sy, sz); scale3(k.b, sx, sy, sz); scale3(k.c, sx, sy, sz); scale3(k.d, sx, sy, sz);
+  scale3(k.e, sx, sy, sz); scale3(k.f, sx, sy, sz); scale3(k.g, sx, sy, sz); scale3(k.h, sx, sy, sz);
+}
+
+// Velocity (cells per unit time) at cell (cx, cy, cz) + (ux, uy, uz); the
+// offset may lie outside [0, 1) (a stage point that left the cell) and the
+// cell outside the grid (clamped, weight 0 or 1).
+__device__ __forceinline__ float3 sample_local(const field_view& f, cell_cache& k, int cx, int cy, int cz, float ux, float uy, float uz)
+{
+  int ix = cx, iy = cy, iz = cz;
+  float wx = ux, wy = uy, wz = uz;
+  if (!(ux >= 0.0f && ux < 1.0f && uy >= 0.0f && uy < 1.0f && uz >= 0.0f && uz < 1.0f))
+  {
+    const float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
+    ix += int(fx); iy += int(fy); iz += int(fz);
+    wx = ux - fx; wy = uy - fy; wz = uz - fz;
+  }
+  if (ix < 0) { ix = 0; wx = 0.0f; } else if (ix > f.nx - 2) { ix = f.nx - 2; wx = 1.0f; }
+  if (iy < 0) { iy = 0; wy = 0.0f; } else if (iy > f.ny - 2) { iy = f.ny - 2; wy = 1.0f; }
+  if (iz < 0) { iz = 0; wz = 0.0f; } else if (iz > f.nz - 2) { iz = f.nz - 2; wz = 1.0f; }
+  if (ix != k.ix || iy != k.iy || iz != k.iz)
+  {
+    cache_load(f, k, ix, iy, iz);
+    scale_cache(k, f.inv_hx, f.inv_hy, f.inv_hz);
+  }
+  return make_float3(cache_eval1(k.a.x, k.b.x, k.c.x, k.d.x, k.e.x, k.f.x, k.g.x, k.h.x, wx, wy, wz),
+                     cache_eval1(k.a.y, k.b.y, k.c.y, k.d.y, k.e.y, k.f.y, k.g.y, k.h.y, wx, wy, wz),
+                     cache_eval1(k.a.z, k.b.z, k.c.z, k.d.z, k.e.z, k.f.z, k.g.z, k.h.z, wx, wy, wz));
+}
+
+// Moves the offset back into [0, 1) and the cell accordingly (exact: the
+// subtraction of an integer-valued floor from a value of magnitude < 2 is exact).
+__device__ __forceinline__ void renormalize(local_position& p)
+{
+  if (!(p.ux >= 0.0f && p.ux < 1.0f)) { const float fl = floorf(p.ux); p.ix += int(fl); p.ux -= fl; }
+  if (!(p.uy >= 0.0f && p.uy < 1.0f)) { const float fl = floorf(p.uy); p.iy += int(fl); p.uy -= fl; }
+  if (!(p.uz >= 0.0f && p.uz < 1.0f)) { const float fl = floorf(p.uz); p.iz += int(fl); p.uz -= fl; }
+}
+
+__device__ __forceinline__ local_position to_local(const field_view& f, const float4& p)
+{
+  local_position q;
+  const axis_cell cx = cell_consistent(p.x, f.ox, f.hx, f.inv_hx);
+  const axis_cell cy = cell_consistent(p.y, f.oy, f.hy, f.inv_hy);
+  const axis_cell cz = cell_consistent(p.z, f.oz, f.hz, f.inv_hz);
+  q.ix = int(cx.s); q.iy = int(cy.s); q.iz = int(cz.s);
+  q.ux = cx.w; q.uy = cy.w; q.uz = cz.w;
+  renormalize(q);   // w can round up to exactly 1
+  return q;
+}
+
+__device__ __forceinline__ float4 to_absolute(const field_view& f, const local_position& q, float w)
+{
+  return make_float4(fmaf(float(q.ix) + q.ux, f.hx, f.ox), fmaf(float(q.iy) + q.uy, f.hy, f.oy),
+                     fmaf(float(q.iz) + q.uz, f.hz, f.oz), w);
+}
+
+__device__ __forceinline__ bool local_inside(const field_view& f, const local_position& q)
+{
+  return q.ix >= 0 && q.ix <= f.nx - 2 && q.iy >= 0 && q.iy <= f.ny - 2 && q.iz >= 0 && q.iz <= f.nz - 2;
+}
+
+// |v_i| <= 1e-5 with v in cells per unit time: |v_i| <= 1e-5 / h_i.
+__device__ __forceinline__ bool is_zero_local(const field_view& f, const float3& v)
+{
+  return fabsf(v.x) <= 1e-5f * f.inv_hx && fabsf(v.y) <= 1e-5f * f.inv_hy && fabsf(v.z) <= 1e-5f * f.inv_hz;
+}
+
+// One classical RK4 (or Euler) step in local coordinates with k1 sampled at q.
+__device__ __forceinline__ void local_step(const field_view& f, cell_cache& k, int rk4, float h, local_position& q, const float3& k1)
+{
+  if (!rk4)
+  {
+    q.ux = fmaf(h, k1.x, q.ux); q.uy = fmaf(h, k1.y, q.uy); q.uz = fmaf(h, k1.z, q.uz);
+    renormalize(q);
+    return;
+  }
+  const float hh = 0.5f * h;
+  const float3 k2 = sample_local(f, k, q.ix, q.iy, q.iz, fmaf(hh, k1.x, q.ux), fmaf(hh, k1.y, q.uy), fmaf(hh, k1.z, q.uz));
+  const float3 k3 = sample_local(f, k, q.ix, q.iy, q.iz, fmaf(hh, k2.x, q.ux), fmaf(hh, k2.y, q.uy), fmaf(hh, k2.z, q.uz));
+  const float3 k4 = sample_local(f, k, q.ix, q.iy, q.iz, fmaf(h, k3.x, q.ux), fmaf(h, k3.y, q.uy), fmaf(h, k3.z, q.uz));
+  const float h6 = h * (1.0f / 6.0f);
+  q.ux = fmaf(h6, k1.x + 2.0f * (k2.x + k3.x) + k4.x, q.ux);
+  q.uy = fmaf(h6, k1.y + 2.0f * (k2.y + k3.y) + k4.y, q.uy);
+  q.uz = fmaf(h6, k1.z + 2.0f * (k2.z + k3.z) + k4.z, q.uz);
+  renormalize(q);
+}
+
 // Face crossed by a particle leaving its block: the reference's else-if ladder
 // (particle_tracer.cpp:288-293) — the first face, in order -x,+x,-y,+y,-z,+z,
 // whose strict bound test holds and whose neighbour exists; -1 if none.
