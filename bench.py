@@ -277,41 +277,128 @@ def run_pathlines(args):
 
 
 def run_serve(args):
-    """The served mixed stream: requests (reference `settings` messages) into
-    the service, Poisson arrivals; throughput and p50/p99 latency of the
-    batched service (2 lanes, batches up to 64) against the plain path (one
-    request at a time, no batching), at saturation and at offered loads below
-    each path's saturation throughput."""
+    """The served mixed stream, end to end from host memory to host memory.
+
+    plain   : one request at a time through the single-request C ABI, as a
+              caller of the plain kernels serves it: upload the request's
+              field from (pinned) host memory, seeds + trace + index + colour
+              or flow map + FTLE, download every result buffer into pinned
+              host buffers, release.
+    batched : the service (2 lanes, batches of up to 64, datasets resident):
+              requests are submitted as reference `settings` messages at their
+              Poisson arrival times; a client thread collects each finished
+              request's buffers into the same pinned host buffers.
+    Latency runs from a request's arrival to its results being in host
+    memory.  Both paths at saturation (every request present at t = 0) and at
+    offered loads of 50 % and 90 % of their own saturation throughput."""
     import threading as th
     import torch
     from pars_gb300 import native, workloads
     from pars_gb300.requests import encode_settings
     ds, reqs = workloads.served_stream_config(seed=4, requests=args.requests)
-    messages = []
+    f32 = np.float32
+    messages, specs = [], []
     for r in reqs:
         d = ds[r["dataset"]]
         step = 0.01 if d["kind"] == "abc" else 0.05
+        iterations = r["steps"] + (2 if r["kind"] == "streamlines" else 1)
+        specs.append({"kind": r["kind"], "dataset": r["dataset"], "stride": r["stride"], "iterations": iterations, "step": step})
         messages.append(encode_settings({
             "mode": r["kind"], "dataset_filepath": d["name"], "seed_generation_stride": [r["stride"]] * 3,
-            "seed_generation_iterations": r["steps"] + (2 if r["kind"] == "streamlines" else 1),
+            "seed_generation_iterations": iterations,
             "particle_tracing_integrator": "runge_kutta_4", "particle_tracing_step_size": step,
             "color_generation_mode": "hsv_constant_s", "color_generation_free_parameter": 0.75}))
 
-    def make(lanes, max_batch):
-        svc = native.Service(0, budget_bytes=160 << 30, lanes=lanes, max_batch=max_batch)
-        for d in ds:
-            gen = workloads.abc_device if d["kind"] == "abc" else workloads.gyre_snapshot_device
-            xyz, offset, size, spacing = gen(torch, d["edge"])
-            svc.add_dataset_device(d["name"], xyz.data_ptr(), (d["edge"],) * 3, offset, size, spacing)
-            del xyz
-            torch.cuda.synchronize()
-        torch.cuda.empty_cache()
-        return svc
+    # Datasets on the device (for the service) and in pinned host memory (for
+    # the plain path, which uploads the request's field every time).
+    device_fields, host_fields = [], []
+    for d in ds:
+        gen = workloads.abc_device if d["kind"] == "abc" else workloads.gyre_snapshot_device
+        xyz, offset, size, spacing = gen(torch, d["edge"])
+        pinned = torch.empty(xyz.shape, dtype=torch.float32, pin_memory=True)
+        pinned.copy_(xyz)
+        device_fields.append((xyz, offset, size, spacing))
+        host_fields.append((pinned, offset, size, spacing))
+    torch.cuda.synchronize()
 
-    def run(svc, rate):
-        """Submits every request at its Poisson arrival time (rate None: all at
-        once); returns (makespan s, latencies ms, particle-steps)."""
-        tickets = [None] * len(messages)
+    # Pinned collection buffers sized for the largest result.
+    cap_vertices, cap_voxels = 1, 1
+    for s in specs:
+        _, offset, size, spacing = host_fields[s["dataset"]]
+        if s["kind"] == "streamlines":
+            st = (spacing * f32(s["stride"])).astype(f32)
+            n = int(np.prod([int(f32(size[i]) / st[i]) for i in range(3)]))
+            cap_vertices = max(cap_vertices, n * s["iterations"])
+        else:
+            scale = f32(1.0) / f32(s["stride"])
+            edge = ds[s["dataset"]]["edge"]
+            cap_voxels = max(cap_voxels, max(1, int(f32(edge) * scale)) ** 3)
+    vbuf = torch.empty(cap_vertices * 4, dtype=torch.float32, pin_memory=True)
+    cbuf = torch.empty(cap_vertices * 4, dtype=torch.float32, pin_memory=True)
+    ibuf = torch.empty(cap_vertices, dtype=torch.int32, pin_memory=True)
+    fbuf = torch.empty(cap_voxels, dtype=torch.float32, pin_memory=True)
+    collected = {"bytes": 0}
+
+    def plain_request(ctx, k):
+        s = specs[k]
+        xyz, offset, size, spacing = host_fields[s["dataset"]]
+        edge = ds[s["dataset"]]["edge"]
+        h = ctx.upload_field_host(xyz.data_ptr(), (edge,) * 3, offset, size, spacing)
+        if s["kind"] == "streamlines":
+            seeds = ctx.seed_generate(offset, size, (spacing * f32(s["stride"])).astype(f32), s["iterations"])
+            summary = ctx.trace(h, seeds, native.RUNGE_KUTTA_4, native.STAGES_RESAMPLED, s["step"])
+            ctx.curves_index()
+            ctx.curves_color("hsv_constant_s", 0.75)
+            for b in range(summary["batches"]):
+                nv, ni, _, _ = ctx.batch_info(b)
+                ctx._call("pars_gpu_curves_download", b, vbuf.data_ptr(), cbuf.data_ptr(), ibuf.data_ptr())
+                collected["bytes"] += 32 * nv + 4 * ni
+            steps = summary["steps"]
+        else:
+            fm, steps = ctx.flow_map_generate(h, s["iterations"], float(f32(1.0) / f32(s["stride"])), native.RUNGE_KUTTA_4,
+                                              native.STAGES_RESAMPLED, s["step"])
+            t = float(f32(s["step"]) * f32(s["iterations"]))
+            shape = ctx.field_info(fm)["shape"]
+            ctx._call("pars_gpu_ftle_generate", fm, t, native.FTLE_REGULAR, fbuf.data_ptr())
+            collected["bytes"] += 4 * int(np.prod(shape))
+            ctx.release_field(fm)
+        ctx.release_field(h)
+        return steps
+
+    def run_plain(ctx, rate):
+        t0 = time.perf_counter()
+        at, lat, steps = 0.0, [], 0
+        per_kind = {"streamlines": 0.0, "ftle": 0.0}
+        for k in range(len(specs)):
+            if rate:
+                at += reqs[k]["gap"] / rate
+                delay = t0 + at - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+            r0 = time.perf_counter()
+            steps += plain_request(ctx, k)
+            per_kind[specs[k]["kind"]] += time.perf_counter() - r0
+            lat.append(1e3 * (time.perf_counter() - (t0 + at)))
+        span = time.perf_counter() - t0
+        breakdown.update({f"{kind}_fraction": v / span for kind, v in per_kind.items()})
+        return span, np.array(lat), steps
+
+    def collect(svc, ticket):
+        info = svc.info(ticket)
+        if info.kind == 0:
+            for b in range(info.batches):
+                nv, ni = svc.batch_into(ticket, b, vbuf.data_ptr(), cbuf.data_ptr(), ibuf.data_ptr())
+                collected["bytes"] += 32 * nv + 4 * ni
+        else:
+            svc.ftle_into(ticket, fbuf.data_ptr())
+            collected["bytes"] += 4 * int(np.prod(list(info.ftle_shape)))
+        steps = info.steps
+        svc.release(ticket)
+        return steps
+
+    def run_service(svc, rate):
+        n = len(messages)
+        tickets, arrival = [None] * n, [0.0] * n
         t0 = time.perf_counter()
 
         def submitter():
@@ -322,41 +409,82 @@ def run_serve(args):
                     delay = t0 + at - time.perf_counter()
                     if delay > 0:
                         time.sleep(delay)
+                arrival[k] = t0 + at
                 tickets[k] = svc.submit(m)
 
         thread = th.Thread(target=submitter)
         thread.start()
-        lat, steps = [], 0
-        for k in range(len(messages)):
-            while tickets[k] is None:
+        lat, steps, pending, nxt = [], 0, [], 0
+        running, collecting = [], 0.0
+        while len(lat) < n:
+            while nxt < n and tickets[nxt] is not None:
+                pending.append(nxt)
+                nxt += 1
+            progress = False
+            for k in list(pending):
+                if svc.wait(tickets[k], 0) == 2:
+                    info = svc.info(tickets[k])
+                    start = arrival[k] + info.queue_ms / 1e3
+                    running.append((start, start + info.run_ms / 1e3))
+                    c0 = time.perf_counter()
+                    steps += collect(svc, tickets[k])
+                    collecting += time.perf_counter() - c0
+                    lat.append(1e3 * (time.perf_counter() - arrival[k]))
+                    pending.remove(k)
+                    progress = True
+            if not progress:
                 time.sleep(0.0002)
-            svc.wait(tickets[k])
-            info = svc.info(tickets[k])
-            lat.append(info.latency_ms)
-            steps += info.steps
-            svc.release(tickets[k])
         thread.join()
-        return time.perf_counter() - t0, np.array(lat), steps
+        span = time.perf_counter() - t0
+        # wall time during which at least one batch ran, and the collector's share
+        busy, end = 0.0, -1e30
+        for a, b in sorted(running):
+            if b > end:
+                busy += b - max(a, end)
+                end = b
+        breakdown["batch_running_fraction"] = busy / span
+        breakdown["collecting_fraction"] = collecting / span
+        return span, np.array(lat), steps
 
-    results = {}
-    for name, lanes, batch in (("plain", 1, 1), ("batched", 2, 64)):
-        svc = make(lanes, batch)
-        for m in messages[:8]:                       # warm-up (autotuning, allocations)
-            svc.wait(svc.submit(m))
-        span, lat, steps = run(svc, None)
+    breakdown = {}
+
+    def summarise(run, target):
+        collected["bytes"] = 0
+        breakdown.clear()
+        span, lat, steps = run(target, None)
         saturation = len(messages) / span
         out = {"saturation_requests_per_s": saturation, "saturation_particle_steps_per_s": steps / span,
-               "saturation_p50_ms": float(np.percentile(lat, 50)), "saturation_p99_ms": float(np.percentile(lat, 99))}
+               "saturation_p50_ms": float(np.percentile(lat, 50)), "saturation_p99_ms": float(np.percentile(lat, 99)),
+               "result_bytes_to_host": collected["bytes"], "saturation_breakdown": dict(breakdown)}
         for load in (0.5, 0.9):
-            span, lat, _ = run(svc, load * saturation)
+            span, lat, _ = run(target, load * saturation)
             out[f"load{int(load * 100)}"] = {"offered_requests_per_s": load * saturation,
                                              "achieved_requests_per_s": len(messages) / span,
                                              "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
-        results[name] = out
-        svc.close()
+        return out
+
+    results = {}
+    ctx = native.Context(0)
+    for k in range(8):                               # warm-up (autotuning, allocations)
+        plain_request(ctx, k)
+    results["plain"] = summarise(run_plain, ctx)
+    ctx.close()
+
+    svc = native.Service(0, budget_bytes=160 << 30, lanes=2, max_batch=64)
+    for d, (xyz, offset, size, spacing) in zip(ds, device_fields):
+        svc.add_dataset_device(d["name"], xyz.data_ptr(), (d["edge"],) * 3, offset, size, spacing)
+    torch.cuda.synchronize()
+    del device_fields
+    torch.cuda.empty_cache()
+    for m in messages[:8]:                           # warm-up
+        t = svc.submit(m)
+        svc.wait(t)
+        collect(svc, t)
+    results["batched"] = summarise(run_service, svc)
+    svc.close()
     print(json.dumps({"workload": f"served_{len(messages)}: {len(messages)} requests (seed 4), 70% streamlines / 30% FTLE on "
-                                  f"{len(ds)} resident ABC / double-gyre fields (edge 64-512), seeds 1k-2M, 200-2000 RK4 steps, "
-                                  "Poisson arrivals",
+                                  f"{len(ds)} ABC / double-gyre fields (edge 64-512), seeds 1k-2M (streamlines <= 16384), "
+                                  "200-2000 RK4 steps, Poisson arrivals; results collected into pinned host buffers",
                       "datasets": ds, "plain": results["plain"], "batched": results["batched"],
                       "throughput_ratio_at_saturation": results["batched"]["saturation_requests_per_s"] /
                                                         results["plain"]["saturation_requests_per_s"]}))

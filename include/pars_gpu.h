@@ -296,8 +296,14 @@ int32_t pars_gpu_batch_tuned   (pars_gpu_context* context, int32_t job_class, in
  * The service queues requests as they arrive.  `lanes` worker threads, each
  * with its own CUDA stream, take batches of queued requests of one kind that
  * fit into the device-memory budget (requests arriving while others run are
- * admitted as memory frees up) and run each batch as one launch; results are
- * copied to host memory before the batch's memory is returned. */
+ * admitted as memory frees up) and run each batch as one launch.  A request's
+ * results stay in device memory until the client copies them out
+ * (pars_gpu_service_result_batch / _result_ftle, into any host buffers; pinned
+ * ones copy fastest) and releases the request; held results count against
+ * the budget.  When no queued request fits and no batch is running, held
+ * results move to host memory, so a client that collects results in any order
+ * cannot stall the queue.  Each lane keeps at most min(budget / (4 lanes),
+ * 8 GiB) of scratch between batches. */
 typedef struct pars_gpu_service pars_gpu_service;
 
 /* The scalar fields of a decoded `settings` message (strings truncated). */

@@ -84,7 +84,7 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
   int steps = 0;
   float4 pos = make_float4(0.f, 0.f, 0.f, 0.f);   // unsteady: absolute position
   float3 lo = make_float3(0.f, 0.f, 0.f);         // unsteady: its compensation term
-  local_position local {0, 0, 0, 0.f, 0.f, 0.f};  // steady: cell + offset
+  local_position local {0, 0, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // steady: cell + offset
   lane_cache<UNSTEADY> cache;
   // current job's parameters (warp-uniform)
   field_view f {};

@@ -213,6 +213,9 @@ private:
 device_buffer acquire_buffer(pars_gpu_context& ctx, std::size_t bytes);
 // Returns a buffer to the cache (freed instead when the cache is full).
 void recycle_buffer(pars_gpu_context& ctx, device_buffer&& buffer);
+// Frees every scratch buffer and the buffer cache after the stream drains
+// (fields and domains stay); the last trace's curves are dropped.
+void release_scratch(pars_gpu_context& ctx);
 
 // Integrator parameters for (integrator, stage mode, step size); throws
 // pars::error for integrators the kernels do not implement.
@@ -301,8 +304,9 @@ void launch_batch_advect(pars_gpu_context& ctx, int job_class, int variant, cons
 void trace_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, const trace_block* device_blocks, long long count,
                   std::vector<long long> block_count, std::vector<int> block_max, const step_rule& rule, bool route_exits,
                   pars_gpu_trace_summary* summary, const step_rule* device_block_rules = nullptr);
-// Batched advection of `jobs` in one persistent launch; returns each job's steps.
-std::vector<unsigned long long> run_batch(pars_gpu_context& ctx, std::vector<batch_job_device>& jobs, int job_class, int variant);
+// Batched advection of `jobs` (one persistent launch per job class: steady,
+// unsteady); returns each job's steps.
+std::vector<unsigned long long> run_batch(pars_gpu_context& ctx, std::vector<batch_job_device>& jobs, int variant);
 pars_partition_info partition(int ranks, int rank, const int32_t domain[3]);
 
 void launch_flow_map(pars_gpu_context& ctx, const field_view& f, const step_rule& rule, int iterations,

@@ -455,11 +455,14 @@ __device__ __forceinline__ void unsteady_step(const field_view& f, const time_ax
 // velocity in cells per unit time and a stage point is u + c * h * k.  A
 // sample inside the current cell needs no floor, division or conversion; the
 // offset keeps 24 bits of precision within its cell however far the cell is
-// from the origin.
+// from the origin.  A compensation term (lx, ly, lz) carries what the rounding
+// of each step's update dropped from the offset (as compensated_add does for
+// absolute positions), so rounding does not accumulate over the steps.
 struct local_position
 {
   int   ix, iy, iz;
   float ux, uy, uz;
+  float lx, ly, lz;
 };
 
 __device__ __forceinline__ void scale3(float3& v, float sx, float sy, float sz) { v.x *= sx; v.y *= sy; v.z *= sz; }
@@ -495,8 +498,10 @@ __device__ __forceinline__ float3 sample_local(const field_view& f, cell_cache& 
                      cache_eval1(k.a.z, k.b.z, k.c.z, k.d.z, k.e.z, k.f.z, k.g.z, k.h.z, wx, wy, wz));
 }
 
-// Moves the offset back into [0, 1) and the cell accordingly (exact: the
-// subtraction of an integer-valued floor from a value of magnitude < 2 is exact).
+// Moves the offset back into [0, 1) and the cell accordingly.  For an offset
+// >= 1 the subtraction of its floor is exact; for a negative offset u, 1 + u
+// rounds to within 2^-25 and may give exactly 1 (the same point as offset 0
+// of the next cell).
 __device__ __forceinline__ void renormalize(local_position& p)
 {
   if (!(p.ux >= 0.0f && p.ux < 1.0f)) { const float fl = floorf(p.ux); p.ix += int(fl); p.ux -= fl; }
@@ -512,6 +517,7 @@ __device__ __forceinline__ local_position to_local(const field_view& f, const fl
   const axis_cell cz = cell_consistent(p.z, f.oz, f.hz, f.inv_hz);
   q.ix = int(cx.s); q.iy = int(cy.s); q.iz = int(cz.s);
   q.ux = cx.w; q.uy = cy.w; q.uz = cz.w;
+  q.lx = q.ly = q.lz = 0.0f;
   renormalize(q);   // w can round up to exactly 1
   return q;
 }
@@ -538,7 +544,9 @@ __device__ __forceinline__ void local_step(const field_view& f, cell_cache& k, i
 {
   if (!rk4)
   {
-    q.ux = fmaf(h, k1.x, q.ux); q.uy = fmaf(h, k1.y, q.uy); q.uz = fmaf(h, k1.z, q.uz);
+    compensated_add(q.ux, q.lx, h * k1.x);
+    compensated_add(q.uy, q.ly, h * k1.y);
+    compensated_add(q.uz, q.lz, h * k1.z);
     renormalize(q);
     return;
   }
@@ -547,9 +555,9 @@ __device__ __forceinline__ void local_step(const field_view& f, cell_cache& k, i
   const float3 k3 = sample_local(f, k, q.ix, q.iy, q.iz, fmaf(hh, k2.x, q.ux), fmaf(hh, k2.y, q.uy), fmaf(hh, k2.z, q.uz));
   const float3 k4 = sample_local(f, k, q.ix, q.iy, q.iz, fmaf(h, k3.x, q.ux), fmaf(h, k3.y, q.uy), fmaf(h, k3.z, q.uz));
   const float h6 = h * (1.0f / 6.0f);
-  q.ux = fmaf(h6, k1.x + 2.0f * (k2.x + k3.x) + k4.x, q.ux);
-  q.uy = fmaf(h6, k1.y + 2.0f * (k2.y + k3.y) + k4.y, q.uy);
-  q.uz = fmaf(h6, k1.z + 2.0f * (k2.z + k3.z) + k4.z, q.uz);
+  compensated_add(q.ux, q.lx, h6 * (k1.x + 2.0f * (k2.x + k3.x) + k4.x));
+  compensated_add(q.uy, q.ly, h6 * (k1.y + 2.0f * (k2.y + k3.y) + k4.y));
+  compensated_add(q.uz, q.lz, h6 * (k1.z + 2.0f * (k2.z + k3.z) + k4.z));
   renormalize(q);
 }
 

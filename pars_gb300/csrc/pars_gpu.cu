@@ -15,19 +15,29 @@
 
 using pars::device_buffer;
 
+namespace
+{
+// Every grow-only scratch buffer of a context (not its fields or domains).
+template <typename context_type, typename visit_type>
+void for_each_scratch(context_type& c, visit_type&& visit)
+{
+  for (auto* b : {&c.particles_in, &c.particles_next, &c.slots, &c.kept, &c.written, &c.offsets, &c.block_of,
+                  &c.block_of_next, &c.exits, &c.exit_keys, &c.exit_keys_sorted, &c.exit_order,
+                  &c.exit_order_sorted, &c.counters, &c.block_max, &c.cub_temp, &c.scan_input, &c.tile_counts,
+                  &c.tile_offsets, &c.staging, &c.ftle, &c.curves.vertices, &c.curves.colors,
+                  &c.curves.indices, &c.boundary_positions, &c.boundary_offsets, &c.batch_jobs,
+                  &c.batch_counters, &c.single_block})
+    visit(*b);
+}
+}
+
 long long pars_gpu_context::held_bytes() const
 {
   long long total = 0;
   for (auto& f : fields) total += (long long)f.second->data.bytes();
   for (auto& d : domains) total += (long long)d.second->device_blocks.bytes();
-  const device_buffer* scratch[] = {&particles_in, &particles_next, &slots, &kept, &written, &offsets, &block_of,
-                                    &block_of_next, &exits, &exit_keys, &exit_keys_sorted, &exit_order,
-                                    &exit_order_sorted, &counters, &block_max, &cub_temp, &scan_input, &tile_counts,
-                                    &tile_offsets, &staging, &ftle, &curves.vertices, &curves.colors,
-                                    &curves.indices, &boundary_positions, &boundary_offsets, &batch_jobs,
-                                    &batch_counters};
-  for (auto* b : scratch) total += (long long)b->bytes();
-  return total + (long long)buffer_cache_bytes + (long long)single_block.bytes();
+  for_each_scratch(*this, [&](const pars::device_buffer& b) { total += (long long)b.bytes(); });
+  return total + (long long)buffer_cache_bytes;
 }
 
 namespace pars
@@ -68,6 +78,18 @@ void recycle_buffer(pars_gpu_context& ctx, device_buffer&& buffer)
   }
   ctx.buffer_cache_bytes += bytes;
   ctx.buffer_cache.emplace(bytes, std::move(buffer));
+}
+
+void release_scratch(pars_gpu_context& ctx)
+{
+  PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+  for_each_scratch(ctx, [](device_buffer& b) { b.release(); });
+  ctx.buffer_cache.clear();
+  ctx.buffer_cache_bytes = 0;
+  ctx.curves.vertex_total = 0;
+  ctx.curves.indexed = ctx.curves.colored = false;
+  ctx.curves.batches.clear();
+  ctx.ftle_count = 0;
 }
 
 launch_scope::launch_scope(pars_gpu_context& ctx, const char* name) : ctx_(ctx), name_(name)
@@ -432,37 +454,59 @@ void trace_single(pars_gpu_context& ctx, int32_t field, long long count, int32_t
   run_rounds(ctx, blocks, device_blocks, count, block_count, block_max, rule, false, summary);
 }
 
-// Runs batched jobs in one persistent launch and returns each job's steps.
-// variant < 0 uses the context's tuned launch shape for the job class, tuning
-// it first if needed: every job capped at 16384 seeds, each shape timed twice
-// with CUDA events, the fastest kept.
-std::vector<unsigned long long> execute_batch(pars_gpu_context& ctx, std::vector<batch_job_device>& jobs, int job_class, int variant)
+// Runs batched jobs and returns each job's steps.  Jobs on steady fields (one
+// slice) and jobs on unsteady fields run in two persistent launches, one per
+// job class, so that a job's arithmetic, and so its result, does not depend on
+// the other jobs of the batch.  variant < 0 uses the context's tuned launch
+// shape for each class, tuning it first if needed: every job of the class
+// capped at 16384 seeds, each shape timed twice with CUDA events, the fastest
+// kept.
+std::vector<unsigned long long> execute_batch(pars_gpu_context& ctx, std::vector<batch_job_device>& jobs, int variant)
 {
   const int count = int(jobs.size());
-  ctx.batch_jobs.reserve(sizeof(batch_job_device) * count);
-  ctx.batch_counters.reserve(sizeof(unsigned long long) * (count + 1));
-  auto* counters = ctx.batch_counters.as<unsigned long long>();
+  // steady jobs first, then unsteady ones; order[k] = caller's index of job k
+  std::vector<int> order;
+  order.reserve(count);
+  for (int j = 0; j < count; ++j) if (jobs[j].time.nt <= 1) order.push_back(j);
+  const int steady = int(order.size());
+  for (int j = 0; j < count; ++j) if (jobs[j].time.nt > 1) order.push_back(j);
+  std::vector<batch_job_device> queue(count);
+  for (int k = 0; k < count; ++k) queue[k] = jobs[order[k]];
+  const int first[2] = {0, steady}, size[2] = {steady, count - steady};
 
-  // The device queue: each job's seeds in pools of batch_pool_seeds(); counter
-  // 0 hands out pools, counters 1.. count each job's steps.
-  auto run = [&](int v) {
+  ctx.batch_jobs.reserve(sizeof(batch_job_device) * count);
+  ctx.batch_counters.reserve(sizeof(unsigned long long) * (count + 2));
+  auto* counters = ctx.batch_counters.as<unsigned long long>();
+  auto* device_jobs = ctx.batch_jobs.as<batch_job_device>();
+
+  // The device queues: each job's seeds in pools of batch_pool_seeds(), numbered
+  // per class; counters 0 and 1 hand out the pools of the two classes, counters
+  // 2.. count each job's steps.
+  long long pools[2] = {0, 0};
+  auto upload = [&] {
     const int pool = batch_pool_seeds();
-    long long pools = 0;
-    for (int j = 0; j < count; ++j)
+    for (int c = 0; c < 2; ++c)
     {
-      jobs[j].first_pool = pools;
-      jobs[j].steps = counters + 1 + j;
-      pools += (jobs[j].seed_count + pool - 1) / pool;
+      pools[c] = 0;
+      for (int k = first[c]; k < first[c] + size[c]; ++k)
+      {
+        queue[k].first_pool = pools[c];
+        queue[k].steps = counters + 2 + k;
+        pools[c] += (queue[k].seed_count + pool - 1) / pool;
+      }
     }
-    PARS_CUDA(cudaMemcpyAsync(ctx.batch_jobs.get(), jobs.data(), sizeof(batch_job_device) * count, cudaMemcpyHostToDevice, ctx.stream));
-    PARS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (count + 1), ctx.stream));
-    launch_batch_advect(ctx, job_class, v, ctx.batch_jobs.as<const batch_job_device>(), count, pools, counters);
+    PARS_CUDA(cudaMemcpyAsync(device_jobs, queue.data(), sizeof(batch_job_device) * count, cudaMemcpyHostToDevice, ctx.stream));
+    PARS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (count + 2), ctx.stream));
+  };
+  auto launch = [&](int c, int v) {
+    if (size[c] > 0) launch_batch_advect(ctx, c, v, device_jobs + first[c], size[c], pools[c], counters + c);
   };
 
-  if (variant < 0 && ctx.batch_variant[job_class] < 0)
+  for (int c = 0; c < 2; ++c)
   {
+    if (variant >= 0 || size[c] == 0 || ctx.batch_variant[c] >= 0) continue;
     std::vector<long long> full(count);
-    for (int j = 0; j < count; ++j) { full[j] = jobs[j].seed_count; jobs[j].seed_count = std::min(full[j], 16384LL); }
+    for (int k = 0; k < count; ++k) { full[k] = queue[k].seed_count; queue[k].seed_count = std::min(full[k], 16384LL); }
     cudaEvent_t a, b;
     PARS_CUDA(cudaEventCreate(&a));
     PARS_CUDA(cudaEventCreate(&b));
@@ -473,8 +517,9 @@ std::vector<unsigned long long> execute_batch(pars_gpu_context& ctx, std::vector
       float fastest = 0.0f;
       for (int rep = 0; rep < 2; ++rep)
       {
+        upload();
         PARS_CUDA(cudaEventRecord(a, ctx.stream));
-        run(v);
+        launch(c, v);
         PARS_CUDA(cudaEventRecord(b, ctx.stream));
         PARS_CUDA(cudaEventSynchronize(b));
         float ms = 0.0f;
@@ -485,14 +530,17 @@ std::vector<unsigned long long> execute_batch(pars_gpu_context& ctx, std::vector
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    ctx.batch_variant[job_class] = best_v;
-    for (int j = 0; j < count; ++j) jobs[j].seed_count = full[j];
+    ctx.batch_variant[c] = best_v;
+    for (int k = 0; k < count; ++k) queue[k].seed_count = full[k];
   }
-  run(variant >= 0 ? variant : ctx.batch_variant[job_class]);
-  std::vector<unsigned long long> steps(count + 1);
-  PARS_CUDA(cudaMemcpyAsync(steps.data(), counters, sizeof(unsigned long long) * (count + 1), cudaMemcpyDeviceToHost, ctx.stream));
+  upload();
+  for (int c = 0; c < 2; ++c) launch(c, variant >= 0 ? variant : ctx.batch_variant[c]);
+  std::vector<unsigned long long> steps(count + 2);
+  PARS_CUDA(cudaMemcpyAsync(steps.data(), counters, sizeof(unsigned long long) * (count + 2), cudaMemcpyDeviceToHost, ctx.stream));
   PARS_CUDA(cudaStreamSynchronize(ctx.stream));
-  return std::vector<unsigned long long>(steps.begin() + 1, steps.end());
+  std::vector<unsigned long long> result(count);
+  for (int k = 0; k < count; ++k) result[order[k]] = steps[2 + k];
+  return result;
 }
 
 std::size_t checked_bytes(long long count, std::size_t element)
@@ -512,9 +560,9 @@ void trace_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks,
              device_block_rules);
 }
 
-std::vector<unsigned long long> run_batch(pars_gpu_context& ctx, std::vector<batch_job_device>& jobs, int job_class, int variant)
+std::vector<unsigned long long> run_batch(pars_gpu_context& ctx, std::vector<batch_job_device>& jobs, int variant)
 {
-  return execute_batch(ctx, jobs, job_class, variant);
+  return execute_batch(ctx, jobs, variant);
 }
 
 pars_partition_info partition(int ranks, int rank, const int32_t domain[3]) { return partition_of(ranks, rank, domain); }
@@ -1060,7 +1108,7 @@ int32_t pars_gpu_flow_map_generate(pars_gpu_context* ctx, int32_t field, int32_t
       d.ux = entry->shape[0]; d.uy = entry->shape[1]; d.uz = entry->shape[2];
       d.end_positions = entry->data.as<float4>();
       d.end_steps = nullptr;
-      const auto s = execute_batch(*ctx, job, f.slices > 1 ? 1 : 0, -1);
+      const auto s = execute_batch(*ctx, job, -1);
       if (steps) *steps = (int64_t)s[0];
     }
     *flow_map = add_field(*ctx, std::move(entry));
@@ -1107,7 +1155,6 @@ int32_t pars_gpu_batch_advect(pars_gpu_context* ctx, pars_gpu_batch_job* jobs, i
     PARS_REQUIRE(variant >= -1 && variant < batch_variant_count(), "unknown launch variant");
     if (count == 0) return;
     std::vector<batch_job_device> device_jobs(count);
-    bool unsteady = false;
     for (int j = 0; j < count; ++j)
     {
       const pars_gpu_batch_job& in = jobs[j];
@@ -1134,9 +1181,8 @@ int32_t pars_gpu_batch_advect(pars_gpu_context* ctx, pars_gpu_batch_job* jobs, i
       d.px = in.lattice_count[0]; d.py = in.lattice_count[1]; d.pz = in.lattice_count[2];
       d.end_positions = reinterpret_cast<float4*>(in.end_positions);
       d.end_steps = in.end_steps;
-      unsteady = unsteady || f.slices > 1;
     }
-    const std::vector<unsigned long long> steps = execute_batch(*ctx, device_jobs, unsteady ? 1 : 0, variant);
+    const std::vector<unsigned long long> steps = execute_batch(*ctx, device_jobs, variant);
     for (int j = 0; j < count; ++j) jobs[j].steps = (int64_t)steps[j];
   });
 }

@@ -4,9 +4,14 @@
 // `settings` message at a time, runs pipeline::execute on it and replies.
 // Here requests are queued as they arrive and several lanes (each a context
 // with its own CUDA stream and worker thread) take batches from the queue:
-//  * admission: a request enters a batch only while the device memory the
-//    running batches are estimated to need stays within the budget; memory is
-//    returned when a batch completes (its results are then on the host);
+//  * admission: a request enters a batch only while the device memory that
+//    the running batches are estimated to need, plus the results held on the
+//    device, stays within the budget;
+//  * results: each request's buffers (vertices, colours, indices or the FTLE
+//    field) stay on the device, in one allocation from the service's
+//    stream-ordered pool, until the client copies them into its own host
+//    buffers and releases the request; when no queued request fits and no
+//    batch runs, held results move to host memory so that the queue moves on;
 //  * batching: a lane takes every queued request of the same kind that fits
 //    (up to max_batch) and runs them as one launch — FTLE requests as jobs of
 //    the persistent batched advection engine, streamline requests as blocks of
@@ -48,6 +53,11 @@ struct dataset
   float       offset[3], size[3], spacing[3];
 };
 
+struct curve_span
+{
+  int64_t vertex_offset, vertex_count, index_offset, index_count;
+};
+
 struct request
 {
   int64_t            ticket = 0;
@@ -64,11 +74,18 @@ struct request
   std::string        error;
   clock_type::time_point submitted, started, finished;
   long long          steps = 0;
-  // results on the host
-  std::vector<std::vector<float4>>  vertices, colors;
-  std::vector<std::vector<int32_t>> indices;
-  std::vector<float> ftle_values;
   int                ftle_shape[3] = {0, 0, 0};
+  // Results: one device allocation from the service's pool, laid out as
+  // vertices (float4 [vertex_total]), colours (float4 [vertex_total]) and
+  // indices (int32 [index_total]) for streamlines, float [voxels] for FTLE;
+  // `spilled` holds the same bytes once they were moved to host memory.
+  std::mutex              result_mutex;
+  char*                   result = nullptr;
+  std::size_t             result_bytes = 0;
+  std::vector<char>       spilled;
+  bool                    released = false;
+  std::vector<curve_span> spans;   // streamlines: one per integral_curves batch
+  int64_t                 vertex_total = 0, index_total = 0;
 };
 
 int integrator_of(const std::string& name)
@@ -93,8 +110,12 @@ struct pars_gpu_service
 {
   int                                  device = 0;
   std::size_t                          budget = 0;
-  std::size_t                          in_use = 0;
+  std::size_t                          in_use = 0;      // running batches' estimates + held results
+  std::size_t                          held = 0;        // result bytes held on the device
+  std::size_t                          lane_keep = 0;   // scratch a lane keeps between batches
   int                                  max_batch = 64;
+  cudaMemPool_t                        pool = nullptr;  // result allocations
+  cudaStream_t                         copy_stream = nullptr;   // client copies and frees
   pars_gpu_context*                    owner = nullptr;
   std::vector<pars_gpu_context*>       lanes;
   std::vector<std::thread>             workers;
@@ -105,6 +126,7 @@ struct pars_gpu_service
   std::vector<pars::dataset>           datasets;
   std::map<std::string, int>           dataset_index;
   bool                                 stopping = false;
+  bool                                 spilling = false;
   int64_t                              next_ticket = 1;
   int                                  running_batches = 0;
 };
@@ -130,14 +152,44 @@ std::size_t estimate_bytes(const request& r, const dataset& d)
     seeds *= std::size_t(std::max(0, int(d.size[i] / (d.spacing[i] * float(stride)))));
   }
   const std::size_t slots = seeds * std::size_t(std::max(1, r.s.seed_generation_iterations));
-  // padded slots + packed vertices + colours + indices + particle records
-  return slots * (sizeof(float4) * 3 + sizeof(int32_t)) + seeds * (sizeof(pars_particle) * 2 + 32) + (1 << 20);
+  // padded slots + packed vertices + colours + indices + particle records,
+  // and the result (vertices, colours, indices)
+  return slots * (sizeof(float4) * 5 + sizeof(int32_t) * 2) + seeds * (sizeof(pars_particle) * 2 + 32) + (1 << 20);
 }
 
 void fail(request& r, int32_t status, const std::string& message)
 {
   r.status = status;
   r.error = message;
+}
+
+void allocate_result(pars_gpu_service& svc, pars_gpu_context& c, request& r, std::size_t bytes)
+{
+  void* p = nullptr;
+  PARS_CUDA(cudaMallocFromPoolAsync(&p, std::max<std::size_t>(bytes, 256), svc.pool, c.stream));
+  r.result = static_cast<char*>(p);
+  r.result_bytes = bytes;
+}
+
+// Returns a request's device result to the pool (stream-ordered on `stream`).
+void free_result(request& r, cudaStream_t stream)
+{
+  if (r.result) cudaFreeAsync(r.result, stream);
+  r.result = nullptr;
+}
+
+// Copies `bytes` at `offset` of a finished request's result into host `out`,
+// from the device (on the service's copy stream) or from its spilled copy.
+// The caller holds r.result_mutex and synchronises the copy stream.
+void copy_result(pars_gpu_service& svc, const request& r, std::size_t offset, void* out, std::size_t bytes)
+{
+  if (!out || bytes == 0) return;
+  if (r.result)
+    PARS_CUDA(cudaMemcpyAsync(out, r.result + offset, bytes, cudaMemcpyDeviceToHost, svc.copy_stream));
+  else if (offset + bytes <= r.spilled.size())
+    std::memcpy(out, r.spilled.data() + offset, bytes);
+  else
+    throw error(PARS_ERR_STATE, "the request has no result");
 }
 
 // FTLE requests: flow maps as jobs of one batched launch, then the FTLE kernel
@@ -181,8 +233,7 @@ void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std:
     j.end_steps = nullptr;
     jobs.push_back(j);
   }
-  const auto steps = run_batch(c, jobs, 0, -1);
-  device_buffer values;
+  const auto steps = run_batch(c, jobs, -1);
   for (std::size_t k = 0; k < batch.size(); ++k)
   {
     request& r = *batch[k];
@@ -192,12 +243,10 @@ void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std:
     fv.nx = r.ftle_shape[0]; fv.ny = r.ftle_shape[1]; fv.nz = r.ftle_shape[2];
     fv.hx = jobs[k].sx; fv.hy = jobs[k].sy; fv.hz = jobs[k].sz;
     const long long voxels = (long long)fv.nx * fv.ny * fv.nz;
-    values.reserve(sizeof(float) * voxels);
+    allocate_result(svc, c, r, sizeof(float) * voxels);
     // time = step * iterations in FP32, as pipeline.cpp:403 sets it
     const float time = r.s.particle_tracing_step_size * float(r.s.seed_generation_iterations);
-    launch_ftle(c, fv, time == 0.0f ? 1.0 : double(time), r.ftle_mode, values.as<float>());
-    r.ftle_values.resize(voxels);
-    PARS_CUDA(cudaMemcpyAsync(r.ftle_values.data(), values.get(), sizeof(float) * voxels, cudaMemcpyDeviceToHost, c.stream));
+    launch_ftle(c, fv, time == 0.0f ? 1.0 : double(time), r.ftle_mode, reinterpret_cast<float*>(r.result));
   }
   PARS_CUDA(cudaStreamSynchronize(c.stream));
   for (auto& f : flows) recycle_buffer(c, std::move(f));
@@ -282,33 +331,70 @@ void run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vecto
                           b.index_count, r.color_mode, r.s.color_generation_free_parameter, curves.colors.as<float4>() + b.vertex_offset);
   }
   curves.indexed = curves.colored = true;
-  for (auto& b : curves.batches)
+  // Each request's curve batches move (device to device) into its own result.
+  std::vector<std::size_t> span_of(curves.batches.size());
+  for (std::size_t i = 0; i < curves.batches.size(); ++i)
   {
+    const auto& b = curves.batches[i];
     request& r = *batch[b.rank];
-    r.vertices.emplace_back(b.vertex_count);
-    r.colors.emplace_back(b.vertex_count);
-    r.indices.emplace_back(b.index_count);
+    span_of[i] = r.spans.size();
+    r.spans.push_back({r.vertex_total, b.vertex_count, r.index_total, b.index_count});
+    r.vertex_total += b.vertex_count;
+    r.index_total += b.index_count;
+  }
+  for (auto& rp : batch)
+    allocate_result(svc, c, *rp, std::size_t(rp->vertex_total) * 2 * sizeof(float4) + std::size_t(rp->index_total) * sizeof(int32_t));
+  for (std::size_t i = 0; i < curves.batches.size(); ++i)
+  {
+    const auto& b = curves.batches[i];
+    request& r = *batch[b.rank];
+    const curve_span& s = r.spans[span_of[i]];
+    char* colors = r.result + sizeof(float4) * r.vertex_total;
+    char* indices = r.result + 2 * sizeof(float4) * r.vertex_total;
     if (b.vertex_count)
     {
-      PARS_CUDA(cudaMemcpyAsync(r.vertices.back().data(), curves.vertices.as<float4>() + b.vertex_offset, sizeof(float4) * b.vertex_count,
-                                cudaMemcpyDeviceToHost, c.stream));
-      PARS_CUDA(cudaMemcpyAsync(r.colors.back().data(), curves.colors.as<float4>() + b.vertex_offset, sizeof(float4) * b.vertex_count,
-                                cudaMemcpyDeviceToHost, c.stream));
+      PARS_CUDA(cudaMemcpyAsync(r.result + sizeof(float4) * s.vertex_offset, curves.vertices.as<float4>() + b.vertex_offset,
+                                sizeof(float4) * b.vertex_count, cudaMemcpyDeviceToDevice, c.stream));
+      PARS_CUDA(cudaMemcpyAsync(colors + sizeof(float4) * s.vertex_offset, curves.colors.as<float4>() + b.vertex_offset,
+                                sizeof(float4) * b.vertex_count, cudaMemcpyDeviceToDevice, c.stream));
     }
     if (b.index_count)
-      PARS_CUDA(cudaMemcpyAsync(r.indices.back().data(), curves.indices.as<int>() + b.index_offset, sizeof(int) * b.index_count,
-                                cudaMemcpyDeviceToHost, c.stream));
+      PARS_CUDA(cudaMemcpyAsync(indices + sizeof(int32_t) * s.index_offset, curves.indices.as<int>() + b.index_offset,
+                                sizeof(int32_t) * b.index_count, cudaMemcpyDeviceToDevice, c.stream));
   }
   PARS_CUDA(cudaStreamSynchronize(c.stream));
   // Steps per request: each curve holds its seed, one vertex per step and the
   // termination vertex (remaining_iterations >= 2; one block, one round).
   for (std::size_t k = 0; k < batch.size(); ++k)
-  {
-    long long vertices = 0;
-    for (auto& v : batch[k]->vertices) vertices += (long long)v.size();
-    batch[k]->steps = batch[k]->s.seed_generation_iterations >= 2 ? std::max(0LL, vertices - 2 * block_count[k]) : 0;
-  }
+    batch[k]->steps = batch[k]->s.seed_generation_iterations >= 2 ? std::max(0LL, (long long)batch[k]->vertex_total - 2 * block_count[k]) : 0;
   (void)summary;
+}
+
+// Moves every finished request's device result to host memory (the queue is
+// blocked on held results and no batch runs); returns the bytes freed.
+std::size_t spill_results(pars_gpu_service& svc, pars_gpu_context& c, const std::vector<std::shared_ptr<request>>& finished)
+{
+  std::size_t freed = 0;
+  for (auto& rp : finished)
+  {
+    request& r = *rp;
+    std::lock_guard<std::mutex> lock(r.result_mutex);
+    if (!r.result || r.released) continue;
+    r.spilled.resize(r.result_bytes);
+    if (r.result_bytes)
+      PARS_CUDA(cudaMemcpyAsync(r.spilled.data(), r.result, r.result_bytes, cudaMemcpyDeviceToHost, c.stream));
+    PARS_CUDA(cudaStreamSynchronize(c.stream));
+    free_result(r, c.stream);
+    freed += r.result_bytes;
+  }
+  PARS_CUDA(cudaStreamSynchronize(c.stream));
+  return freed;
+}
+
+// Returns scratch beyond what a lane keeps between batches.
+void trim_lane(pars_gpu_service& svc, pars_gpu_context& c)
+{
+  if ((std::size_t)c.held_bytes() > svc.lane_keep) release_scratch(c);
 }
 
 void worker(pars_gpu_service* svc, int lane)
@@ -344,21 +430,46 @@ void worker(pars_gpu_service* svc, int lane)
           else ++it;
         }
         if (!batch.empty()) break;
+        if (!svc->queue.empty() && svc->running_batches == 0 && svc->held > 0 && !svc->spilling)
+        {
+          // Nothing fits because finished results hold the budget: move them
+          // to host memory (the client still collects them the same way).
+          std::vector<std::shared_ptr<request>> finished;
+          for (auto& t : svc->requests) if (t.second->state == done) finished.push_back(t.second);
+          svc->spilling = true;
+          lock.unlock();
+          std::size_t freed = 0;
+          try { freed = spill_results(*svc, c, finished); } catch (const std::exception&) {}
+          lock.lock();
+          svc->spilling = false;
+          svc->held -= std::min(svc->held, freed);
+          svc->in_use -= std::min(svc->in_use, freed);
+          continue;
+        }
         svc->work.wait(lock);
       }
       svc->in_use += reserved;
       ++svc->running_batches;
     }
+    bool ok = true;
     try
     {
       if (kind == ftle) run_ftle_batch(*svc, c, batch);
       else run_streamline_batch(*svc, c, batch, stage_mode);
     }
-    catch (const error& e) { for (auto& r : batch) fail(*r, e.status, e.what()); }
-    catch (const std::exception& e) { for (auto& r : batch) fail(*r, PARS_ERR_STATE, e.what()); }
+    catch (const error& e) { ok = false; for (auto& r : batch) fail(*r, e.status, e.what()); }
+    catch (const std::exception& e) { ok = false; for (auto& r : batch) fail(*r, PARS_ERR_STATE, e.what()); }
+    if (!ok)
+    {
+      for (auto& r : batch) { free_result(*r, c.stream); r->result_bytes = 0; r->spans.clear(); }
+      cudaStreamSynchronize(c.stream);
+    }
+    try { trim_lane(*svc, c); } catch (const std::exception&) {}
     {
       std::lock_guard<std::mutex> lock(svc->mutex);
       svc->in_use -= reserved;
+      for (auto& r : batch)
+        if (r->result) { svc->in_use += r->result_bytes; svc->held += r->result_bytes; }
       --svc->running_batches;
       for (auto& r : batch) { r->state = done; r->finished = clock_type::now(); }
     }
@@ -422,8 +533,25 @@ int32_t pars_gpu_service_create(pars_gpu_service** service, int32_t device, int6
   if (!svc) return PARS_ERR_OUT_OF_MEMORY;
   svc->device = device;
   svc->budget = std::size_t(budget_bytes);
+  svc->lane_keep = std::min<std::size_t>(svc->budget / (4 * std::size_t(lanes)), std::size_t(8) << 30);
   svc->max_batch = max_batch;
   int32_t status = pars_gpu_create(&svc->owner, device);
+  if (status == PARS_OK)
+  {
+    // A pool that keeps up to lane_keep bytes of freed results for reuse.
+    cudaMemPoolProps props {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    uint64_t keep = svc->lane_keep;
+    if (cudaSetDevice(device) != cudaSuccess || cudaMemPoolCreate(&svc->pool, &props) != cudaSuccess ||
+        cudaMemPoolSetAttribute(svc->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&svc->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+    {
+      (void)cudaGetLastError();
+      status = PARS_ERR_CUDA;
+    }
+  }
   for (int i = 0; status == PARS_OK && i < lanes; ++i)
   {
     pars_gpu_context* c = nullptr;
@@ -434,6 +562,8 @@ int32_t pars_gpu_service_create(pars_gpu_service** service, int32_t device, int6
   {
     for (auto* c : svc->lanes) pars_gpu_destroy(c);
     if (svc->owner) pars_gpu_destroy(svc->owner);
+    if (svc->copy_stream) cudaStreamDestroy(svc->copy_stream);
+    if (svc->pool) cudaMemPoolDestroy(svc->pool);
     delete svc;
     return status;
   }
@@ -451,8 +581,18 @@ int32_t pars_gpu_service_destroy(pars_gpu_service* svc)
   }
   svc->work.notify_all();
   for (auto& t : svc->workers) t.join();
+  cudaSetDevice(svc->device);
+  for (auto& t : svc->requests)
+  {
+    std::lock_guard<std::mutex> lock(t.second->result_mutex);
+    free_result(*t.second, svc->copy_stream);
+  }
+  svc->requests.clear();
+  cudaStreamSynchronize(svc->copy_stream);
   for (auto* c : svc->lanes) pars_gpu_destroy(c);
   pars_gpu_destroy(svc->owner);
+  cudaStreamDestroy(svc->copy_stream);
+  cudaMemPoolDestroy(svc->pool);
   delete svc;
   return PARS_OK;
 }
@@ -557,7 +697,7 @@ int32_t pars_gpu_service_result_info(pars_gpu_service* svc, int64_t ticket, pars
     info->state = r->state;
     info->status = r->status;
     info->kind = r->kind;
-    info->batches = (int64_t)r->vertices.size();
+    info->batches = r->state == done ? (int64_t)r->spans.size() : 0;
     for (int i = 0; i < 3; ++i) info->ftle_shape[i] = r->ftle_shape[i];
     info->steps = r->steps;
     using ms = std::chrono::duration<double, std::milli>;
@@ -570,41 +710,83 @@ int32_t pars_gpu_service_result_batch(pars_gpu_service* svc, int64_t ticket, int
                                       float* vertex_data, float* color_data, int32_t* index_data)
 {
   return service_guard(svc, [&] {
-    std::lock_guard<std::mutex> lock(svc->mutex);
-    auto r = find_request(svc, ticket);
-    if (r->state != done) throw error(PARS_ERR_STATE, "request has not finished");
-    PARS_REQUIRE(batch >= 0 && batch < (int64_t)r->vertices.size(), "batch out of range");
-    if (vertices) *vertices = (int64_t)r->vertices[batch].size();
-    if (indices) *indices = (int64_t)r->indices[batch].size();
-    if (vertex_data && !r->vertices[batch].empty()) std::memcpy(vertex_data, r->vertices[batch].data(), 16 * r->vertices[batch].size());
-    if (color_data && !r->colors[batch].empty()) std::memcpy(color_data, r->colors[batch].data(), 16 * r->colors[batch].size());
-    if (index_data && !r->indices[batch].empty()) std::memcpy(index_data, r->indices[batch].data(), 4 * r->indices[batch].size());
+    std::shared_ptr<request> r;
+    {
+      std::lock_guard<std::mutex> lock(svc->mutex);
+      r = find_request(svc, ticket);
+      if (r->state != done) throw error(PARS_ERR_STATE, "request has not finished");
+    }
+    std::lock_guard<std::mutex> lock(r->result_mutex);
+    if (r->released) throw error(PARS_ERR_NOT_FOUND, "request was released");
+    PARS_REQUIRE(r->kind == streamlines, "not a streamline request");
+    PARS_REQUIRE(batch >= 0 && batch < (int64_t)r->spans.size(), "batch out of range");
+    const curve_span& s = r->spans[batch];
+    if (vertices) *vertices = s.vertex_count;
+    if (indices) *indices = s.index_count;
+    PARS_CUDA(cudaSetDevice(svc->device));
+    const std::size_t colors = sizeof(float4) * r->vertex_total, index_base = 2 * colors;
+    copy_result(*svc, *r, sizeof(float4) * s.vertex_offset, vertex_data, sizeof(float4) * s.vertex_count);
+    copy_result(*svc, *r, colors + sizeof(float4) * s.vertex_offset, color_data, sizeof(float4) * s.vertex_count);
+    copy_result(*svc, *r, index_base + sizeof(int32_t) * s.index_offset, index_data, sizeof(int32_t) * s.index_count);
+    PARS_CUDA(cudaStreamSynchronize(svc->copy_stream));
   });
 }
 
 int32_t pars_gpu_service_result_ftle(pars_gpu_service* svc, int64_t ticket, float* values)
 {
   return service_guard(svc, [&] {
-    std::lock_guard<std::mutex> lock(svc->mutex);
-    auto r = find_request(svc, ticket);
-    if (r->state != done) throw error(PARS_ERR_STATE, "request has not finished");
     PARS_REQUIRE(values, "values is required");
-    if (!r->ftle_values.empty()) std::memcpy(values, r->ftle_values.data(), sizeof(float) * r->ftle_values.size());
+    std::shared_ptr<request> r;
+    {
+      std::lock_guard<std::mutex> lock(svc->mutex);
+      r = find_request(svc, ticket);
+      if (r->state != done) throw error(PARS_ERR_STATE, "request has not finished");
+    }
+    std::lock_guard<std::mutex> lock(r->result_mutex);
+    if (r->released) throw error(PARS_ERR_NOT_FOUND, "request was released");
+    PARS_REQUIRE(r->kind == ftle, "not an FTLE request");
+    PARS_CUDA(cudaSetDevice(svc->device));
+    copy_result(*svc, *r, 0, values, r->result_bytes);
+    PARS_CUDA(cudaStreamSynchronize(svc->copy_stream));
   });
 }
 
 int32_t pars_gpu_service_release(pars_gpu_service* svc, int64_t ticket)
 {
   return service_guard(svc, [&] {
-    std::lock_guard<std::mutex> lock(svc->mutex);
-    auto r = find_request(svc, ticket);
-    if (r->state == running) throw error(PARS_ERR_STATE, "request is running");
-    if (r->state == queued)
+    std::shared_ptr<request> r;
     {
-      svc->queue.erase(std::remove(svc->queue.begin(), svc->queue.end(), r), svc->queue.end());
-      r->status = PARS_ERR_CANCELLED;
+      std::lock_guard<std::mutex> lock(svc->mutex);
+      r = find_request(svc, ticket);
+      if (r->state == running) throw error(PARS_ERR_STATE, "request is running");
+      if (r->state == queued)
+      {
+        svc->queue.erase(std::remove(svc->queue.begin(), svc->queue.end(), r), svc->queue.end());
+        r->status = PARS_ERR_CANCELLED;
+      }
+      svc->requests.erase(ticket);
     }
-    svc->requests.erase(ticket);
+    std::size_t freed = 0;
+    {
+      std::lock_guard<std::mutex> lock(r->result_mutex);
+      r->released = true;
+      if (r->result)
+      {
+        PARS_CUDA(cudaSetDevice(svc->device));
+        free_result(*r, svc->copy_stream);
+        freed = r->result_bytes;
+      }
+      std::vector<char>().swap(r->spilled);
+    }
+    if (freed)
+    {
+      {
+        std::lock_guard<std::mutex> lock(svc->mutex);
+        svc->held -= std::min(svc->held, freed);
+        svc->in_use -= std::min(svc->in_use, freed);
+      }
+      svc->work.notify_all();
+    }
   });
 }
 

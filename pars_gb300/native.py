@@ -235,6 +235,13 @@ class Context:
                    _ptr(field.spacing), ctypes.byref(h))
         return h.value
 
+    def upload_field_host(self, host_xyz_ptr, dims, offset, size, spacing):
+        """pars_gpu_field_upload from a host address (e.g. a pinned buffer)."""
+        h = _I32()
+        d, o, s, sp = _i3(dims), _f3(offset), _f3(size), _f3(spacing)
+        self._call("pars_gpu_field_upload", host_xyz_ptr, _ptr(d), _ptr(o), _ptr(s), _ptr(sp), ctypes.byref(h))
+        return h.value
+
     def upload_field_device(self, device_xyz_ptr, dims, offset, size, spacing):
         h = _I32()
         d, o, s, sp = _i3(dims), _f3(offset), _f3(size), _f3(spacing)
@@ -497,6 +504,26 @@ class Service:
         out = np.zeros(shape, np.float32)
         self._check(self.lib.pars_gpu_service_result_ftle(self.handle, ticket, _ptr(out)), "pars_gpu_service_result_ftle")
         return out
+
+    def batch_counts(self, ticket, batch):
+        """(vertices, indices) of one streamline batch."""
+        nv, ni = _I64(), _I64()
+        self._check(self.lib.pars_gpu_service_result_batch(self.handle, ticket, batch, ctypes.byref(nv), ctypes.byref(ni),
+                                                           None, None, None), "pars_gpu_service_result_batch")
+        return nv.value, ni.value
+
+    def batch_into(self, ticket, batch, vertices_ptr, colors_ptr, indices_ptr):
+        """Copies one streamline batch to host addresses (e.g. pinned
+        buffers); returns (vertices, indices)."""
+        nv, ni = _I64(), _I64()
+        self._check(self.lib.pars_gpu_service_result_batch(self.handle, ticket, batch, ctypes.byref(nv), ctypes.byref(ni),
+                                                           vertices_ptr, colors_ptr, indices_ptr),
+                    "pars_gpu_service_result_batch")
+        return nv.value, ni.value
+
+    def ftle_into(self, ticket, values_ptr):
+        """Copies an FTLE result to a host address."""
+        self._check(self.lib.pars_gpu_service_result_ftle(self.handle, ticket, values_ptr), "pars_gpu_service_result_ftle")
 
     def release(self, ticket):
         self._check(self.lib.pars_gpu_service_release(self.handle, ticket), "pars_gpu_service_release")

@@ -131,3 +131,43 @@ def test_unknown_dataset_and_oversized_requests_are_rejected(service):
                                         "seed_generation_iterations": 2_000_000, "particle_tracing_integrator": "runge_kutta_4",
                                         "particle_tracing_step_size": 0.01}))
     assert e.value.status == -6
+
+
+def test_held_results_move_to_host_when_they_block_the_queue(service):
+    """With a budget that holds only a few requests' results, requests that are
+    submitted together and collected only at the end all finish (the held
+    results move to host memory) and give the same buffers."""
+    from pars_gb300 import native, workloads as W
+    from pars_gb300.requests import encode_settings
+    req = {"mode": "streamlines", "dataset_filepath": "abc40", "seed_generation_stride": [3, 3, 3],
+           "seed_generation_iterations": 302, "particle_tracing_integrator": "runge_kutta_4",
+           "particle_tracing_step_size": 0.01, "color_generation_mode": "rgb"}
+    t = service.submit(encode_settings(req))
+    assert service.wait(t) == 2
+    expected = service.streamlines(t)
+    service.release(t)
+    small = native.Service(0, budget_bytes=200 << 20, lanes=2, max_batch=4)
+    try:
+        small.add_dataset("abc40", W.abc_field(40, noise_sigma=0.01, seed=4))
+        tickets = [small.submit(encode_settings(req)) for _ in range(12)]
+        for t in tickets:
+            assert small.wait(t, timeout_ms=120_000) == 2
+        for t in tickets:
+            assert _same(small.streamlines(t), expected, "streamlines")
+            small.release(t)
+    finally:
+        small.close()
+
+
+def test_released_results_are_gone(service):
+    from pars_gb300 import native
+    from pars_gb300.requests import encode_settings
+    t = service.submit(encode_settings({"mode": "ftle", "dataset_filepath": "abc28", "seed_generation_stride": [2, 2, 2],
+                                        "seed_generation_iterations": 21, "particle_tracing_integrator": "runge_kutta_4",
+                                        "particle_tracing_step_size": 0.01}))
+    assert service.wait(t) == 2
+    assert np.isfinite(service.ftle(t)).any()
+    service.release(t)
+    with pytest.raises(native.ParsGpuError) as e:
+        service.ftle(t)
+    assert e.value.status == -5
