@@ -47,6 +47,8 @@ def parse_args():
     p.add_argument("--iterations", type=int, default=501)
     p.add_argument("--cpu-sample", type=int, default=1048576, help="seeds in the CPU baseline's bounded sample")
     p.add_argument("--requests", type=int, default=300, help="served workload: number of requests")
+    p.add_argument("--serve-arms", default="plain,batched", help="served workload: arms to run (plain, batched)")
+    p.add_argument("--serve-loads", default="0.5,0.9", help="served workload: offered loads as fractions of saturation")
     p.add_argument("--workload", choices=["ftle", "streamlines", "domain", "pathlines", "serve"], default="ftle",
                    help="ftle: the headline line; the others print one line for the other workloads")
     return p.parse_args()
@@ -456,38 +458,45 @@ def run_serve(args):
         out = {"saturation_requests_per_s": saturation, "saturation_particle_steps_per_s": steps / span,
                "saturation_p50_ms": float(np.percentile(lat, 50)), "saturation_p99_ms": float(np.percentile(lat, 99)),
                "result_bytes_to_host": collected["bytes"], "saturation_breakdown": dict(breakdown)}
-        for load in (0.5, 0.9):
+        for load in loads:
             span, lat, _ = run(target, load * saturation)
             out[f"load{int(load * 100)}"] = {"offered_requests_per_s": load * saturation,
                                              "achieved_requests_per_s": len(messages) / span,
                                              "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
         return out
 
+    arms = args.serve_arms.split(",")
+    loads = [float(x) for x in args.serve_loads.split(",") if x]
     results = {}
-    ctx = native.Context(0)
-    for k in range(8):                               # warm-up (autotuning, allocations)
-        plain_request(ctx, k)
-    results["plain"] = summarise(run_plain, ctx)
-    ctx.close()
+    if "plain" in arms:
+        ctx = native.Context(0)
+        for k in range(8):                           # warm-up (autotuning, allocations)
+            plain_request(ctx, k)
+        results["plain"] = summarise(run_plain, ctx)
+        ctx.close()
 
-    svc = native.Service(0, budget_bytes=160 << 30, lanes=2, max_batch=64)
-    for d, (xyz, offset, size, spacing) in zip(ds, device_fields):
-        svc.add_dataset_device(d["name"], xyz.data_ptr(), (d["edge"],) * 3, offset, size, spacing)
-    torch.cuda.synchronize()
-    del device_fields
-    torch.cuda.empty_cache()
-    for m in messages[:8]:                           # warm-up
-        t = svc.submit(m)
-        svc.wait(t)
-        collect(svc, t)
-    results["batched"] = summarise(run_service, svc)
-    svc.close()
-    print(json.dumps({"workload": f"served_{len(messages)}: {len(messages)} requests (seed 4), 70% streamlines / 30% FTLE on "
-                                  f"{len(ds)} ABC / double-gyre fields (edge 64-512), seeds 1k-2M (streamlines <= 16384), "
-                                  "200-2000 RK4 steps, Poisson arrivals; results collected into pinned host buffers",
-                      "datasets": ds, "plain": results["plain"], "batched": results["batched"],
-                      "throughput_ratio_at_saturation": results["batched"]["saturation_requests_per_s"] /
-                                                        results["plain"]["saturation_requests_per_s"]}))
+    if "batched" in arms:
+        svc = native.Service(0, budget_bytes=160 << 30, lanes=2, max_batch=64)
+        for d, (xyz, offset, size, spacing) in zip(ds, device_fields):
+            svc.add_dataset_device(d["name"], xyz.data_ptr(), (d["edge"],) * 3, offset, size, spacing)
+        torch.cuda.synchronize()
+        del device_fields
+        torch.cuda.empty_cache()
+        for m in messages[:8]:                       # warm-up
+            t = svc.submit(m)
+            svc.wait(t)
+            collect(svc, t)
+        results["batched"] = summarise(run_service, svc)
+        svc.close()
+    line = {"workload": f"served_{len(messages)}: {len(messages)} requests (seed 4), 70% streamlines / 30% FTLE on "
+                        f"{len(ds)} ABC / double-gyre fields (edge 64-512), seeds 1k-2M (streamlines <= 16384), "
+                        "200-2000 RK4 steps, Poisson arrivals; results collected into pinned host buffers",
+            "datasets": ds}
+    line.update(results)
+    if "plain" in results and "batched" in results:
+        line["throughput_ratio_at_saturation"] = (results["batched"]["saturation_requests_per_s"] /
+                                                  results["plain"]["saturation_requests_per_s"])
+    print(json.dumps(line))
 
 
 def main():

@@ -171,7 +171,8 @@ struct pars_gpu_context
   pars::device_buffer                     particles_in, particles_next, slots, kept, written, offsets, block_of,
                                           block_of_next, exits, exit_keys, exit_keys_sorted, exit_order,
                                           exit_order_sorted, counters, block_max, cub_temp, scan_input, tile_counts,
-                                          tile_offsets, staging, boundary_positions, boundary_offsets, single_block;
+                                          tile_offsets, staging, boundary_positions, boundary_offsets, single_block,
+                                          slot_layouts;
   pars::device_buffer                     ftle;
   long long                               ftle_count = 0;
   // Released field buffers kept for reuse (bytes -> buffer), so that a caller
@@ -228,13 +229,22 @@ void launch_field_sample(pars_gpu_context& ctx, const field_view& f, const float
 void launch_seed_generate(pars_gpu_context& ctx, const float offset[3], const float stride[3], const int per_dimension[3],
                           int iterations, int rank, pars_particle* out);
 
+// Where a block's particles keep their vertex slots: particle i (of this
+// block) owns slots [origin + i * stride, origin + (i + 1) * stride), stride =
+// the block's largest remaining_iterations (the reference's per-curve layout,
+// particle_tracer.cpp:235-252, with each block padded to its own maximum).
+struct slot_layout
+{
+  long long origin, stride;
+};
+
 struct trace_launch
 {
   const trace_block*   blocks;
   const pars_particle* particles;
   const int*           block_of;      // nullptr: every particle is in block 0
   long long            count;
-  long long            slot_stride;
+  const slot_layout*   block_slots;   // per block (device)
   float4*              slots;
   int*                 written;
   int*                 kept;
@@ -247,7 +257,8 @@ struct trace_launch
   unsigned long long*  steps;
 };
 void launch_trace(pars_gpu_context& ctx, const trace_launch& a);
-void launch_compact_vertices(pars_gpu_context& ctx, const float4* slots, long long slot_stride, const int* written,
+void launch_compact_vertices(pars_gpu_context& ctx, const float4* slots, const slot_layout* block_slots, const int* block_of,
+                             const int* written,
                              const long long* offsets, long long count, float4* out);
 // Exclusive sum of `count` int32 into int64 offsets; offsets[count] = total.
 void exclusive_sum(pars_gpu_context& ctx, const int* in, long long* out, long long count);

@@ -26,7 +26,7 @@ void for_each_scratch(context_type& c, visit_type&& visit)
                   &c.exit_order_sorted, &c.counters, &c.block_max, &c.cub_temp, &c.scan_input, &c.tile_counts,
                   &c.tile_offsets, &c.staging, &c.ftle, &c.curves.vertices, &c.curves.colors,
                   &c.curves.indices, &c.boundary_positions, &c.boundary_offsets, &c.batch_jobs,
-                  &c.batch_counters, &c.single_block})
+                  &c.batch_counters, &c.single_block, &c.slot_layouts})
     visit(*b);
 }
 }
@@ -298,9 +298,23 @@ void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, c
   int round = 0;
   while (count > 0)
   {
-    int stride = 1;
-    for (int b = 0; b < nblocks; ++b) if (block_count[b] > 0) stride = std::max(stride, block_max[b]);
-    ctx.slots.reserve(sizeof(float4) * (std::size_t)count * stride);
+    // The round's particles are grouped by block in block order (seeds per
+    // rank; exits sorted by destination block), so each block's slots follow
+    // the previous block's.
+    std::vector<slot_layout> layout(nblocks);
+    long long total_slots = 0, first_particle = 0;
+    for (int b = 0; b < nblocks; ++b)
+    {
+      const long long stride = std::max(1, block_max[b]);
+      layout[b].origin = total_slots - first_particle * stride;
+      layout[b].stride = stride;
+      total_slots += block_count[b] * stride;
+      first_particle += block_count[b];
+    }
+    PARS_REQUIRE(first_particle == count, "block particle counts do not add up to the particle count");
+    ctx.slots.reserve(sizeof(float4) * (std::size_t)total_slots);
+    ctx.slot_layouts.reserve(sizeof(slot_layout) * nblocks);
+    PARS_CUDA(cudaMemcpyAsync(ctx.slot_layouts.get(), layout.data(), sizeof(slot_layout) * nblocks, cudaMemcpyHostToDevice, ctx.stream));
     ctx.written.reserve(sizeof(int) * count);
     ctx.kept.reserve(sizeof(int) * count);
     ctx.offsets.reserve(sizeof(long long) * (count + 1));
@@ -316,7 +330,7 @@ void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, c
     a.particles = ctx.particles_in.as<const pars_particle>();
     a.block_of = nblocks > 1 ? ctx.block_of.as<const int>() : nullptr;
     a.count = count;
-    a.slot_stride = stride;
+    a.block_slots = ctx.slot_layouts.as<const slot_layout>();
     a.slots = ctx.slots.as<float4>();
     a.written = ctx.written.as<int>();
     a.kept = ctx.kept.as<int>();
@@ -365,8 +379,9 @@ void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, c
     const long long round_vertices = boundary.back();
 
     grow_curves(ctx, curves.vertex_total + round_vertices);
-    launch_compact_vertices(ctx, ctx.slots.as<const float4>(), stride, ctx.written.as<const int>(), ctx.offsets.as<const long long>(),
-                            count, curves.vertices.as<float4>() + curves.vertex_total);
+    launch_compact_vertices(ctx, ctx.slots.as<const float4>(), ctx.slot_layouts.as<const slot_layout>(), a.block_of,
+                            ctx.written.as<const int>(), ctx.offsets.as<const long long>(), count,
+                            curves.vertices.as<float4>() + curves.vertex_total);
     for (std::size_t k = 0; k < pending.size(); ++k)
     {
       curves_batch batch;

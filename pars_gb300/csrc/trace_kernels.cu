@@ -36,7 +36,8 @@ __global__ void __launch_bounds__(256) trace_kernel(const trace_launch a)
     const float4* record = reinterpret_cast<const float4*>(a.particles + i);
     float4 last = record[0];
     const int N = __float_as_int(record[1].x);   // remaining_iterations
-    float4* out = a.slots + i * a.slot_stride;
+    const slot_layout L = a.block_slots[block];
+    float4* out = a.slots + L.origin + i * L.stride;
     out[0] = last;
     int written = 1;
     int kept = is_invalid_vertex(last) ? 0 : 1;
@@ -116,16 +117,18 @@ __global__ void __launch_bounds__(256) trace_kernel(const trace_launch a)
 
 // One warp per particle: copy its written slots, minus invalid vertices, to
 // the packed output at its offset.
-__global__ void __launch_bounds__(256) compact_kernel(const float4* __restrict__ slots, long long slot_stride,
-                                                      const int* __restrict__ written, const long long* __restrict__ offsets,
-                                                      long long count, float4* __restrict__ out)
+__global__ void __launch_bounds__(256) compact_kernel(const float4* __restrict__ slots, const slot_layout* __restrict__ block_slots,
+                                                      const int* __restrict__ block_of, const int* __restrict__ written,
+                                                      const long long* __restrict__ offsets, long long count,
+                                                      float4* __restrict__ out)
 {
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= count) return;
   const int n = written[warp];
   long long dst = offsets[warp];
-  const float4* src = slots + warp * slot_stride;
+  const slot_layout L = block_slots[block_of ? block_of[warp] : 0];
+  const float4* src = slots + L.origin + warp * L.stride;
   for (int j0 = 0; j0 < n; j0 += 32)
   {
     const int j = j0 + lane;
@@ -213,12 +216,12 @@ void launch_trace(pars_gpu_context& ctx, const trace_launch& a)
   else               trace_kernel<false><<<grid_for(a.count, threads), threads, 0, ctx.stream>>>(a);
 }
 
-void launch_compact_vertices(pars_gpu_context& ctx, const float4* slots, long long slot_stride, const int* written,
-                             const long long* offsets, long long count, float4* out)
+void launch_compact_vertices(pars_gpu_context& ctx, const float4* slots, const slot_layout* block_slots, const int* block_of,
+                             const int* written, const long long* offsets, long long count, float4* out)
 {
   if (count <= 0) return;
   launch_scope scope(ctx, "prune_compact");
-  compact_kernel<<<grid_for(count * 32, 256), 256, 0, ctx.stream>>>(slots, slot_stride, written, offsets, count, out);
+  compact_kernel<<<grid_for(count * 32, 256), 256, 0, ctx.stream>>>(slots, block_slots, block_of, written, offsets, count, out);
 }
 
 void exclusive_sum(pars_gpu_context& ctx, const int* in, long long* out, long long count)
