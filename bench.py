@@ -54,6 +54,20 @@ def parse_args():
     return p.parse_args()
 
 
+def combine_ranks(dist, elapsed, steps, device):
+    """Whole-job figures of N independent replicas: the slowest rank's time
+    (max over ranks) and the steps all ranks took (sum).  dist is
+    torch.distributed (or None for one process)."""
+    if dist is None:
+        return float(elapsed), float(steps)
+    import torch
+    t = torch.tensor([float(elapsed)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    s = torch.tensor([float(steps)], device=device, dtype=torch.float64)
+    dist.all_reduce(s)
+    return float(t.item()), float(s.item())
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -514,7 +528,8 @@ def main():
                           f"({seeds} particles), classical RK4 (4 samples/step) h=0.01, <= {max_steps} steps (T=5), "
                           "flow map + fused central-difference / Cauchy-Green / FP64 eigenvalue / log FTLE",
               "grid": n, "seeds": seeds, "max_steps": max_steps, "step_size": 0.01, "stage_mode": "resampled",
-              "ranks": world, "l2": "inputs larger than L2 (268 MB float4 field) and a 256 MB L2 flush before every step"}
+              "ranks": world, "l2": f"inputs larger than L2 ({16 * n ** 3 / 1e6:.0f} MB float4 field) and a 256 MB L2 flush "
+                                    "before every step"}
 
     if args.impl == "reference":
         if rank != 0:
@@ -582,16 +597,7 @@ def main():
     advect_ms, advect_n = ctx.profile_get("batch_advect")
     ftle_ms, ftle_n = ctx.profile_get("ftle_fused")
 
-    if dist:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-        s = torch.tensor([float(total_steps)], device="cuda", dtype=torch.float64)
-        dist.all_reduce(s)
-        total_steps_all = float(s.item())
-    else:
-        total_steps_all = float(total_steps)
-
+    elapsed_ms, total_steps_all = combine_ranks(dist, elapsed_ms, total_steps, "cuda")
     value = total_steps_all / (elapsed_ms * 1e-3)
     ftle_voxels_per_s = world * seeds * args.steps / (elapsed_ms * 1e-3)
     steps_per_launch = total_steps / args.steps
@@ -635,11 +641,8 @@ def main():
         e2e_steps += e2e_step()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * e2e_steps / e2e_s
+    e2e_s, e2e_steps_all = combine_ranks(dist, e2e_s, e2e_steps, "cuda")
+    e2e_value = e2e_steps_all / e2e_s
 
     cpu = None
     if rank == 0 and world == 1:

@@ -472,30 +472,49 @@ __device__ __forceinline__ void scale_cache(cell_cache& k, float sx, float sy, f
   scale3(k.e, sx, sy, sz); scale3(k.f, sx, sy, sz); scale3(k.g, sx, sy, sz); scale3(k.h, sx, sy, sz);
 }
 
-// Velocity (cells per unit time) at cell (cx, cy, cz) + (ux, uy, uz); the
-// offset may lie outside [0, 1) (a stage point that left the cell) and the
-// cell outside the grid (clamped, weight 0 or 1).
-__device__ __forceinline__ float3 sample_local(const field_view& f, cell_cache& k, int cx, int cy, int cz, float ux, float uy, float uz)
+// Whether an offset lies in [0, 1): the bit patterns of the floats in [0, 1)
+// are exactly the unsigned values below that of 1.0f (negative values, -0,
+// infinities and NaNs all compare above), so one unsigned compare per axis —
+// or one for the largest of three — does the two-sided test.
+__device__ __forceinline__ bool in_unit(float u) { return __float_as_uint(u) < 0x3f800000u; }
+__device__ __forceinline__ bool in_unit_cube(float ux, float uy, float uz)
 {
-  int ix = cx, iy = cy, iz = cz;
-  float wx = ux, wy = uy, wz = uz;
-  if (!(ux >= 0.0f && ux < 1.0f && uy >= 0.0f && uy < 1.0f && uz >= 0.0f && uz < 1.0f))
-  {
-    const float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
-    ix += int(fx); iy += int(fy); iz += int(fz);
-    wx = ux - fx; wy = uy - fy; wz = uz - fz;
-  }
-  if (ix < 0) { ix = 0; wx = 0.0f; } else if (ix > f.nx - 2) { ix = f.nx - 2; wx = 1.0f; }
-  if (iy < 0) { iy = 0; wy = 0.0f; } else if (iy > f.ny - 2) { iy = f.ny - 2; wy = 1.0f; }
-  if (iz < 0) { iz = 0; wz = 0.0f; } else if (iz > f.nz - 2) { iz = f.nz - 2; wz = 1.0f; }
-  if (ix != k.ix || iy != k.iy || iz != k.iz)
-  {
-    cache_load(f, k, ix, iy, iz);
-    scale_cache(k, f.inv_hx, f.inv_hy, f.inv_hz);
-  }
+  return max(max(__float_as_uint(ux), __float_as_uint(uy)), __float_as_uint(uz)) < 0x3f800000u;
+}
+
+__device__ __forceinline__ float3 local_eval(const cell_cache& k, float wx, float wy, float wz)
+{
   return make_float3(cache_eval1(k.a.x, k.b.x, k.c.x, k.d.x, k.e.x, k.f.x, k.g.x, k.h.x, wx, wy, wz),
                      cache_eval1(k.a.y, k.b.y, k.c.y, k.d.y, k.e.y, k.f.y, k.g.y, k.h.y, wx, wy, wz),
                      cache_eval1(k.a.z, k.b.z, k.c.z, k.d.z, k.e.z, k.f.z, k.g.z, k.h.z, wx, wy, wz));
+}
+
+// The cell's polynomial from its eight corners, scaled to cells per unit time.
+__device__ __forceinline__ void local_cache_load(const field_view& f, cell_cache& k, int ix, int iy, int iz)
+{
+  cache_load(f, k, ix, iy, iz);
+  scale_cache(k, f.inv_hx, f.inv_hy, f.inv_hz);
+}
+
+// Velocity (cells per unit time) at cell (cx, cy, cz) + (ux, uy, uz), where
+// (cx, cy, cz) is the particle's own cell (inside the grid).  The offset may
+// lie outside [0, 1) (a stage point that left the cell); the cell it falls in
+// is then clamped to the grid (weight 0 or 1).
+__device__ __forceinline__ float3 sample_local(const field_view& f, cell_cache& k, int cx, int cy, int cz, float ux, float uy, float uz)
+{
+  if (in_unit_cube(ux, uy, uz))
+  {
+    if (cx != k.ix || cy != k.iy || cz != k.iz) local_cache_load(f, k, cx, cy, cz);
+    return local_eval(k, ux, uy, uz);
+  }
+  const float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
+  int ix = cx + int(fx), iy = cy + int(fy), iz = cz + int(fz);
+  float wx = ux - fx, wy = uy - fy, wz = uz - fz;
+  if (ix < 0) { ix = 0; wx = 0.0f; } else if (ix > f.nx - 2) { ix = f.nx - 2; wx = 1.0f; }
+  if (iy < 0) { iy = 0; wy = 0.0f; } else if (iy > f.ny - 2) { iy = f.ny - 2; wy = 1.0f; }
+  if (iz < 0) { iz = 0; wz = 0.0f; } else if (iz > f.nz - 2) { iz = f.nz - 2; wz = 1.0f; }
+  if (ix != k.ix || iy != k.iy || iz != k.iz) local_cache_load(f, k, ix, iy, iz);
+  return local_eval(k, wx, wy, wz);
 }
 
 // Moves the offset back into [0, 1) and the cell accordingly.  For an offset
@@ -504,9 +523,9 @@ __device__ __forceinline__ float3 sample_local(const field_view& f, cell_cache& 
 // of the next cell).
 __device__ __forceinline__ void renormalize(local_position& p)
 {
-  if (!(p.ux >= 0.0f && p.ux < 1.0f)) { const float fl = floorf(p.ux); p.ix += int(fl); p.ux -= fl; }
-  if (!(p.uy >= 0.0f && p.uy < 1.0f)) { const float fl = floorf(p.uy); p.iy += int(fl); p.uy -= fl; }
-  if (!(p.uz >= 0.0f && p.uz < 1.0f)) { const float fl = floorf(p.uz); p.iz += int(fl); p.uz -= fl; }
+  if (!in_unit(p.ux)) { const float fl = floorf(p.ux); p.ix += int(fl); p.ux -= fl; }
+  if (!in_unit(p.uy)) { const float fl = floorf(p.uy); p.iy += int(fl); p.uy -= fl; }
+  if (!in_unit(p.uz)) { const float fl = floorf(p.uz); p.iz += int(fl); p.uz -= fl; }
 }
 
 __device__ __forceinline__ local_position to_local(const field_view& f, const float4& p)
@@ -530,7 +549,8 @@ __device__ __forceinline__ float4 to_absolute(const field_view& f, const local_p
 
 __device__ __forceinline__ bool local_inside(const field_view& f, const local_position& q)
 {
-  return q.ix >= 0 && q.ix <= f.nx - 2 && q.iy >= 0 && q.iy <= f.ny - 2 && q.iz >= 0 && q.iz <= f.nz - 2;
+  // 0 <= i < n - 1 as one unsigned compare per axis (false for every i when n = 1)
+  return unsigned(q.ix) < unsigned(f.nx - 1) && unsigned(q.iy) < unsigned(f.ny - 1) && unsigned(q.iz) < unsigned(f.nz - 1);
 }
 
 // |v_i| <= 1e-5 with v in cells per unit time: |v_i| <= 1e-5 / h_i.

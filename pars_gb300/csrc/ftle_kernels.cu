@@ -9,7 +9,8 @@
 // FTLE: per voxel, the flow map's central-difference gradient J (FP32, one-sided
 //   at the borders), the Cauchy-Green tensor C = J^T J and its largest
 //   eigenvalue in FP64 by the trigonometric closed form (O. K. Smith, CACM 4(4),
-//   1961), then log(sqrt(lambda)) / |T| in FP64, stored as FP32 — the intent of
+//   1961; its cosine refined by Newton steps, see largest_eigenvalue), then
+//   log(sqrt(lambda)) / |T| = 0.5 log(lambda) / |T| in FP64, stored as FP32 — the intent of
 //   vector_field::gradient + ftle_map_generator::generate
 //   (vector_field.cpp:49-93, ftle_map_generator.cpp:22-60).
 #include "context.hpp"
@@ -101,6 +102,46 @@ __device__ void symmetric_eigenvalues(double a00, double a01, double a02, double
   out[1] = 3.0 * q - out[0] - out[2];
 }
 
+// Largest eigenvalue of a symmetric 3x3 matrix in FP64 (the trigonometric
+// form above, lambda = q + 2 p cos(acos(r) / 3)), with c = cos(acos(r) / 3)
+// found as the largest root of 4 c^3 - 3 c = r (cos 3t = 4 cos^3 t - 3 cos t)
+// in [1/2, 1]: an FP32 start from acosf / cosf, then Newton steps on the
+// cubic in FP64 whose derivative 12 c^2 - 3 is inverted in FP32 (each step
+// multiplies the error by about the FP32 relative error of that reciprocal,
+// plus the quadratic term), which is far cheaper than FP64 acos and cos.  Near
+// the double root c = 1/2 (r -> -1: the two largest eigenvalues meet) the
+// derivative vanishes, and the FP64 trigonometric evaluation is used instead.
+__device__ __forceinline__ double largest_eigenvalue(double a00, double a01, double a02, double a11, double a12, double a22)
+{
+  const double p1 = a01 * a01 + a02 * a02 + a12 * a12;
+  if (p1 == 0.0) return fmax(a00, fmax(a11, a22));
+  const double q  = (a00 + a11 + a22) * (1.0 / 3.0);
+  const double d0 = a00 - q, d1 = a11 - q, d2 = a22 - q;
+  const double s  = (d0 * d0 + d1 * d1 + d2 * d2 + 2.0 * p1) * (1.0 / 6.0);
+  const double inv = rsqrt(s);   // 1 / p
+  const double p  = s * inv;
+  const double b00 = d0 * inv, b11 = d1 * inv, b22 = d2 * inv, b01 = a01 * inv, b02 = a02 * inv, b12 = a12 * inv;
+  const double det = b00 * (b11 * b22 - b12 * b12) - b01 * (b01 * b22 - b12 * b02) + b02 * (b01 * b12 - b11 * b02);
+  double r = 0.5 * det;
+  r = r < -1.0 ? -1.0 : (r > 1.0 ? 1.0 : r);
+  const float cf = cosf(acosf(float(r)) * (1.0f / 3.0f));
+  double c;
+  if (cf > 0.52f)
+  {
+    c = cf;
+    #pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+      const double f = fma(4.0 * c, c * c, fma(-3.0, c, -r));   // 4 c^3 - 3 c - r
+      const float slope = fmaf(12.0f * float(c), float(c), -3.0f);
+      c = fma(-f, double(__frcp_rn(slope)), c);
+    }
+  }
+  else
+    c = cos(acos(r) * (1.0 / 3.0));
+  return fma(2.0 * p, c, q);
+}
+
 struct ftle_args
 {
   const float4* flow;
@@ -111,6 +152,7 @@ struct ftle_args
   float*        out;
 };
 
+template <int MODE>
 __global__ void __launch_bounds__(256) ftle_kernel(const ftle_args a)
 {
   const long long total = (long long)a.nx * a.ny * a.nz;
@@ -148,18 +190,28 @@ __global__ void __launch_bounds__(256) ftle_kernel(const ftle_args a)
     #pragma unroll
     for (int c = r; c < 3; ++c)
       C[r][c] = double(J[0][r]) * double(J[0][c]) + double(J[1][r]) * double(J[1][c]) + double(J[2][r]) * double(J[2][c]);
-  double lambda[3];
-  symmetric_eigenvalues(C[0][0], C[0][1], C[0][2], C[1][1], C[1][2], C[2][2], lambda);
   double value;
-  if (a.mode == PARS_FTLE_REGULAR)
-    value = log(sqrt(lambda[0])) * a.inverse_time;
+  if constexpr (MODE == PARS_FTLE_REGULAR)
+  {
+    // log(sqrt(lambda_max)) / |T|
+    const double lambda = largest_eigenvalue(C[0][0], C[0][1], C[0][2], C[1][1], C[1][2], C[2][2]);
+    value = 0.5 * log(lambda) * a.inverse_time;
+  }
   else
   {
+    double lambda[3];
+    symmetric_eigenvalues(C[0][0], C[0][1], C[0][2], C[1][1], C[1][2], C[2][2], lambda);
     const double d01 = lambda[0] - lambda[1], d12 = lambda[1] - lambda[2], d20 = lambda[2] - lambda[0];
     value = sqrt(0.5) * sqrt(d01 * d01 + d12 * d12 + d20 * d20) /
             sqrt(lambda[0] * lambda[0] + lambda[1] * lambda[1] + lambda[2] * lambda[2]);
   }
   a.out[i] = float(value);
+}
+
+void launch_ftle_kernel(const ftle_args& a, unsigned grid, cudaStream_t stream)
+{
+  if (a.mode == PARS_FTLE_REGULAR) ftle_kernel<PARS_FTLE_REGULAR><<<grid, 256, 0, stream>>>(a);
+  else                             ftle_kernel<PARS_FTLE_FRACTIONAL_ANISOTROPY><<<grid, 256, 0, stream>>>(a);
 }
 }
 
@@ -192,7 +244,7 @@ void launch_ftle(pars_gpu_context& ctx, const field_view& flow, double time, int
   const long long total = (long long)a.nx * a.ny * a.nz;
   if (total <= 0) return;
   launch_scope scope(ctx, "ftle_fused");
-  ftle_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx.stream>>>(a);
+  launch_ftle_kernel(a, (unsigned)((total + 255) / 256), ctx.stream);
 }
 
 // ---- Allocation-free FTLE ------------------------------------------------------
@@ -309,7 +361,7 @@ extern "C" int32_t pars_gpu_ftle_no_alloc(const float* device_xyz, const int32_t
   t.inverse_time = 1.0 / fabs(double(time));
   t.mode = mode;
   t.out = device_ftle;
-  ftle_kernel<<<(unsigned)((voxels + 255) / 256), 256, 0, s>>>(t);
+  launch_ftle_kernel(t, (unsigned)((voxels + 255) / 256), s);
   if (device_steps) steps_to_int64_kernel<<<1, 1, 0, s>>>(counter, device_steps);
   if (cudaGetLastError() != cudaSuccess) return PARS_ERR_CUDA;
   return PARS_OK;

@@ -485,6 +485,25 @@ std::shared_ptr<request> find_request(pars_gpu_service* svc, int64_t ticket)
   return it->second;
 }
 
+// A field uploaded into the owner context becomes a dataset.
+void register_dataset(pars_gpu_service* svc, const char* name, int32_t handle)
+{
+  PARS_CUDA(cudaSetDevice(svc->device));
+  dataset d;
+  d.name = name;
+  d.field = handle;
+  {
+    std::lock_guard<std::mutex> owner_lock(svc->owner->mutex);
+    auto& f = *svc->owner->fields.at(handle);
+    d.view = f.view();
+    for (int i = 0; i < 3; ++i) { d.shape[i] = f.shape[i]; d.offset[i] = f.offset[i]; d.size[i] = f.size[i]; d.spacing[i] = f.spacing[i]; }
+    PARS_CUDA(cudaStreamSynchronize(svc->owner->stream));
+  }
+  std::lock_guard<std::mutex> lock(svc->mutex);
+  svc->dataset_index[d.name] = int(svc->datasets.size());
+  svc->datasets.push_back(d);
+}
+
 template <typename body_type>
 int32_t service_guard(pars_gpu_service* svc, body_type&& body)
 {
@@ -605,17 +624,7 @@ int32_t pars_gpu_service_add_dataset(pars_gpu_service* svc, const char* name, co
     int32_t handle = -1;
     const int32_t status = pars_gpu_field_upload(svc->owner, xyz, shape, offset, size, spacing, &handle);
     if (status != PARS_OK) throw error(status, pars_gpu_last_error(svc->owner));
-    PARS_CUDA(cudaSetDevice(svc->device));
-    pars_gpu_synchronize(svc->owner);
-    dataset d;
-    d.name = name;
-    d.field = handle;
-    auto& f = *svc->owner->fields.at(handle);
-    d.view = f.view();
-    for (int i = 0; i < 3; ++i) { d.shape[i] = f.shape[i]; d.offset[i] = f.offset[i]; d.size[i] = f.size[i]; d.spacing[i] = f.spacing[i]; }
-    std::lock_guard<std::mutex> lock(svc->mutex);
-    svc->dataset_index[d.name] = int(svc->datasets.size());
-    svc->datasets.push_back(d);
+    register_dataset(svc, name, handle);
   });
 }
 
@@ -627,16 +636,7 @@ int32_t pars_gpu_service_add_dataset_device(pars_gpu_service* svc, const char* n
     int32_t handle = -1;
     const int32_t status = pars_gpu_field_upload_device(svc->owner, device_xyz, shape, offset, size, spacing, &handle);
     if (status != PARS_OK) throw error(status, pars_gpu_last_error(svc->owner));
-    pars_gpu_synchronize(svc->owner);
-    dataset d;
-    d.name = name;
-    d.field = handle;
-    auto& f = *svc->owner->fields.at(handle);
-    d.view = f.view();
-    for (int i = 0; i < 3; ++i) { d.shape[i] = f.shape[i]; d.offset[i] = f.offset[i]; d.size[i] = f.size[i]; d.spacing[i] = f.spacing[i]; }
-    std::lock_guard<std::mutex> lock(svc->mutex);
-    svc->dataset_index[d.name] = int(svc->datasets.size());
-    svc->datasets.push_back(d);
+    register_dataset(svc, name, handle);
   });
 }
 

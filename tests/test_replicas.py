@@ -1,0 +1,51 @@
+"""The bench's multi-GPU path (independent replicas, one process per GPU):
+whole-job time is the slowest rank's and whole-job steps the sum over ranks.
+Run here as two gloo processes on the CPU."""
+import os
+import socket
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, results):
+    import torch.distributed as dist
+    sys.path.insert(0, ROOT)
+    import bench
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        # rank r: 10 + r seconds, 1000 * (r + 1) steps
+        results[rank] = bench.combine_ranks(dist, 10.0 + rank, 1000 * (rank + 1), "cpu")
+    finally:
+        dist.destroy_process_group()
+
+
+def test_replica_time_is_the_max_and_steps_the_sum():
+    torch = pytest.importorskip("torch")
+    mp = torch.multiprocessing.get_context("spawn")
+    world, port = 2, _free_port()
+    with mp.Manager() as manager:
+        results = manager.dict()
+        procs = [mp.Process(target=_rank, args=(r, world, port, results)) for r in range(world)]
+        for p in procs:
+            p.start()
+        for p in procs:
+            p.join(120)
+        assert all(p.exitcode == 0 for p in procs)
+        for r in range(world):
+            assert results[r] == (11.0, 3000.0)
+
+
+def test_single_process_passes_through():
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.combine_ranks(None, 2.5, 7, "cpu") == (2.5, 7.0)
