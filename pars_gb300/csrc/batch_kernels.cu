@@ -60,7 +60,7 @@ __device__ __forceinline__ float3 sample_cell(const field_view& f, cell_cache& k
 
 template <bool UNSTEADY>
 struct lane_cache;
-template <> struct lane_cache<false> { cell_cache k; };
+template <> struct lane_cache<false> { corner_cache k; };
 template <> struct lane_cache<true>  { cell_cache2 k; };
 
 // UNSTEADY = false: every job is on a steady field (one slice).

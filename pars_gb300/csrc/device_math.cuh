@@ -451,13 +451,20 @@ __device__ __forceinline__ void unsteady_step(const field_view& f, const time_ax
 // ---- Local cell coordinates (batched engine) -----------------------------------
 // A particle is carried as its cell (ix, iy, iz) and its offset u in [0, 1)^3
 // within that cell, in units of the cell; position = offset + (i + u) * h.
-// The cached cell polynomial is scaled by 1/h per component, so it returns the
-// velocity in cells per unit time and a stage point is u + c * h * k.  A
-// sample inside the current cell needs no floor, division or conversion; the
-// offset keeps 24 bits of precision within its cell however far the cell is
-// from the origin.  A compensation term (lx, ly, lz) carries what the rounding
-// of each step's update dropped from the offset (as compensated_add does for
-// absolute positions), so rounding does not accumulate over the steps.
+// Samples return the velocity in cells per unit time (scaled by 1/h per
+// component), so a stage point is u + c * h * k.  A sample inside the current
+// cell needs no floor, division or conversion; the offset keeps 24 bits of
+// precision within its cell however far the cell is from the origin.  A
+// compensation term (lx, ly, lz) carries what the rounding of each step's
+// update dropped from the offset (as compensated_add does for absolute
+// positions), so rounding does not accumulate over the steps.
+//
+// The lane caches the eight corners of the cell it last sampled.  Within a
+// warp some lane changes cell at almost every sample, so whatever runs only
+// for the lanes that change cell costs the whole warp nearly every sample:
+// that part is kept to the eight loads (and, for a stage point outside the
+// particle's cell, the floor and clamp), and the interpolation itself runs
+// once for all lanes together.
 struct local_position
 {
   int   ix, iy, iz;
@@ -465,11 +472,36 @@ struct local_position
   float lx, ly, lz;
 };
 
-__device__ __forceinline__ void scale3(float3& v, float sx, float sy, float sz) { v.x *= sx; v.y *= sy; v.z *= sz; }
-__device__ __forceinline__ void scale_cache(cell_cache& k, float sx, float sy, float sz)
+struct corner_cache
 {
-  scale3(k.a, sx, sy, sz); scale3(k.b, sx, sy, sz); scale3(k.c, sx, sy, sz); scale3(k.d, sx, sy, sz);
-  scale3(k.e, sx, sy, sz); scale3(k.f, sx, sy, sz); scale3(k.g, sx, sy, sz); scale3(k.h, sx, sy, sz);
+  int    ix = -1, iy = -1, iz = -1;
+  float3 c000, c001, c010, c011, c100, c101, c110, c111;
+};
+
+__device__ __forceinline__ float3 xyz_of(const float4& v) { return make_float3(v.x, v.y, v.z); }
+
+__device__ __forceinline__ void corner_load(const field_view& f, corner_cache& k, int ix, int iy, int iz)
+{
+  const long long syz = (long long)f.ny * f.nz;
+  const float4* base = f.data + ((long long)ix * f.ny + iy) * f.nz + iz;
+  k.ix = ix; k.iy = iy; k.iz = iz;
+  k.c000 = xyz_of(__ldg(base));
+  k.c001 = xyz_of(__ldg(base + 1));
+  k.c010 = xyz_of(__ldg(base + f.nz));
+  k.c011 = xyz_of(__ldg(base + f.nz + 1));
+  k.c100 = xyz_of(__ldg(base + syz));
+  k.c101 = xyz_of(__ldg(base + syz + 1));
+  k.c110 = xyz_of(__ldg(base + syz + f.nz));
+  k.c111 = xyz_of(__ldg(base + syz + f.nz + 1));
+}
+
+// Trilinear interpolation from the corners: lerps along z, then y, then x.
+__device__ __forceinline__ float corner_eval1(float c000, float c001, float c010, float c011, float c100, float c101,
+                                              float c110, float c111, float wx, float wy, float wz)
+{
+  const float c00 = lerp_fast(c000, c001, wz), c01 = lerp_fast(c010, c011, wz);
+  const float c10 = lerp_fast(c100, c101, wz), c11 = lerp_fast(c110, c111, wz);
+  return lerp_fast(lerp_fast(c00, c01, wy), lerp_fast(c10, c11, wy), wx);
 }
 
 // Whether an offset lies in [0, 1): the bit patterns of the floats in [0, 1)
@@ -482,39 +514,28 @@ __device__ __forceinline__ bool in_unit_cube(float ux, float uy, float uz)
   return max(max(__float_as_uint(ux), __float_as_uint(uy)), __float_as_uint(uz)) < 0x3f800000u;
 }
 
-__device__ __forceinline__ float3 local_eval(const cell_cache& k, float wx, float wy, float wz)
-{
-  return make_float3(cache_eval1(k.a.x, k.b.x, k.c.x, k.d.x, k.e.x, k.f.x, k.g.x, k.h.x, wx, wy, wz),
-                     cache_eval1(k.a.y, k.b.y, k.c.y, k.d.y, k.e.y, k.f.y, k.g.y, k.h.y, wx, wy, wz),
-                     cache_eval1(k.a.z, k.b.z, k.c.z, k.d.z, k.e.z, k.f.z, k.g.z, k.h.z, wx, wy, wz));
-}
-
-// The cell's polynomial from its eight corners, scaled to cells per unit time.
-__device__ __forceinline__ void local_cache_load(const field_view& f, cell_cache& k, int ix, int iy, int iz)
-{
-  cache_load(f, k, ix, iy, iz);
-  scale_cache(k, f.inv_hx, f.inv_hy, f.inv_hz);
-}
-
 // Velocity (cells per unit time) at cell (cx, cy, cz) + (ux, uy, uz), where
 // (cx, cy, cz) is the particle's own cell (inside the grid).  The offset may
 // lie outside [0, 1) (a stage point that left the cell); the cell it falls in
 // is then clamped to the grid (weight 0 or 1).
-__device__ __forceinline__ float3 sample_local(const field_view& f, cell_cache& k, int cx, int cy, int cz, float ux, float uy, float uz)
+__device__ __forceinline__ float3 sample_local(const field_view& f, corner_cache& k, int cx, int cy, int cz, float ux, float uy, float uz)
 {
-  if (in_unit_cube(ux, uy, uz))
+  int ix = cx, iy = cy, iz = cz;
+  float wx = ux, wy = uy, wz = uz;
+  if (!in_unit_cube(ux, uy, uz))
   {
-    if (cx != k.ix || cy != k.iy || cz != k.iz) local_cache_load(f, k, cx, cy, cz);
-    return local_eval(k, ux, uy, uz);
+    const float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
+    ix += int(fx); iy += int(fy); iz += int(fz);
+    wx -= fx; wy -= fy; wz -= fz;
+    if (ix < 0) { ix = 0; wx = 0.0f; } else if (ix > f.nx - 2) { ix = f.nx - 2; wx = 1.0f; }
+    if (iy < 0) { iy = 0; wy = 0.0f; } else if (iy > f.ny - 2) { iy = f.ny - 2; wy = 1.0f; }
+    if (iz < 0) { iz = 0; wz = 0.0f; } else if (iz > f.nz - 2) { iz = f.nz - 2; wz = 1.0f; }
   }
-  const float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
-  int ix = cx + int(fx), iy = cy + int(fy), iz = cz + int(fz);
-  float wx = ux - fx, wy = uy - fy, wz = uz - fz;
-  if (ix < 0) { ix = 0; wx = 0.0f; } else if (ix > f.nx - 2) { ix = f.nx - 2; wx = 1.0f; }
-  if (iy < 0) { iy = 0; wy = 0.0f; } else if (iy > f.ny - 2) { iy = f.ny - 2; wy = 1.0f; }
-  if (iz < 0) { iz = 0; wz = 0.0f; } else if (iz > f.nz - 2) { iz = f.nz - 2; wz = 1.0f; }
-  if (ix != k.ix || iy != k.iy || iz != k.iz) local_cache_load(f, k, ix, iy, iz);
-  return local_eval(k, wx, wy, wz);
+  if (ix != k.ix || iy != k.iy || iz != k.iz) corner_load(f, k, ix, iy, iz);
+  return make_float3(
+    f.inv_hx * corner_eval1(k.c000.x, k.c001.x, k.c010.x, k.c011.x, k.c100.x, k.c101.x, k.c110.x, k.c111.x, wx, wy, wz),
+    f.inv_hy * corner_eval1(k.c000.y, k.c001.y, k.c010.y, k.c011.y, k.c100.y, k.c101.y, k.c110.y, k.c111.y, wx, wy, wz),
+    f.inv_hz * corner_eval1(k.c000.z, k.c001.z, k.c010.z, k.c011.z, k.c100.z, k.c101.z, k.c110.z, k.c111.z, wx, wy, wz));
 }
 
 // Moves the offset back into [0, 1) and the cell accordingly.  For an offset
@@ -560,7 +581,7 @@ __device__ __forceinline__ bool is_zero_local(const field_view& f, const float3&
 }
 
 // One classical RK4 (or Euler) step in local coordinates with k1 sampled at q.
-__device__ __forceinline__ void local_step(const field_view& f, cell_cache& k, int rk4, float h, local_position& q, const float3& k1)
+__device__ __forceinline__ void local_step(const field_view& f, corner_cache& k, int rk4, float h, local_position& q, const float3& k1)
 {
   if (!rk4)
   {
