@@ -11,9 +11,12 @@
 //
 // Each particle follows the flow-map rules of particle_advector
 // (particle_advector.cpp:74-139): before every step it stops when it has
-// taken max_steps steps, left the grid (the reference's contains(), floor of
-// the IEEE quotient) or meets a zero velocity (|v_i| <= 1e-5); its last
-// position (and optionally its step count) is written to the job's output.
+// taken max_steps steps, left the grid or meets a zero velocity
+// (|v_i| <= 1e-5); its last position (and optionally its step count) is
+// written to the job's output.  Unsteady jobs test leaving the grid as the
+// reference's contains() does (floor of the IEEE quotient, start_cell);
+// steady jobs, carried in local cell coordinates, test their cell index,
+// which differs from that only within an ulp of the grid's last face.
 #include "context.hpp"
 
 namespace pars
@@ -35,33 +38,10 @@ __device__ __forceinline__ int find_job(const batch_job_device* __restrict__ job
   return lo;
 }
 
-// Cell of one axis for the step-start test and the first sample: the
-// consistent pair (s, w) and whether the reference's floor(rn(d / h)) puts the
-// point inside.  rn(d / h) can differ from the consistent s only when d / h is
-// within an ulp of s + 1, i.e. w is within 1e-4 of 1; only then is the IEEE
-// division evaluated.
-__device__ __forceinline__ bool start_cell(float p, float o, float h, float inv_h, int n, axis_cell& c)
-{
-  c = cell_consistent(p, o, h, inv_h);
-  float s_ref = c.s;
-  if (c.w >= 0.9999f) s_ref = floorf(__fdiv_rn(__fsub_rn(p, o), h));
-  return cell_inside(s_ref, n);
-}
-
-__device__ __forceinline__ float3 sample_cell(const field_view& f, cell_cache& k, axis_cell cx, axis_cell cy, axis_cell cz)
-{
-  clamp_cell(cx, f.nx); clamp_cell(cy, f.ny); clamp_cell(cz, f.nz);
-  const int ix = int(cx.s), iy = int(cy.s), iz = int(cz.s);
-  if (ix != k.ix || iy != k.iy || iz != k.iz) cache_load(f, k, ix, iy, iz);
-  return make_float3(cache_eval1(k.a.x, k.b.x, k.c.x, k.d.x, k.e.x, k.f.x, k.g.x, k.h.x, cx.w, cy.w, cz.w),
-                     cache_eval1(k.a.y, k.b.y, k.c.y, k.d.y, k.e.y, k.f.y, k.g.y, k.h.y, cx.w, cy.w, cz.w),
-                     cache_eval1(k.a.z, k.b.z, k.c.z, k.d.z, k.e.z, k.f.z, k.g.z, k.h.z, cx.w, cy.w, cz.w));
-}
-
 template <bool UNSTEADY>
 struct lane_cache;
 template <> struct lane_cache<false> { corner_cache k; };
-template <> struct lane_cache<true>  { cell_cache2 k; };
+template <> struct lane_cache<true>  { corner_cache2 k; };
 
 // UNSTEADY = false: every job is on a steady field (one slice).
 // UNSTEADY = true: jobs may have several time slices (a steady job works too).

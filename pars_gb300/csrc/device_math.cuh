@@ -155,119 +155,100 @@ __device__ __forceinline__ void clamp_cell(axis_cell& c, int n)
   else if (c.s > float(n - 2)) { c.s = float(n - 2); c.w = 1.0f; }
 }
 
-// Trilinear blend with FMAs (re-sampled path; not bit-exact with the reference).
+// Lerp with one FMA (re-sampled path; not bit-exact with the reference).
 __device__ __forceinline__ float lerp_fast(float a, float b, float w) { return fmaf(w, b - a, a); }
-__device__ __forceinline__ float3 gather_blend_fast(const field_view& f, int ix, int iy, int iz, float wx, float wy, float wz)
+
+// ---- Register-cached cell (re-sampled path) ----------------------------------
+// A particle moves up to about a cell per RK4 step, so most stage samples fall
+// into the cell sampled last.  The lane keeps that cell's eight corners in
+// registers, and only a change of cell issues the eight 16-byte corner loads.
+// Within a warp some lane changes cell at almost every sample, so whatever
+// runs only for the lanes that change cell costs the whole warp nearly every
+// sample: that part is kept to the loads, and the interpolation (lerps along
+// z, then y, then x) runs once for all lanes together.
+struct corner_cache
+{
+  int    ix = -1, iy = -1, iz = -1;
+  float3 c000, c001, c010, c011, c100, c101, c110, c111;
+};
+
+__device__ __forceinline__ float3 xyz_of(const float4& v) { return make_float3(v.x, v.y, v.z); }
+
+__device__ __forceinline__ void corner_load(const field_view& f, corner_cache& k, int ix, int iy, int iz)
 {
   const long long syz = (long long)f.ny * f.nz;
   const float4* base = f.data + ((long long)ix * f.ny + iy) * f.nz + iz;
-  const float4 c000 = __ldg(base);
-  const float4 c001 = __ldg(base + 1);
-  const float4 c010 = __ldg(base + f.nz);
-  const float4 c011 = __ldg(base + f.nz + 1);
-  const float4 c100 = __ldg(base + syz);
-  const float4 c101 = __ldg(base + syz + 1);
-  const float4 c110 = __ldg(base + syz + f.nz);
-  const float4 c111 = __ldg(base + syz + f.nz + 1);
-  float3 out;
-  out.x = lerp_fast(lerp_fast(lerp_fast(c000.x, c001.x, wz), lerp_fast(c010.x, c011.x, wz), wy),
-                    lerp_fast(lerp_fast(c100.x, c101.x, wz), lerp_fast(c110.x, c111.x, wz), wy), wx);
-  out.y = lerp_fast(lerp_fast(lerp_fast(c000.y, c001.y, wz), lerp_fast(c010.y, c011.y, wz), wy),
-                    lerp_fast(lerp_fast(c100.y, c101.y, wz), lerp_fast(c110.y, c111.y, wz), wy), wx);
-  out.z = lerp_fast(lerp_fast(lerp_fast(c000.z, c001.z, wz), lerp_fast(c010.z, c011.z, wz), wy),
-                    lerp_fast(lerp_fast(c100.z, c101.z, wz), lerp_fast(c110.z, c111.z, wz), wy), wx);
-  return out;
-}
-
-__device__ __forceinline__ float3 sample_clamped(const field_view& f, float px, float py, float pz)
-{
-  axis_cell cx = cell_consistent(px, f.ox, f.hx, f.inv_hx), cy = cell_consistent(py, f.oy, f.hy, f.inv_hy),
-            cz = cell_consistent(pz, f.oz, f.hz, f.inv_hz);
-  clamp_cell(cx, f.nx); clamp_cell(cy, f.ny); clamp_cell(cz, f.nz);
-  return gather_blend_fast(f, int(cx.s), int(cy.s), int(cz.s), cx.w, cy.w, cz.w);
-}
-
-// ---- Register-cached cell (re-sampled path) ----------------------------------
-// A particle moves about a quarter of a cell per RK4 step, so consecutive stage
-// samples mostly fall into the cell sampled last.  The cache holds that cell's
-// trilinear polynomial
-//   v(wx,wy,wz) = a + b wx + c wy + d wz + e wx wy + f wy wz + g wx wz + h wx wy wz
-// in registers; a sample in the same cell costs 18 FMAs and no memory access,
-// and only a change of cell issues the eight 16-byte corner loads.
-struct cell_cache
-{
-  int    ix = -1, iy = -1, iz = -1;
-  float3 a, b, c, d, e, f, g, h;
-};
-
-__device__ __forceinline__ float3 sub3(const float4& p, const float4& q) { return make_float3(p.x - q.x, p.y - q.y, p.z - q.z); }
-
-__device__ __forceinline__ void cache_load(const field_view& fv, cell_cache& k, int ix, int iy, int iz)
-{
-  const long long syz = (long long)fv.ny * fv.nz;
-  const float4* base = fv.data + ((long long)ix * fv.ny + iy) * fv.nz + iz;
-  const float4 c000 = __ldg(base);
-  const float4 c001 = __ldg(base + 1);
-  const float4 c010 = __ldg(base + fv.nz);
-  const float4 c011 = __ldg(base + fv.nz + 1);
-  const float4 c100 = __ldg(base + syz);
-  const float4 c101 = __ldg(base + syz + 1);
-  const float4 c110 = __ldg(base + syz + fv.nz);
-  const float4 c111 = __ldg(base + syz + fv.nz + 1);
   k.ix = ix; k.iy = iy; k.iz = iz;
-  k.a = make_float3(c000.x, c000.y, c000.z);
-  k.b = sub3(c100, c000);
-  k.c = sub3(c010, c000);
-  k.d = sub3(c001, c000);
-  const float3 c110_c100 = sub3(c110, c100), c011_c010 = sub3(c011, c010), c101_c100 = sub3(c101, c100);
-  k.e = make_float3(c110_c100.x - k.c.x, c110_c100.y - k.c.y, c110_c100.z - k.c.z);   // (c110-c100) - (c010-c000)
-  k.f = make_float3(c011_c010.x - k.d.x, c011_c010.y - k.d.y, c011_c010.z - k.d.z);   // (c011-c010) - (c001-c000)
-  k.g = make_float3(c101_c100.x - k.d.x, c101_c100.y - k.d.y, c101_c100.z - k.d.z);   // (c101-c100) - (c001-c000)
-  const float3 c111_c110 = sub3(c111, c110);
-  // h = (c111-c110) - (c101-c100) - (c011-c010) + (c001-c000)
-  k.h = make_float3(c111_c110.x - c101_c100.x - c011_c010.x + k.d.x, c111_c110.y - c101_c100.y - c011_c010.y + k.d.y,
-                    c111_c110.z - c101_c100.z - c011_c010.z + k.d.z);
+  k.c000 = xyz_of(__ldg(base));
+  k.c001 = xyz_of(__ldg(base + 1));
+  k.c010 = xyz_of(__ldg(base + f.nz));
+  k.c011 = xyz_of(__ldg(base + f.nz + 1));
+  k.c100 = xyz_of(__ldg(base + syz));
+  k.c101 = xyz_of(__ldg(base + syz + 1));
+  k.c110 = xyz_of(__ldg(base + syz + f.nz));
+  k.c111 = xyz_of(__ldg(base + syz + f.nz + 1));
 }
 
-__device__ __forceinline__ float cache_eval1(float a, float b, float c, float d, float e, float f, float g, float h,
-                                             float wx, float wy, float wz)
+__device__ __forceinline__ float corner_eval1(float c000, float c001, float c010, float c011, float c100, float c101,
+                                              float c110, float c111, float wx, float wy, float wz)
 {
-  const float xpart = fmaf(wy, fmaf(wz, h, e), fmaf(wz, g, b));
-  const float ypart = fmaf(wz, f, c);
-  return fmaf(wx, xpart, fmaf(wy, ypart, fmaf(wz, d, a)));
+  const float c00 = lerp_fast(c000, c001, wz), c01 = lerp_fast(c010, c011, wz);
+  const float c10 = lerp_fast(c100, c101, wz), c11 = lerp_fast(c110, c111, wz);
+  return lerp_fast(lerp_fast(c00, c01, wy), lerp_fast(c10, c11, wy), wx);
 }
 
-__device__ __forceinline__ float3 sample_cached(const field_view& fv, cell_cache& k, float px, float py, float pz)
+__device__ __forceinline__ float3 corner_eval(const corner_cache& k, float wx, float wy, float wz)
 {
-  axis_cell cx = cell_consistent(px, fv.ox, fv.hx, fv.inv_hx), cy = cell_consistent(py, fv.oy, fv.hy, fv.inv_hy),
-            cz = cell_consistent(pz, fv.oz, fv.hz, fv.inv_hz);
+  return make_float3(corner_eval1(k.c000.x, k.c001.x, k.c010.x, k.c011.x, k.c100.x, k.c101.x, k.c110.x, k.c111.x, wx, wy, wz),
+                     corner_eval1(k.c000.y, k.c001.y, k.c010.y, k.c011.y, k.c100.y, k.c101.y, k.c110.y, k.c111.y, wx, wy, wz),
+                     corner_eval1(k.c000.z, k.c001.z, k.c010.z, k.c011.z, k.c100.z, k.c101.z, k.c110.z, k.c111.z, wx, wy, wz));
+}
+
+// The velocity at the consistent cells (cx, cy, cz) — clamped to the grid:
+// constant extension of the boundary values — through the lane's cached cell.
+__device__ __forceinline__ float3 sample_cached_cells(const field_view& fv, corner_cache& k, axis_cell cx, axis_cell cy, axis_cell cz)
+{
   clamp_cell(cx, fv.nx); clamp_cell(cy, fv.ny); clamp_cell(cz, fv.nz);
   const int ix = int(cx.s), iy = int(cy.s), iz = int(cz.s);
-  if (ix != k.ix || iy != k.iy || iz != k.iz) cache_load(fv, k, ix, iy, iz);
-  return make_float3(cache_eval1(k.a.x, k.b.x, k.c.x, k.d.x, k.e.x, k.f.x, k.g.x, k.h.x, cx.w, cy.w, cz.w),
-                     cache_eval1(k.a.y, k.b.y, k.c.y, k.d.y, k.e.y, k.f.y, k.g.y, k.h.y, cx.w, cy.w, cz.w),
-                     cache_eval1(k.a.z, k.b.z, k.c.z, k.d.z, k.e.z, k.f.z, k.g.z, k.h.z, cx.w, cy.w, cz.w));
+  if (ix != k.ix || iy != k.iy || iz != k.iz) corner_load(fv, k, ix, iy, iz);
+  return corner_eval(k, cx.w, cy.w, cz.w);
 }
 
-// The reference's contains() (floor of the IEEE quotient, vector_field.cpp:16-17).
-__device__ __forceinline__ bool contains_reference(const field_view& f, const float4& p)
+__device__ __forceinline__ float3 sample_cached(const field_view& fv, corner_cache& k, float px, float py, float pz)
 {
-  const float sx = floorf(__fdiv_rn(__fsub_rn(p.x, f.ox), f.hx));
-  const float sy = floorf(__fdiv_rn(__fsub_rn(p.y, f.oy), f.hy));
-  const float sz = floorf(__fdiv_rn(__fsub_rn(p.z, f.oz), f.hz));
-  return cell_inside(sx, f.nx) && cell_inside(sy, f.ny) && cell_inside(sz, f.nz);
+  return sample_cached_cells(fv, k, cell_consistent(px, fv.ox, fv.hx, fv.inv_hx), cell_consistent(py, fv.oy, fv.hy, fv.inv_hy),
+                             cell_consistent(pz, fv.oz, fv.hz, fv.inv_hz));
 }
 
-// First stage of a re-sampled step: the reference's contains() decides
-// termination (floor of the IEEE quotient, as vector_field.cpp:16-17), and the
-// velocity comes from the consistent sampler.
-__device__ __forceinline__ bool sample_inside_resampled(const field_view& f, const float4& p, float3& v)
+// Cell of one axis for the step-start test: the consistent pair (s, w), and
+// whether the reference's floor(rn(d / h)) (contains(), vector_field.cpp:16-17)
+// puts the point inside.  rn(d / h) can differ from s only when d / h lies
+// within half an ulp of s + 1 (at most (s + 1) 2^-24), i.e. when w is that
+// close to 1, or when d is a tiny negative number (a point just below the
+// grid's origin, where no representable remainder lies in [0, h) and w comes
+// out negative); the IEEE division is evaluated only when w < 0 or w is within
+// max(2^-20, (s + 1) 2^-22) of 1, which covers those cases with room for the
+// rounding of w itself.
+__device__ __forceinline__ bool start_cell(float p, float o, float h, float inv_h, int n, axis_cell& c)
 {
-  const float sx = floorf(__fdiv_rn(__fsub_rn(p.x, f.ox), f.hx));
-  const float sy = floorf(__fdiv_rn(__fsub_rn(p.y, f.oy), f.hy));
-  const float sz = floorf(__fdiv_rn(__fsub_rn(p.z, f.oz), f.hz));
-  if (!(cell_inside(sx, f.nx) && cell_inside(sy, f.ny) && cell_inside(sz, f.nz))) return false;
-  v = sample_clamped(f, p.x, p.y, p.z);
+  c = cell_consistent(p, o, h, inv_h);
+  float s_ref = c.s;
+  if (c.w < 0.0f || c.w >= 1.0f - fmaxf(0x1p-20f, (c.s + 1.0f) * 0x1p-22f)) s_ref = floorf(__fdiv_rn(__fsub_rn(p, o), h));
+  return cell_inside(s_ref, n);
+}
+
+// The reference's contains() at p (floor of the IEEE quotient per axis inside
+// [0, n-2], vector_field.cpp:16-17) and, when p is inside, the velocity there
+// through the cell cache — the IEEE divisions are evaluated only within
+// rounding distance of a cell face.
+__device__ __forceinline__ bool sample_start(const field_view& f, corner_cache& k, const float4& p, float3& v)
+{
+  axis_cell cx, cy, cz;
+  const bool in_x = start_cell(p.x, f.ox, f.hx, f.inv_hx, f.nx, cx);
+  const bool in_y = start_cell(p.y, f.oy, f.hy, f.inv_hy, f.ny, cy);
+  const bool in_z = start_cell(p.z, f.oz, f.hz, f.inv_hz, f.nz, cz);
+  if (!(in_x && in_y && in_z)) return false;
+  v = sample_cached_cells(f, k, cx, cy, cz);
   return true;
 }
 
@@ -321,29 +302,8 @@ __device__ __forceinline__ void compensated_add(float& hi, float& lo, float delt
 }
 
 // RESAMPLED step: classical RK4 (or Euler) with the first-stage velocity k1
-// already sampled at x; stage points are sampled with sample_clamped.
-__device__ __forceinline__ void resampled_step(const field_view& f, const step_rule& r, float4& x, float3& lo, const float3& k1)
-{
-  if (!r.rk4)
-  {
-    compensated_add(x.x, lo.x, r.h * k1.x);
-    compensated_add(x.y, lo.y, r.h * k1.y);
-    compensated_add(x.z, lo.z, r.h * k1.z);
-    return;
-  }
-  const float hh = 0.5f * r.h;
-  const float3 k2 = sample_clamped(f, fmaf(hh, k1.x, x.x), fmaf(hh, k1.y, x.y), fmaf(hh, k1.z, x.z));
-  const float3 k3 = sample_clamped(f, fmaf(hh, k2.x, x.x), fmaf(hh, k2.y, x.y), fmaf(hh, k2.z, x.z));
-  const float3 k4 = sample_clamped(f, fmaf(r.h, k3.x, x.x), fmaf(r.h, k3.y, x.y), fmaf(r.h, k3.z, x.z));
-  const float h6 = r.h * (1.0f / 6.0f);
-  compensated_add(x.x, lo.x, h6 * (k1.x + 2.0f * (k2.x + k3.x) + k4.x));
-  compensated_add(x.y, lo.y, h6 * (k1.y + 2.0f * (k2.y + k3.y) + k4.y));
-  compensated_add(x.z, lo.z, h6 * (k1.z + 2.0f * (k2.z + k3.z) + k4.z));
-}
-
-// Re-sampled step through the cell cache (same scheme as resampled_step, the
-// trilinear blend in polynomial form).
-__device__ __forceinline__ void resampled_step_cached(const field_view& f, cell_cache& k, const step_rule& r, float4& x,
+// already sampled at x; stage points are sampled through the cell cache.
+__device__ __forceinline__ void resampled_step_cached(const field_view& f, corner_cache& k, const step_rule& r, float4& x,
                                                       float3& lo, const float3& k1)
 {
   if (!r.rk4)
@@ -387,15 +347,15 @@ __device__ __forceinline__ void slice_of(const time_axis& ta, double t, int& sli
   else { slice = int(fs); wt = float(s - fs); }
 }
 
-// Two slices of one cell (the slices around the current time), as trilinear
-// polynomials; reloaded when the cell or the slice pair changes.
-struct cell_cache2
+// The corners of one cell in the two slices around the current time;
+// reloaded when the cell or the slice pair changes.
+struct corner_cache2
 {
-  int        slice = -1;
-  cell_cache c0, c1;
+  int          slice = -1;
+  corner_cache c0, c1;
 };
 
-__device__ __forceinline__ float3 sample_unsteady_cached(const field_view& fv, const time_axis& ta, cell_cache2& k,
+__device__ __forceinline__ float3 sample_unsteady_cached(const field_view& fv, const time_axis& ta, corner_cache2& k,
                                                          float px, float py, float pz, double t)
 {
   axis_cell cx = cell_consistent(px, fv.ox, fv.hx, fv.inv_hx), cy = cell_consistent(py, fv.oy, fv.hy, fv.inv_hy),
@@ -410,23 +370,19 @@ __device__ __forceinline__ float3 sample_unsteady_cached(const field_view& fv, c
     field_view s0 = fv, s1 = fv;
     s0.data = fv.data + (long long)slice * ta.slice_stride;
     s1.data = fv.data + (long long)(ta.nt > 1 ? slice + 1 : slice) * ta.slice_stride;
-    cache_load(s0, k.c0, ix, iy, iz);
-    cache_load(s1, k.c1, ix, iy, iz);
+    corner_load(s0, k.c0, ix, iy, iz);
+    corner_load(s1, k.c1, ix, iy, iz);
     k.slice = slice;
   }
-  const float3 v0 = make_float3(cache_eval1(k.c0.a.x, k.c0.b.x, k.c0.c.x, k.c0.d.x, k.c0.e.x, k.c0.f.x, k.c0.g.x, k.c0.h.x, cx.w, cy.w, cz.w),
-                                cache_eval1(k.c0.a.y, k.c0.b.y, k.c0.c.y, k.c0.d.y, k.c0.e.y, k.c0.f.y, k.c0.g.y, k.c0.h.y, cx.w, cy.w, cz.w),
-                                cache_eval1(k.c0.a.z, k.c0.b.z, k.c0.c.z, k.c0.d.z, k.c0.e.z, k.c0.f.z, k.c0.g.z, k.c0.h.z, cx.w, cy.w, cz.w));
+  const float3 v0 = corner_eval(k.c0, cx.w, cy.w, cz.w);
   if (wt == 0.0f) return v0;
-  const float3 v1 = make_float3(cache_eval1(k.c1.a.x, k.c1.b.x, k.c1.c.x, k.c1.d.x, k.c1.e.x, k.c1.f.x, k.c1.g.x, k.c1.h.x, cx.w, cy.w, cz.w),
-                                cache_eval1(k.c1.a.y, k.c1.b.y, k.c1.c.y, k.c1.d.y, k.c1.e.y, k.c1.f.y, k.c1.g.y, k.c1.h.y, cx.w, cy.w, cz.w),
-                                cache_eval1(k.c1.a.z, k.c1.b.z, k.c1.c.z, k.c1.d.z, k.c1.e.z, k.c1.f.z, k.c1.g.z, k.c1.h.z, cx.w, cy.w, cz.w));
+  const float3 v1 = corner_eval(k.c1, cx.w, cy.w, cz.w);
   return make_float3(fmaf(wt, v1.x - v0.x, v0.x), fmaf(wt, v1.y - v0.y, v0.y), fmaf(wt, v1.z - v0.z, v0.z));
 }
 
 // One pathline step from (x, t): classical RK4 in space-time with re-sampled
 // stages at t, t + h/2, t + h/2, t + h, or the frozen rule (velocity at (x, t)).
-__device__ __forceinline__ void unsteady_step(const field_view& f, const time_axis& ta, cell_cache2& k, const step_rule& r,
+__device__ __forceinline__ void unsteady_step(const field_view& f, const time_axis& ta, corner_cache2& k, const step_rule& r,
                                               float4& x, float3& lo, const float3& k1, double t)
 {
   if (r.frozen || !r.rk4)
@@ -472,38 +428,6 @@ struct local_position
   float lx, ly, lz;
 };
 
-struct corner_cache
-{
-  int    ix = -1, iy = -1, iz = -1;
-  float3 c000, c001, c010, c011, c100, c101, c110, c111;
-};
-
-__device__ __forceinline__ float3 xyz_of(const float4& v) { return make_float3(v.x, v.y, v.z); }
-
-__device__ __forceinline__ void corner_load(const field_view& f, corner_cache& k, int ix, int iy, int iz)
-{
-  const long long syz = (long long)f.ny * f.nz;
-  const float4* base = f.data + ((long long)ix * f.ny + iy) * f.nz + iz;
-  k.ix = ix; k.iy = iy; k.iz = iz;
-  k.c000 = xyz_of(__ldg(base));
-  k.c001 = xyz_of(__ldg(base + 1));
-  k.c010 = xyz_of(__ldg(base + f.nz));
-  k.c011 = xyz_of(__ldg(base + f.nz + 1));
-  k.c100 = xyz_of(__ldg(base + syz));
-  k.c101 = xyz_of(__ldg(base + syz + 1));
-  k.c110 = xyz_of(__ldg(base + syz + f.nz));
-  k.c111 = xyz_of(__ldg(base + syz + f.nz + 1));
-}
-
-// Trilinear interpolation from the corners: lerps along z, then y, then x.
-__device__ __forceinline__ float corner_eval1(float c000, float c001, float c010, float c011, float c100, float c101,
-                                              float c110, float c111, float wx, float wy, float wz)
-{
-  const float c00 = lerp_fast(c000, c001, wz), c01 = lerp_fast(c010, c011, wz);
-  const float c10 = lerp_fast(c100, c101, wz), c11 = lerp_fast(c110, c111, wz);
-  return lerp_fast(lerp_fast(c00, c01, wy), lerp_fast(c10, c11, wy), wx);
-}
-
 // Whether an offset lies in [0, 1): the bit patterns of the floats in [0, 1)
 // are exactly the unsigned values below that of 1.0f (negative values, -0,
 // infinities and NaNs all compare above), so one unsigned compare per axis —
@@ -532,10 +456,8 @@ __device__ __forceinline__ float3 sample_local(const field_view& f, corner_cache
     if (iz < 0) { iz = 0; wz = 0.0f; } else if (iz > f.nz - 2) { iz = f.nz - 2; wz = 1.0f; }
   }
   if (ix != k.ix || iy != k.iy || iz != k.iz) corner_load(f, k, ix, iy, iz);
-  return make_float3(
-    f.inv_hx * corner_eval1(k.c000.x, k.c001.x, k.c010.x, k.c011.x, k.c100.x, k.c101.x, k.c110.x, k.c111.x, wx, wy, wz),
-    f.inv_hy * corner_eval1(k.c000.y, k.c001.y, k.c010.y, k.c011.y, k.c100.y, k.c101.y, k.c110.y, k.c111.y, wx, wy, wz),
-    f.inv_hz * corner_eval1(k.c000.z, k.c001.z, k.c010.z, k.c011.z, k.c100.z, k.c101.z, k.c110.z, k.c111.z, wx, wy, wz));
+  const float3 v = corner_eval(k, wx, wy, wz);
+  return make_float3(f.inv_hx * v.x, f.inv_hy * v.y, f.inv_hz * v.z);
 }
 
 // Moves the offset back into [0, 1) and the cell accordingly.  For an offset

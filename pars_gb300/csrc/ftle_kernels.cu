@@ -47,17 +47,13 @@ __global__ void __launch_bounds__(256) flow_map_kernel(const flow_map_args a)
                              __fadd_rn(a.oz, __fmul_rn(a.sz, float(iz))), 0.0f);
     bool finished = false;
     float3 lo = make_float3(0.0f, 0.0f, 0.0f);
-    cell_cache cache;
+    corner_cache cache;
     for (int it = 1; it < a.iterations; ++it)
     {
       float3 v;
       bool inside;
       if (FROZEN) inside = sample_inside(a.f, pos, v);
-      else
-      {
-        inside = contains_reference(a.f, pos);
-        if (inside) v = sample_cached(a.f, cache, pos.x, pos.y, pos.z);
-      }
+      else        inside = sample_start(a.f, cache, pos, v);
       if (!inside) { finished = true; break; }
       if (is_zero(v)) { finished = true; break; }
       if (FROZEN) pos = frozen_step(a.rule, pos, v);

@@ -43,18 +43,14 @@ __global__ void __launch_bounds__(256) trace_kernel(const trace_launch a)
     int kept = is_invalid_vertex(last) ? 0 : 1;
     const float4 term = termination_vertex();
     float3 lo = make_float3(0.0f, 0.0f, 0.0f);
-    cell_cache cache;
+    corner_cache cache;
     for (int it = 1; it < N; ++it)
     {
       if (it == N - 1) { out[it] = term; ++written; ++kept; break; }
       float3 v;
       bool inside;
       if (FROZEN) inside = sample_inside(f, last, v);
-      else
-      {
-        inside = contains_reference(f, last);
-        if (inside) v = sample_cached(f, cache, last.x, last.y, last.z);
-      }
+      else        inside = sample_start(f, cache, last, v);
       if (!inside)
       {
         out[it] = term; ++written; ++kept;
