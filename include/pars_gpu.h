@@ -361,6 +361,19 @@ int32_t pars_gpu_service_result_batch(pars_gpu_service* service, int64_t ticket,
 int32_t pars_gpu_service_result_ftle (pars_gpu_service* service, int64_t ticket, float* values);
 /* Forgets a request (cancels it if it is still queued). */
 int32_t pars_gpu_service_release     (pars_gpu_service* service, int64_t ticket);
+/* Instrumentation (no counterpart in the reference's service; the reference
+ * times its stages with its own benchmark recorder).  Enabling clears the
+ * totals; from the next batch on, every lane times its kernels with CUDA
+ * events and each batch phase by wall clock (the lane's stream is drained at
+ * each phase end, so profiling costs some overlap).  Names: kernel names as
+ * pars_gpu_profile_get reports them; phases "streamlines.seed",
+ * "streamlines.trace", "streamlines.index_color", "streamlines.results",
+ * "ftle.setup", "ftle.advect", "ftle.field", "lane.trim" (returning a lane's
+ * scratch beyond what it keeps between batches) (milliseconds, count = batches);
+ * "batches.streamlines" / "batches.ftle" (count = batches, milliseconds =
+ * the number of requests they held). */
+int32_t pars_gpu_service_profile_enable(pars_gpu_service* service, int32_t enable);
+int32_t pars_gpu_service_profile_get   (pars_gpu_service* service, const char* name, double* milliseconds, int64_t* count);
 
 /* ---- allocation-free FTLE --------------------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device

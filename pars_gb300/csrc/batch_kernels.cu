@@ -232,10 +232,10 @@ void launch_batch_advect(pars_gpu_context& ctx, int job_class, int v, const batc
 {
   if (total_pools <= 0) return;
   const variant& var = variants[job_class][v];
-  int per_sm = 0, sms = 0;
-  PARS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, var.kernel, var.threads, 0));
-  PARS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
-  const long long persistent = (long long)std::max(per_sm, 1) * sms;
+  int& per_sm = ctx.batch_ctas_per_sm[job_class][v];
+  if (per_sm < 0) PARS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, var.kernel, var.threads, 0));
+  if (ctx.sm_count <= 0) PARS_CUDA(cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, ctx.device));
+  const long long persistent = (long long)std::max(per_sm, 1) * ctx.sm_count;
   const long long warps_needed = total_pools;   // at least one pool per warp
   const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>(persistent, (warps_needed * 32 + var.threads - 1) / var.threads));
   launch_scope scope(ctx, "batch_advect");

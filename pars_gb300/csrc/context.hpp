@@ -136,8 +136,9 @@ struct curves_store
 {
   device_buffer             vertices;   // float4
   device_buffer             colors;     // float4
-  device_buffer             indices;    // int32
+  device_buffer             indices;    // int32, the batches' indices packed one after the other
   long long                 vertex_total = 0;
+  long long                 index_total = 0;
   bool                      indexed = false;
   bool                      colored = false;
   std::vector<curves_batch> batches;
@@ -172,7 +173,7 @@ struct pars_gpu_context
                                           block_of_next, exits, exit_keys, exit_keys_sorted, exit_order,
                                           exit_order_sorted, counters, block_max, cub_temp, scan_input, tile_counts,
                                           tile_offsets, staging, boundary_positions, boundary_offsets, single_block,
-                                          slot_layouts;
+                                          slot_layouts, curve_bounds, color_specs;
   pars::device_buffer                     ftle;
   long long                               ftle_count = 0;
   // Released field buffers kept for reuse (bytes -> buffer), so that a caller
@@ -184,6 +185,12 @@ struct pars_gpu_context
   // per job class (0 = steady, 1 = unsteady); -1 = not tuned yet
   pars::device_buffer                     batch_jobs, batch_counters;
   int                                     batch_variant[2] = {-1, -1};
+  // tracing kernel: resident CTAs of 128 threads per SM (frozen, re-sampled)
+  // and the device's SM count, queried once
+  int                                     trace_ctas_per_sm[2] = {-1, -1};
+  int                                     sm_count = 0;
+  // batched engine: resident CTAs per SM per job class and launch shape
+  int                                     batch_ctas_per_sm[2][4] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}};
   static constexpr std::size_t            buffer_cache_limit = std::size_t(8) << 30;
   // instrumentation
   bool                                    profile = false;
@@ -217,6 +224,9 @@ void recycle_buffer(pars_gpu_context& ctx, device_buffer&& buffer);
 // Frees every scratch buffer and the buffer cache after the stream drains
 // (fields and domains stay); the last trace's curves are dropped.
 void release_scratch(pars_gpu_context& ctx);
+// Resolves the context's timed launches and moves its per-kernel totals into
+// `into` (adding), leaving the context's totals empty.
+void take_profile(pars_gpu_context& ctx, std::map<std::string, profile_entry>& into);
 
 // Integrator parameters for (integrator, stage mode, step size); throws
 // pars::error for integrators the kernels do not implement.
@@ -255,6 +265,7 @@ struct trace_launch
   unsigned long long*  exit_keys;     // (destination block << 40) | particle index
   unsigned int*        exit_count;
   unsigned long long*  steps;
+  unsigned long long*  next;          // pool counter (zero before the launch)
 };
 void launch_trace(pars_gpu_context& ctx, const trace_launch& a);
 void launch_compact_vertices(pars_gpu_context& ctx, const float4* slots, const slot_layout* block_slots, const int* block_of,
@@ -282,6 +293,20 @@ void launch_extract_block(pars_gpu_context& ctx, const float* domain_xyz, const 
 long long launch_index_generate(pars_gpu_context& ctx, const float4* vertices, long long n, int* indices);
 void launch_color_generate(pars_gpu_context& ctx, const float4* vertices, const int* indices, long long index_count,
                            int mode, float parameter, float4* colors);
+
+// Colour mode and parameter of one curve batch.
+struct color_spec
+{
+  int   mode;
+  float parameter;
+};
+// index_generator::generate on every batch of a curves store in one pass
+// (three launches and one host read for all batches): sets each batch's
+// index_offset / index_count into the packed index buffer.
+void index_batches(pars_gpu_context& ctx, curves_store& c);
+// color_generator::generate on every batch (after index_batches) in one
+// launch, with each batch's own mode and parameter.
+void color_batches(pars_gpu_context& ctx, curves_store& c, const std::vector<color_spec>& specs);
 
 // One job of a batched advection launch, as the persistent kernel reads it.
 struct batch_job_device

@@ -8,8 +8,9 @@
 //   thread per index; the FP32 operations follow the reference one by one with
 //   explicit round-to-nearest intrinsics (no FMA contraction).  The tangent's
 //   squared norm is reduced in the order of Eigen's SSE packet reduction,
-//   (d0^2 + d2^2) + (d1^2 + d3^2).  atan2 and acos are evaluated in FP64 and
-//   rounded to FP32 (the reference calls the host libm's FP32 versions).
+//   (d0^2 + d2^2) + (d1^2 + d3^2).  atan2 and acos are FP32 functions on both
+//   sides (the host libm's there, CUDA's here), so hue / saturation colours
+//   agree to a few FP32 ulps rather than bit for bit.
 #include <cub/cub.cuh>
 
 #include "context.hpp"
@@ -81,11 +82,15 @@ __device__ float4 color_of(const float4& a, const float4& b, int mode, float par
   }
   if (mode == PARS_COLOR_RGB) return make_float4(fabsf(d.x), fabsf(d.z), fabsf(d.y), 1.0f);
 
-  // to_spherical (coordinates.hpp:8-16): std::pow(float, int) promotes to double.
+  // to_spherical (coordinates.hpp:8-16): std::pow(float, int) promotes to
+  // double, so the radius is the FP64 root rounded to FP32, exactly as the
+  // reference computes it (acos near +-1 would magnify any difference in it).
+  // atan2 and acos are the FP32 functions, as the reference calls them (the
+  // host libm's atan2f / acosf there, CUDA's here: within 3 and 2 ulp).
   const double tx = d.x, ty = d.y, tz = d.z;
   const float radius = __double2float_rn(__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(tx, tx), __dmul_rn(ty, ty)), __dmul_rn(tz, tz))));
-  float s1 = __double2float_rn(atan2(ty, tx));
-  float s2 = __double2float_rn(acos(double(__fdiv_rn(d.z, radius))));
+  float s1 = atan2f(d.y, d.x);
+  float s2 = acosf(__fdiv_rn(d.z, radius));
   // correct_range (color_generator.cpp:41-54).
   const float pi = float(3.14159265358979323846);
   if (s1 <  0.0f) s1 = __fadd_rn(s1, pi);
@@ -93,8 +98,12 @@ __device__ float4 color_of(const float4& a, const float4& b, int mode, float par
   s1 = __fsub_rn(pi, s1);
   if (s2 <  0.0f) s2 = fabsf(s2);
   if (s2 >= float(3.14159265358979323846 / 2.0)) s2 = __fsub_rn(pi, s2);
-  const float hue    = __double2float_rn(__ddiv_rn(double(s1), 3.14159265358979323846));
-  const float second = __double2float_rn(__ddiv_rn(double(s2), 3.14159265358979323846 / 2.0));
+  // s / M_PI and s / (M_PI / 2): the reference divides in double and rounds to
+  // float; an FP32 multiply by the rounded reciprocal is within one ulp of
+  // that (hue and saturation are already a few ulps apart from the reference
+  // through atan2f / acosf).
+  const float hue    = __fmul_rn(s1, float(1.0 / 3.14159265358979323846));
+  const float second = __fmul_rn(s2, float(2.0 / 3.14159265358979323846));
 
   const bool constant_first = (mode == PARS_COLOR_HSL_CONSTANT_S || mode == PARS_COLOR_HSV_CONSTANT_S);
   const float sat   = constant_first ? parameter : second;
@@ -130,6 +139,181 @@ __global__ void __launch_bounds__(256) color_kernel(const float4* __restrict__ v
   // The last vertex of a run copies its colour (color_generator.cpp:36-37).
   if (i != m - 1 && indices[i + 1] != index + 1) colors[index + 1] = c;
 }
+
+// ---- every batch of a curves store at once ------------------------------------
+// The batches are consecutive ranges of one vertex buffer (bounds[b] ..
+// bounds[b + 1]).  Index generation runs over the whole buffer with each
+// vertex's flag confined to its batch; one scan gives every flagged vertex its
+// position in the packed index buffer, which holds the batches' indices one
+// after the other (each index relative to its batch, as the reference's).
+
+// The last segment s in [0, segments) with bounds[s] <= x.
+__device__ __forceinline__ int segment_of(const long long* __restrict__ bounds, int segments, long long x)
+{
+  int lo = 0, hi = segments - 1;
+  while (lo < hi)
+  {
+    const int mid = (lo + hi + 1) >> 1;
+    if (bounds[mid] <= x) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Flags of a thread's items: bit k set when vertex first + k is indexed.
+__device__ __forceinline__ unsigned batch_flags(const float4* __restrict__ v, const long long* __restrict__ vbounds, int batches,
+                                                long long first, int& b)
+{
+  const long long n = vbounds[batches];
+  unsigned flags = 0;
+  if (first >= n) return 0;
+  b = segment_of(vbounds, batches, first);
+  long long end = vbounds[b + 1];
+  bool term_i = is_termination_vertex(v[first]);
+  #pragma unroll
+  for (int k = 0; k < index_items; ++k)
+  {
+    const long long i = first + k;
+    if (i >= n) break;
+    while (i >= end) { ++b; end = vbounds[b + 1]; }
+    const bool has_next = i + 1 < end;
+    const bool term_next = i + 1 < n ? is_termination_vertex(v[i + 1]) : true;
+    if (has_next && !term_i && !term_next) flags |= 1u << k;
+    term_i = term_next;
+  }
+  return flags;
+}
+
+__global__ void __launch_bounds__(index_threads) batch_index_count_kernel(const float4* __restrict__ v, const long long* __restrict__ vbounds,
+                                                                          int batches, int* __restrict__ tile_counts)
+{
+  using reduce = cub::BlockReduce<int, index_threads>;
+  __shared__ typename reduce::TempStorage storage;
+  const long long first = (long long)blockIdx.x * index_tile + (long long)threadIdx.x * index_items;
+  int b = 0;
+  const int count = __popc(batch_flags(v, vbounds, batches, first, b));
+  const int total = reduce(storage).Sum(count);
+  if (threadIdx.x == 0) tile_counts[blockIdx.x] = total;
+}
+
+// Writes the packed indices and, for every batch starting at one of the
+// thread's vertices, the batch's first position in the packed buffer.
+__global__ void __launch_bounds__(index_threads) batch_index_write_kernel(const float4* __restrict__ v, const long long* __restrict__ vbounds,
+                                                                          int batches, const long long* __restrict__ tile_offsets,
+                                                                          int* __restrict__ indices, long long* __restrict__ ibounds)
+{
+  using scan = cub::BlockScan<int, index_threads>;
+  __shared__ typename scan::TempStorage storage;
+  const long long first = (long long)blockIdx.x * index_tile + (long long)threadIdx.x * index_items;
+  const long long n = vbounds[batches];
+  int b = 0;
+  const unsigned flags = batch_flags(v, vbounds, batches, first, b);
+  int prefix = 0;
+  scan(storage).ExclusiveSum(__popc(flags), prefix);
+  if (first >= n) return;
+  long long out = tile_offsets[blockIdx.x] + prefix;
+  b = segment_of(vbounds, batches, first);
+  // batches that start inside this thread's range (several when some are empty)
+  int s = b;
+  while (s > 0 && vbounds[s] == first) --s;       // the first batch starting at `first`
+  if (vbounds[s] < first) ++s;
+  #pragma unroll
+  for (int k = 0; k < index_items; ++k)
+  {
+    const long long i = first + k;
+    if (i >= n) break;
+    while (s < batches && vbounds[s] == i) { ibounds[s] = out; ++s; }
+    while (i >= vbounds[b + 1]) ++b;
+    if (flags & (1u << k)) indices[out++] = int(i - vbounds[b]);
+  }
+}
+
+__global__ void __launch_bounds__(256) batch_color_kernel(const float4* __restrict__ v, const int* __restrict__ indices,
+                                                          const long long* __restrict__ vbounds, const long long* __restrict__ ibounds,
+                                                          int batches, const color_spec* __restrict__ specs, float4* __restrict__ colors)
+{
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ibounds[batches]) return;
+  const int b = segment_of(ibounds, batches, k);
+  const int index = indices[k];
+  const long long g = vbounds[b] + index;
+  const color_spec spec = specs[b];
+  const float4 c = color_of(v[g], v[g + 1], spec.mode, spec.parameter);
+  colors[g] = c;
+  // The last vertex of a run copies its colour (color_generator.cpp:36-37);
+  // the last vertex of a batch keeps none.
+  if (k + 1 < ibounds[b + 1] && indices[k + 1] != index + 1) colors[g + 1] = c;
+}
+}
+
+void index_batches(pars_gpu_context& ctx, curves_store& c)
+{
+  const int batches = int(c.batches.size());
+  std::vector<long long> vbounds(batches + 1), ibounds(batches + 1, 0);
+  for (int b = 0; b < batches; ++b) vbounds[b] = c.batches[b].vertex_offset;
+  vbounds[batches] = c.vertex_total;
+  for (int b = 0; b < batches; ++b)
+    PARS_REQUIRE(c.batches[b].vertex_offset + c.batches[b].vertex_count == vbounds[b + 1], "curve batches are not consecutive");
+  c.indices.reserve(sizeof(int) * (std::size_t)std::max<long long>(c.vertex_total, 1));
+  ctx.curve_bounds.reserve(sizeof(long long) * 2 * (batches + 1));
+  long long* d_vbounds = ctx.curve_bounds.as<long long>();
+  long long* d_ibounds = d_vbounds + batches + 1;
+  const long long n = c.vertex_total;
+  if (batches > 0 && n > 0)
+  {
+    PARS_CUDA(cudaMemcpyAsync(d_vbounds, vbounds.data(), sizeof(long long) * (batches + 1), cudaMemcpyHostToDevice, ctx.stream));
+    const long long tiles = (n + index_tile - 1) / index_tile;
+    ctx.tile_counts.reserve(sizeof(int) * tiles);
+    ctx.tile_offsets.reserve(sizeof(long long) * (tiles + 1));
+    {
+      launch_scope scope(ctx, "index_count");
+      batch_index_count_kernel<<<(unsigned)tiles, index_threads, 0, ctx.stream>>>(c.vertices.as<const float4>(), d_vbounds, batches,
+                                                                                  ctx.tile_counts.as<int>());
+    }
+    exclusive_sum(ctx, ctx.tile_counts.as<int>(), ctx.tile_offsets.as<long long>(), tiles);
+    {
+      launch_scope scope(ctx, "index_write");
+      batch_index_write_kernel<<<(unsigned)tiles, index_threads, 0, ctx.stream>>>(c.vertices.as<const float4>(), d_vbounds, batches,
+                                                                                  ctx.tile_offsets.as<const long long>(),
+                                                                                  c.indices.as<int>(), d_ibounds);
+    }
+    long long total = 0;
+    PARS_CUDA(cudaMemcpyAsync(ibounds.data(), d_ibounds, sizeof(long long) * batches, cudaMemcpyDeviceToHost, ctx.stream));
+    PARS_CUDA(cudaMemcpyAsync(&total, ctx.tile_offsets.as<long long>() + tiles, sizeof(long long), cudaMemcpyDeviceToHost, ctx.stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+    ibounds[batches] = total;
+    // batches starting at the very end (empty) were not seen by any thread
+    for (int b = batches - 1; b >= 0; --b) if (vbounds[b] == n) ibounds[b] = total;
+    PARS_CUDA(cudaMemcpyAsync(d_ibounds, ibounds.data(), sizeof(long long) * (batches + 1), cudaMemcpyHostToDevice, ctx.stream));
+  }
+  else if (batches > 0)
+  {
+    PARS_CUDA(cudaMemcpyAsync(d_vbounds, vbounds.data(), sizeof(long long) * (batches + 1), cudaMemcpyHostToDevice, ctx.stream));
+    PARS_CUDA(cudaMemcpyAsync(d_ibounds, ibounds.data(), sizeof(long long) * (batches + 1), cudaMemcpyHostToDevice, ctx.stream));
+  }
+  for (int b = 0; b < batches; ++b)
+  {
+    c.batches[b].index_offset = ibounds[b];
+    c.batches[b].index_count = ibounds[b + 1] - ibounds[b];
+  }
+  c.index_total = ibounds[batches];
+}
+
+void color_batches(pars_gpu_context& ctx, curves_store& c, const std::vector<color_spec>& specs)
+{
+  const int batches = int(c.batches.size());
+  PARS_REQUIRE(specs.size() == std::size_t(batches), "one colour spec per batch");
+  c.colors.reserve(sizeof(float4) * (std::size_t)std::max<long long>(c.vertex_total, 1));
+  if (c.vertex_total > 0) PARS_CUDA(cudaMemsetAsync(c.colors.get(), 0, sizeof(float4) * c.vertex_total, ctx.stream));
+  if (batches == 0 || c.index_total == 0) return;
+  ctx.color_specs.reserve(sizeof(color_spec) * batches);
+  PARS_CUDA(cudaMemcpyAsync(ctx.color_specs.get(), specs.data(), sizeof(color_spec) * batches, cudaMemcpyHostToDevice, ctx.stream));
+  const long long* d_vbounds = ctx.curve_bounds.as<const long long>();
+  const long long* d_ibounds = d_vbounds + batches + 1;
+  launch_scope scope(ctx, "color_generate");
+  batch_color_kernel<<<(unsigned)((c.index_total + 255) / 256), 256, 0, ctx.stream>>>(
+    c.vertices.as<const float4>(), c.indices.as<const int>(), d_vbounds, d_ibounds, batches, ctx.color_specs.as<const color_spec>(),
+    c.colors.as<float4>());
 }
 
 long long launch_index_generate(pars_gpu_context& ctx, const float4* vertices, long long n, int* indices)

@@ -26,7 +26,7 @@ void for_each_scratch(context_type& c, visit_type&& visit)
                   &c.exit_order_sorted, &c.counters, &c.block_max, &c.cub_temp, &c.scan_input, &c.tile_counts,
                   &c.tile_offsets, &c.staging, &c.ftle, &c.curves.vertices, &c.curves.colors,
                   &c.curves.indices, &c.boundary_positions, &c.boundary_offsets, &c.batch_jobs,
-                  &c.batch_counters, &c.single_block, &c.slot_layouts})
+                  &c.batch_counters, &c.single_block, &c.slot_layouts, &c.curve_bounds, &c.color_specs})
     visit(*b);
 }
 }
@@ -87,6 +87,7 @@ void release_scratch(pars_gpu_context& ctx)
   ctx.buffer_cache.clear();
   ctx.buffer_cache_bytes = 0;
   ctx.curves.vertex_total = 0;
+  ctx.curves.index_total = 0;
   ctx.curves.indexed = ctx.curves.colored = false;
   ctx.curves.batches.clear();
   ctx.ftle_count = 0;
@@ -140,7 +141,21 @@ void flush_profile(pars_gpu_context& ctx)
   }
   ctx.pending.clear();
 }
+}
 
+void take_profile(pars_gpu_context& ctx, std::map<std::string, profile_entry>& into)
+{
+  flush_profile(ctx);
+  for (auto& t : ctx.profile_totals)
+  {
+    into[t.first].milliseconds += t.second.milliseconds;
+    into[t.first].launches += t.second.launches;
+  }
+  ctx.profile_totals.clear();
+}
+
+namespace
+{
 template <typename body_type>
 int32_t guarded(pars_gpu_context* ctx, body_type&& body)
 {
@@ -285,14 +300,17 @@ void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, c
   auto& curves = ctx.curves;
   curves.batches.clear();
   curves.vertex_total = 0;
+  curves.index_total = 0;
   curves.indexed = curves.colored = false;
   const int nblocks = int(blocks.size());
   int key_bits = 40;
   while ((1 << (key_bits - 40)) < nblocks) ++key_bits;
 
-  ctx.counters.reserve(sizeof(unsigned long long) * 2);
+  // counters: steps, exit queue size (32-bit), the tracing kernel's pool counter
+  ctx.counters.reserve(sizeof(unsigned long long) * 3);
   auto* steps_counter = ctx.counters.as<unsigned long long>();
   auto* exit_counter = reinterpret_cast<unsigned int*>(steps_counter + 1);
+  auto* pool_counter = steps_counter + 2;
   PARS_CUDA(cudaMemsetAsync(steps_counter, 0, sizeof(unsigned long long), ctx.stream));
 
   int round = 0;
@@ -324,6 +342,7 @@ void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, c
       ctx.exit_keys.reserve(sizeof(unsigned long long) * count);
     }
     PARS_CUDA(cudaMemsetAsync(exit_counter, 0, sizeof(unsigned int), ctx.stream));
+    PARS_CUDA(cudaMemsetAsync(pool_counter, 0, sizeof(unsigned long long), ctx.stream));
 
     trace_launch a {};
     a.blocks = device_blocks;
@@ -341,6 +360,7 @@ void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, c
     a.exit_keys = route_exits ? ctx.exit_keys.as<unsigned long long>() : nullptr;
     a.exit_count = exit_counter;
     a.steps = steps_counter;
+    a.next = pool_counter;
     launch_trace(ctx, a);
 
     // prune: packed offsets of every particle's kept vertices.
@@ -964,13 +984,7 @@ int32_t pars_gpu_curves_index(pars_gpu_context* ctx)
 {
   return guarded(ctx, [&] {
     auto& c = ctx->curves;
-    c.indices.reserve(sizeof(int) * (std::size_t)std::max<long long>(c.vertex_total, 1));
-    for (auto& b : c.batches)
-    {
-      b.index_offset = b.vertex_offset;
-      b.index_count = launch_index_generate(*ctx, c.vertices.as<const float4>() + b.vertex_offset, b.vertex_count,
-                                            c.indices.as<int>() + b.index_offset);
-    }
+    index_batches(*ctx, c);
     c.indexed = true;
     c.colored = false;
   });
@@ -982,11 +996,7 @@ int32_t pars_gpu_curves_color(pars_gpu_context* ctx, int32_t mode, float paramet
     auto& c = ctx->curves;
     if (!c.indexed) throw error(PARS_ERR_STATE, "curves must be indexed before they are coloured");
     PARS_REQUIRE(mode >= PARS_COLOR_HSL_CONSTANT_S && mode <= PARS_COLOR_RGB, "unknown colour mode");
-    c.colors.reserve(sizeof(float4) * (std::size_t)std::max<long long>(c.vertex_total, 1));
-    PARS_CUDA(cudaMemsetAsync(c.colors.get(), 0, sizeof(float4) * c.vertex_total, ctx->stream));
-    for (auto& b : c.batches)
-      launch_color_generate(*ctx, c.vertices.as<const float4>() + b.vertex_offset, c.indices.as<const int>() + b.index_offset,
-                            b.index_count, mode, parameter, c.colors.as<float4>() + b.vertex_offset);
+    color_batches(*ctx, c, std::vector<color_spec>(c.batches.size(), color_spec{mode, parameter}));
     c.colored = true;
   });
 }

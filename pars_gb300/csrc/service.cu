@@ -127,6 +127,10 @@ struct pars_gpu_service
   std::map<std::string, int>           dataset_index;
   bool                                 stopping = false;
   bool                                 spilling = false;
+  // instrumentation: per-kernel CUDA-event totals of all lanes and wall time
+  // of each batch phase, collected while profile is set
+  bool                                 profile = false;
+  std::map<std::string, pars::profile_entry> profile_totals;
   int64_t                              next_ticket = 1;
   int                                  running_batches = 0;
 };
@@ -171,6 +175,27 @@ void allocate_result(pars_gpu_service& svc, pars_gpu_context& c, request& r, std
   r.result_bytes = bytes;
 }
 
+// Wall time of the phases of one batch, recorded when the service profiles:
+// mark() drains the lane's stream and books the time since the previous mark.
+struct phase_clock
+{
+  pars_gpu_service&      svc;
+  pars_gpu_context&      c;
+  bool                   on;
+  clock_type::time_point t = clock_type::now();
+  void mark(const char* name)
+  {
+    if (!on) return;
+    cudaStreamSynchronize(c.stream);
+    const auto now = clock_type::now();
+    std::lock_guard<std::mutex> lock(svc.mutex);
+    auto& e = svc.profile_totals[name];
+    e.milliseconds += std::chrono::duration<double, std::milli>(now - t).count();
+    e.launches += 1;
+    t = now;
+  }
+};
+
 // Returns a request's device result to the pool (stream-ordered on `stream`).
 void free_result(request& r, cudaStream_t stream)
 {
@@ -196,6 +221,7 @@ void copy_result(pars_gpu_service& svc, const request& r, std::size_t offset, vo
 // per request (pipeline::execute_ftle, pars/source/pipeline.cpp:345-409).
 void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std::shared_ptr<request>>& batch)
 {
+  phase_clock clock {svc, c, c.profile};
   std::vector<batch_job_device> jobs;
   std::vector<device_buffer> flows;
   std::vector<int> shapes;
@@ -233,7 +259,9 @@ void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std:
     j.end_steps = nullptr;
     jobs.push_back(j);
   }
+  clock.mark("ftle.setup");
   const auto steps = run_batch(c, jobs, -1);
+  clock.mark("ftle.advect");
   for (std::size_t k = 0; k < batch.size(); ++k)
   {
     request& r = *batch[k];
@@ -249,6 +277,7 @@ void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std:
     launch_ftle(c, fv, time == 0.0f ? 1.0 : double(time), r.ftle_mode, reinterpret_cast<float*>(r.result));
   }
   PARS_CUDA(cudaStreamSynchronize(c.stream));
+  clock.mark("ftle.field");
   for (auto& f : flows) recycle_buffer(c, std::move(f));
 }
 
@@ -256,6 +285,7 @@ void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std:
 // index and colour per batch (pipeline::execute, pipeline.cpp:107-260).
 void run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std::shared_ptr<request>>& batch, int stage_mode)
 {
+  phase_clock clock {svc, c, c.profile};
   std::vector<trace_block> blocks;
   std::vector<step_rule> rules;
   std::vector<long long> block_count;
@@ -312,25 +342,22 @@ void run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vecto
   device_rules.reserve(sizeof(step_rule) * rules.size());
   PARS_CUDA(cudaMemcpyAsync(device_blocks.get(), blocks.data(), sizeof(trace_block) * blocks.size(), cudaMemcpyHostToDevice, c.stream));
   PARS_CUDA(cudaMemcpyAsync(device_rules.get(), rules.data(), sizeof(step_rule) * rules.size(), cudaMemcpyHostToDevice, c.stream));
+  clock.mark("streamlines.seed");
   pars_gpu_trace_summary summary {};
   trace_rounds(c, blocks, device_blocks.as<const trace_block>(), total, block_count, block_max, rules[0], false, &summary,
                device_rules.as<const step_rule>());
 
+  clock.mark("streamlines.trace");
   auto& curves = c.curves;
-  curves.indices.reserve(sizeof(int) * (std::size_t)std::max<long long>(curves.vertex_total, 1));
-  curves.colors.reserve(sizeof(float4) * (std::size_t)std::max<long long>(curves.vertex_total, 1));
-  if (curves.vertex_total > 0)
-    PARS_CUDA(cudaMemsetAsync(curves.colors.get(), 0, sizeof(float4) * curves.vertex_total, c.stream));
+  // index and colour every request's batches together, each with its mode
+  index_batches(c, curves);
+  std::vector<color_spec> specs;
+  specs.reserve(curves.batches.size());
   for (auto& b : curves.batches)
-  {
-    request& r = *batch[b.rank];
-    b.index_offset = b.vertex_offset;
-    b.index_count = launch_index_generate(c, curves.vertices.as<const float4>() + b.vertex_offset, b.vertex_count,
-                                          curves.indices.as<int>() + b.index_offset);
-    launch_color_generate(c, curves.vertices.as<const float4>() + b.vertex_offset, curves.indices.as<const int>() + b.index_offset,
-                          b.index_count, r.color_mode, r.s.color_generation_free_parameter, curves.colors.as<float4>() + b.vertex_offset);
-  }
+    specs.push_back(color_spec{batch[b.rank]->color_mode, batch[b.rank]->s.color_generation_free_parameter});
+  color_batches(c, curves, specs);
   curves.indexed = curves.colored = true;
+  clock.mark("streamlines.index_color");
   // Each request's curve batches move (device to device) into its own result.
   std::vector<std::size_t> span_of(curves.batches.size());
   for (std::size_t i = 0; i < curves.batches.size(); ++i)
@@ -363,6 +390,7 @@ void run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vecto
                                 sizeof(int32_t) * b.index_count, cudaMemcpyDeviceToDevice, c.stream));
   }
   PARS_CUDA(cudaStreamSynchronize(c.stream));
+  clock.mark("streamlines.results");
   // Steps per request: each curve holds its seed, one vertex per step and the
   // termination vertex (remaining_iterations >= 2; one block, one round).
   for (std::size_t k = 0; k < batch.size(); ++k)
@@ -450,6 +478,7 @@ void worker(pars_gpu_service* svc, int lane)
       }
       svc->in_use += reserved;
       ++svc->running_batches;
+      c.profile = svc->profile;
     }
     bool ok = true;
     try
@@ -464,7 +493,25 @@ void worker(pars_gpu_service* svc, int lane)
       for (auto& r : batch) { free_result(*r, c.stream); r->result_bytes = 0; r->spans.clear(); }
       cudaStreamSynchronize(c.stream);
     }
-    try { trim_lane(*svc, c); } catch (const std::exception&) {}
+    {
+      phase_clock clock {*svc, c, c.profile};
+      try { trim_lane(*svc, c); } catch (const std::exception&) {}
+      clock.mark("lane.trim");
+    }
+    if (c.profile)
+    {
+      std::map<std::string, profile_entry> kernels;
+      try { take_profile(c, kernels); } catch (const std::exception&) {}
+      std::lock_guard<std::mutex> lock(svc->mutex);
+      for (auto& k : kernels)
+      {
+        svc->profile_totals[k.first].milliseconds += k.second.milliseconds;
+        svc->profile_totals[k.first].launches += k.second.launches;
+      }
+      auto& b = svc->profile_totals[kind == ftle ? "batches.ftle" : "batches.streamlines"];
+      b.launches += 1;
+      b.milliseconds += double(batch.size());   // requests in these batches
+    }
     {
       std::lock_guard<std::mutex> lock(svc->mutex);
       svc->in_use -= reserved;
@@ -787,6 +834,26 @@ int32_t pars_gpu_service_release(pars_gpu_service* svc, int64_t ticket)
       }
       svc->work.notify_all();
     }
+  });
+}
+
+int32_t pars_gpu_service_profile_enable(pars_gpu_service* svc, int32_t enable)
+{
+  return service_guard(svc, [&] {
+    std::lock_guard<std::mutex> lock(svc->mutex);
+    svc->profile = enable != 0;
+    if (svc->profile) svc->profile_totals.clear();
+  });
+}
+
+int32_t pars_gpu_service_profile_get(pars_gpu_service* svc, const char* name, double* milliseconds, int64_t* count)
+{
+  return service_guard(svc, [&] {
+    PARS_REQUIRE(name, "name is required");
+    std::lock_guard<std::mutex> lock(svc->mutex);
+    auto it = svc->profile_totals.find(name);
+    if (milliseconds) *milliseconds = it == svc->profile_totals.end() ? 0.0 : it->second.milliseconds;
+    if (count) *count = it == svc->profile_totals.end() ? 0 : it->second.launches;
   });
 }
 

@@ -1,10 +1,13 @@
-// Streamline tracing kernels: one thread per particle runs the reference's
-// per-particle loop (particle_tracer.cpp:258-336) and writes its slot range of
-// the padded vertex layout; a warp per particle then prunes invalid vertices
-// (particle_tracer.cpp:402-409) into the packed curve buffer.  Particles that
-// leave their block are pushed onto a device exit queue (warp ballot + one
-// atomic per warp), then stably sorted by (destination block, source order) to
-// form the next round's per-block particle lists (particle_tracer.cpp:376-393).
+// Streamline tracing kernels: a lane at a time runs the reference's
+// per-particle loop (particle_tracer.cpp:258-336) for one particle and writes
+// its slot range of the padded vertex layout; a warp per particle then prunes
+// invalid vertices (particle_tracer.cpp:402-409) into the packed curve buffer.
+// Particles that leave their block are pushed onto a device exit queue (one
+// atomic per exiting particle), then stably sorted by (destination block,
+// source order) to form the next round's per-block particle lists
+// (particle_tracer.cpp:376-393).
+#include <algorithm>
+
 #include <cub/cub.cuh>
 
 #include "context.hpp"
@@ -15,100 +18,142 @@ namespace
 {
 constexpr unsigned full_mask = 0xffffffffu;
 
+// One persistent launch per round.  Warps take pools of particles from a
+// device counter; a lane whose particle has ended takes the next particle of
+// the pool at once (warp ballot + prefix), so lanes do not idle while the rest
+// of the warp finishes longer curves.  Every particle writes only its own slot
+// range, its counts and (when it leaves the block) an exit-queue entry keyed
+// by its index, so the result does not depend on which lane traced it.
 // FROZEN = true: the reference's scheme and FP32 operation order (bit-exact).
 // FROZEN = false: re-sampled stages, consistent cell weights, compensated
 // position accumulation.
 template <bool FROZEN>
-__global__ void __launch_bounds__(256) trace_kernel(const trace_launch a)
+__global__ void __launch_bounds__(128) trace_kernel(const trace_launch a, int pool_size)
 {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = i < a.count;
-  unsigned int steps = 0;
-  bool exits = false;
-  float4 exit_position = make_float4(0.f, 0.f, 0.f, 0.f);
-  int exit_remaining = 0, exit_block = 0;
+  const int lane = threadIdx.x & 31;
+  const unsigned lanes_below = (1u << lane) - 1u;
+  const float4 term = termination_vertex();
+  // warp-uniform pool state
+  long long pool_next = 0, pool_end = 0;
+  bool exhausted = false;
+  unsigned int steps = 0;            // this lane's steps, all particles
+  // the lane's particle
+  bool alive = false;
+  long long i = 0;
+  int it = 0, N = 0, written = 0, kept = 0, block = 0;
+  float4 last = make_float4(0.f, 0.f, 0.f, 0.f);
+  float3 lo = make_float3(0.f, 0.f, 0.f);
+  corner_cache cache;
+  field_view f {};
+  step_rule rule {};
+  float4* out = nullptr;
 
-  if (active)
+  for (;;)
   {
-    const int block = a.block_of ? a.block_of[i] : 0;
-    const field_view f = a.blocks[block].field;
-    const step_rule rule = a.block_rules ? a.block_rules[block] : a.rule;
-    const float4* record = reinterpret_cast<const float4*>(a.particles + i);
-    float4 last = record[0];
-    const int N = __float_as_int(record[1].x);   // remaining_iterations
-    const slot_layout L = a.block_slots[block];
-    float4* out = a.slots + L.origin + i * L.stride;
-    out[0] = last;
-    int written = 1;
-    int kept = is_invalid_vertex(last) ? 0 : 1;
-    const float4 term = termination_vertex();
-    float3 lo = make_float3(0.0f, 0.0f, 0.0f);
-    corner_cache cache;
-    for (int it = 1; it < N; ++it)
+    unsigned need = __ballot_sync(full_mask, !alive);
+    if (need && !exhausted)
     {
-      if (it == N - 1) { out[it] = term; ++written; ++kept; break; }
-      float3 v;
-      bool inside;
-      if (FROZEN) inside = sample_inside(f, last, v);
-      else        inside = sample_start(f, cache, last, v);
-      if (!inside)
+      // ---- refill idle lanes ---------------------------------------------------
+      while (need)
       {
-        out[it] = term; ++written; ++kept;
-        if (a.route_exits)
+        if (pool_next < pool_end)
         {
-          const int face = exit_face(f, last, a.blocks[block].neighbor);
-          if (face >= 0)
+          const long long s = pool_next + __popc(need & lanes_below);
+          if (!alive && s < pool_end)
           {
-            exits = true;
-            exit_position = last;
-            exit_remaining = N - it;
-            exit_block = a.blocks[block].neighbor[face];
+            i = s;
+            block = a.block_of ? a.block_of[i] : 0;
+            f = a.blocks[block].field;
+            rule = a.block_rules ? a.block_rules[block] : a.rule;
+            const float4* record = reinterpret_cast<const float4*>(a.particles + i);
+            last = record[0];
+            N = __float_as_int(record[1].x);   // remaining_iterations
+            const slot_layout L = a.block_slots[block];
+            out = a.slots + L.origin + i * L.stride;
+            out[0] = last;
+            written = 1;
+            kept = is_invalid_vertex(last) ? 0 : 1;
+            lo = make_float3(0.f, 0.f, 0.f);
+            cache = corner_cache();
+            it = 1;
+            alive = true;
+          }
+          pool_next = min(pool_end, pool_next + (long long)__popc(need));
+          need = __ballot_sync(full_mask, !alive);
+          continue;
+        }
+        long long p = 0;
+        if (lane == 0) p = (long long)atomicAdd(a.next, (unsigned long long)pool_size);
+        p = __shfl_sync(full_mask, p, 0);
+        if (p >= a.count) { exhausted = true; break; }
+        pool_next = p;
+        pool_end = min(p + pool_size, a.count);
+      }
+    }
+    if (need == full_mask) break;   // every lane idle, and the pools are exhausted
+
+    // ---- one iteration of the reference's per-particle loop -------------------
+    if (alive)
+    {
+      bool finish = false;
+      if (it >= N) finish = true;                                   // remaining_iterations <= 1
+      else if (it == N - 1) { out[it] = term; ++written; ++kept; finish = true; }
+      else
+      {
+        float3 v;
+        bool inside;
+        if (FROZEN) inside = sample_inside(f, last, v);
+        else        inside = sample_start(f, cache, last, v);
+        if (!inside)
+        {
+          out[it] = term; ++written; ++kept; finish = true;
+          if (a.route_exits)
+          {
+            const int face = exit_face(f, last, a.blocks[block].neighbor);
+            if (face >= 0)
+            {
+              // the exit queue is sorted by (destination, source index)
+              // afterwards, so its slots may be taken in any order
+              const unsigned int slot = atomicAdd(a.exit_count, 1u);
+              pars_particle p;
+              p.position[0] = last.x; p.position[1] = last.y; p.position[2] = last.z; p.position[3] = last.w;
+              p.remaining_iterations = N - it;
+              p.vector_field_index = -1;
+              p.original_rank = 0;
+              p.original_voxel[0] = p.original_voxel[1] = p.original_voxel[2] = 0;
+              p.padding[0] = p.padding[1] = 0;
+              const int destination = a.blocks[block].neighbor[face];
+              a.exit_particles[slot] = p;
+              a.exit_keys[slot] = ((unsigned long long)destination << 40) | (unsigned long long)i;
+            }
           }
         }
-        break;
+        else if (is_zero(v)) { out[it] = term; ++written; ++kept; finish = true; }
+        else
+        {
+          float4 next;
+          if (FROZEN) next = frozen_step(rule, last, v);
+          else { next = last; resampled_step_cached(f, cache, rule, next, lo, v); }
+          out[it] = next;
+          ++written;
+          kept += is_invalid_vertex(next) ? 0 : 1;
+          last = next;
+          ++steps;
+          ++it;
+        }
       }
-      if (is_zero(v)) { out[it] = term; ++written; ++kept; break; }
-      float4 next;
-      if (FROZEN) next = frozen_step(rule, last, v);
-      else { next = last; resampled_step_cached(f, cache, rule, next, lo, v); }
-      out[it] = next;
-      ++written;
-      kept += is_invalid_vertex(next) ? 0 : 1;
-      last = next;
-      ++steps;
+      if (finish)
+      {
+        a.written[i] = written;
+        a.kept[i] = kept;
+        alive = false;
+      }
     }
-    a.written[i] = written;
-    a.kept[i] = kept;
   }
 
   // Warp-aggregated step count.
   const unsigned int warp_steps = __reduce_add_sync(full_mask, steps);
-  const int lane = threadIdx.x & 31;
   if (lane == 0 && warp_steps) atomicAdd(a.steps, (unsigned long long)warp_steps);
-
-  // Warp ballot + prefix: one atomic reserves the warp's exit slots.
-  const unsigned mask = __ballot_sync(full_mask, exits);
-  if (mask)
-  {
-    unsigned int base = 0;
-    const int leader = __ffs(mask) - 1;
-    if (lane == leader) base = atomicAdd(a.exit_count, (unsigned int)__popc(mask));
-    base = __shfl_sync(full_mask, base, leader);
-    if (exits)
-    {
-      const unsigned int slot = base + __popc(mask & ((1u << lane) - 1u));
-      pars_particle p;
-      p.position[0] = exit_position.x; p.position[1] = exit_position.y;
-      p.position[2] = exit_position.z; p.position[3] = exit_position.w;
-      p.remaining_iterations = exit_remaining;
-      p.vector_field_index = -1;
-      p.original_rank = 0;
-      p.original_voxel[0] = p.original_voxel[1] = p.original_voxel[2] = 0;
-      p.padding[0] = p.padding[1] = 0;
-      a.exit_particles[slot] = p;
-      a.exit_keys[slot] = ((unsigned long long)exit_block << 40) | (unsigned long long)i;
-    }
-  }
 }
 
 // One warp per particle: copy its written slots, minus invalid vertices, to
@@ -203,13 +248,23 @@ unsigned int grid_for(long long work, int threads)
 void launch_trace(pars_gpu_context& ctx, const trace_launch& a)
 {
   if (a.count <= 0) return;
-  // Small particle counts: narrow blocks so that the work spreads over all SMs.
-  int threads = 128;
-  if (a.count <= 152LL * 128) threads = 32;
-  else if (a.count <= 152LL * 256) threads = 64;
+  const void* kernel = a.rule.frozen ? (const void*)trace_kernel<true> : (const void*)trace_kernel<false>;
+  int& per_sm = ctx.trace_ctas_per_sm[a.rule.frozen ? 0 : 1];
+  if (ctx.sm_count <= 0) PARS_CUDA(cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, ctx.device));
+  if (per_sm < 0) PARS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0));
+  const int sms = ctx.sm_count;
+  const long long resident_warps = (long long)std::max(per_sm, 1) * sms * 4;
+  // Pools of 256 particles when every resident warp gets several; otherwise
+  // one particle per lane, spread over as many SMs as possible (narrow CTAs)
+  // because small launches are latency-bound.
+  const int pool = a.count >= resident_warps * 256 * 2 ? 256 : 32;
+  const long long warps = std::min(resident_warps, (a.count + pool - 1) / pool);
+  const int threads = warps >= 4LL * sms ? 128 : 32;
+  const unsigned grid = (unsigned)((warps * 32 + threads - 1) / threads);
   launch_scope scope(ctx, "trace_streamlines");
-  if (a.rule.frozen) trace_kernel<true><<<grid_for(a.count, threads), threads, 0, ctx.stream>>>(a);
-  else               trace_kernel<false><<<grid_for(a.count, threads), threads, 0, ctx.stream>>>(a);
+  int pool_size = pool;
+  void* args[] = {(void*)&a, (void*)&pool_size};
+  PARS_CUDA(cudaLaunchKernel(kernel, grid, threads, args, 0, ctx.stream));
 }
 
 void launch_compact_vertices(pars_gpu_context& ctx, const float4* slots, const slot_layout* block_slots, const int* block_of,

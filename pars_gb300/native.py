@@ -131,6 +131,8 @@ SIGNATURES = {
     "pars_gpu_service_result_batch": [_P, _I64, _I64, ctypes.POINTER(_I64), ctypes.POINTER(_I64), _P, _P, _P],
     "pars_gpu_service_result_ftle": [_P, _I64, _P],
     "pars_gpu_service_release": [_P, _I64],
+    "pars_gpu_service_profile_enable": [_P, _I32],
+    "pars_gpu_service_profile_get": [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)],
     "pars_gpu_profile_enable": [_P, _I32],
     "pars_gpu_profile_reset": [_P],
     "pars_gpu_profile_get": [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)],
@@ -527,3 +529,13 @@ class Service:
 
     def release(self, ticket):
         self._check(self.lib.pars_gpu_service_release(self.handle, ticket), "pars_gpu_service_release")
+
+    def profile_enable(self, on=True):
+        self._check(self.lib.pars_gpu_service_profile_enable(self.handle, 1 if on else 0), "pars_gpu_service_profile_enable")
+
+    def profile_get(self, name):
+        """(milliseconds, count) of a kernel or batch phase (see pars_gpu.h)."""
+        ms, n = ctypes.c_double(), _I64()
+        self._check(self.lib.pars_gpu_service_profile_get(self.handle, name.encode(), ctypes.byref(ms), ctypes.byref(n)),
+                    "pars_gpu_service_profile_get")
+        return ms.value, n.value

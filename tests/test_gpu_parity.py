@@ -229,6 +229,28 @@ def test_frozen_flow_map_matches_reference_fixture(ctx, key, iterations, scale, 
     ctx.release_field(h)
 
 
+@pytest.mark.parametrize("mode", ["hsv_constant_s", "hsl_constant_l", "hsl_constant_s", "hsv_constant_v"])
+def test_hue_colours_match_the_reference_arithmetic_on_random_tangents(ctx, port, mode):
+    """500,000 random segments (a third of them nearly parallel to an axis,
+    where acos is ill-conditioned): the GPU colours against the CPU
+    restatement, which calls the host libm's atan2f / acosf as the reference
+    does.  Both sides use FP32 atan2 / acos, so they agree to a few ulps."""
+    rng = np.random.default_rng(11)
+    n = 500_000
+    steps = rng.normal(size=(n, 3)) * np.float32(0.01)
+    axis = rng.integers(0, 3, n // 3)
+    steps[: n // 3] *= 1e-4
+    steps[np.arange(n // 3), axis] = rng.choice([-0.01, 0.01], n // 3)
+    v = np.zeros((n + 1, 4), np.float32)
+    v[1:, :3] = np.cumsum(steps, axis=0).astype(np.float32) + np.float32(3.0)
+    idx = np.arange(n, dtype=np.int32)
+    got = ctx.color_generate(v, idx, mode, 0.75)
+    expected = port.color_generate(v, idx, mode, 0.75)
+    diff = np.abs(got[:n].astype(np.float64) - expected[:n].astype(np.float64)).max()
+    print(f"{mode}: max colour difference {diff:.3g}")
+    assert diff <= HSX_TOLERANCE
+
+
 def test_stage_buffers_match_reference_fixture(ctx):
     g = golden("index_color.npz")
     v = g["vertices"]
