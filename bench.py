@@ -49,6 +49,7 @@ def parse_args():
     p.add_argument("--requests", type=int, default=300, help="served workload: number of requests")
     p.add_argument("--serve-arms", default="plain,batched", help="served workload: arms to run (plain, batched)")
     p.add_argument("--serve-loads", default="0.5,0.9", help="served workload: offered loads as fractions of saturation")
+    p.add_argument("--serve-lanes", type=int, default=1, help="served workload: service lanes of the batched arm")
     p.add_argument("--workload", choices=["ftle", "streamlines", "domain", "pathlines", "serve"], default="ftle",
                    help="ftle: the headline line; the others print one line for the other workloads")
     return p.parse_args()
@@ -300,7 +301,8 @@ def run_serve(args):
               field from (pinned) host memory, seeds + trace + index + colour
               or flow map + FTLE, download every result buffer into pinned
               host buffers, release.
-    batched : the service (2 lanes, batches of up to 64, datasets resident):
+    batched : the service (one lane by default, batches of up to 64, datasets
+              resident; the other lane count is timed at saturation beside it):
               requests are submitted as reference `settings` messages at their
               Poisson arrival times; a client thread collects each finished
               request's buffers into the same pinned host buffers.
@@ -490,17 +492,26 @@ def run_serve(args):
         ctx.close()
 
     if "batched" in arms:
-        svc = native.Service(0, budget_bytes=160 << 30, lanes=2, max_batch=64)
-        for d, (xyz, offset, size, spacing) in zip(ds, device_fields):
-            svc.add_dataset_device(d["name"], xyz.data_ptr(), (d["edge"],) * 3, offset, size, spacing)
-        torch.cuda.synchronize()
-        del device_fields
-        torch.cuda.empty_cache()
-        for m in messages[:8]:                       # warm-up
-            t = svc.submit(m)
-            svc.wait(t)
-            collect(svc, t)
+        def service(lanes):
+            svc = native.Service(0, budget_bytes=160 << 30, lanes=lanes, max_batch=64)
+            for d, (xyz, offset, size, spacing) in zip(ds, device_fields):
+                svc.add_dataset_device(d["name"], xyz.data_ptr(), (d["edge"],) * 3, offset, size, spacing)
+            torch.cuda.synchronize()
+            for m in messages[:8]:                   # warm-up
+                t = svc.submit(m)
+                svc.wait(t)
+                collect(svc, t)
+            return svc
+
+        svc = service(args.serve_lanes)
         results["batched"] = summarise(run_service, svc)
+        results["batched"]["lanes"] = args.serve_lanes
+        svc.close()
+        # the other lane count, at saturation only
+        other = 2 if args.serve_lanes == 1 else 1
+        svc = service(other)
+        span, _, _ = run_service(svc, None)
+        results["batched"][f"saturation_requests_per_s_lanes{other}"] = len(messages) / span
         svc.close()
     line = {"workload": f"served_{len(messages)}: {len(messages)} requests (seed 4), 70% streamlines / 30% FTLE on "
                         f"{len(ds)} ABC / double-gyre fields (edge 64-512), seeds 1k-2M (streamlines <= 16384), "

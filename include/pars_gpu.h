@@ -302,8 +302,10 @@ int32_t pars_gpu_batch_tuned   (pars_gpu_context* context, int32_t job_class, in
  * ones copy fastest) and releases the request; held results count against
  * the budget.  When no queued request fits and no batch is running, held
  * results move to host memory, so a client that collects results in any order
- * cannot stall the queue.  Each lane keeps at most min(budget / (4 lanes),
- * 8 GiB) of scratch between batches. */
+ * cannot stall the queue.  Between batches the lanes keep up to budget / 4 of
+ * scratch in total and the result pool up to budget / 4 of freed results, so
+ * steady batches do not allocate: the service uses up to 1.5 x the budget of
+ * device memory, plus the datasets. */
 typedef struct pars_gpu_service pars_gpu_service;
 
 /* The scalar fields of a decoded `settings` message (strings truncated). */

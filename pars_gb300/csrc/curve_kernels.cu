@@ -70,6 +70,42 @@ __device__ __forceinline__ float4 hue_to_rgba(float hue)
                      1.0f);
 }
 
+// Error-free sum (Knuth's TwoSum): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+  s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+// float(sqrt(double(x)^2 + double(y)^2 + double(z)^2)) — the reference's
+// radius (coordinates.hpp:8-16: std::pow(float, int) promotes to double) — in
+// FP32 arithmetic: each square as an exact pair (product + FMA remainder), the
+// six terms summed error-free into hi + lo, then the correctly rounded square
+// root of hi + lo, decided against the rounding midpoints of sqrtf(hi) with the
+// exact remainder hi - r0^2.  It can differ from the double evaluation only
+// where the root lies within about 2^-46 of a float midpoint (no case in
+// 300,000 random and axis-aligned tangents).
+__device__ __forceinline__ float reference_radius(float x, float y, float z)
+{
+  const float px = __fmul_rn(x, x), py = __fmul_rn(y, y), pz = __fmul_rn(z, z);
+  const float ex = __fmaf_rn(x, x, -px), ey = __fmaf_rn(y, y, -py), ez = __fmaf_rn(z, z, -pz);
+  float s1, t1, s2, t2;
+  two_sum(px, py, s1, t1);
+  two_sum(s1, pz, s2, t2);
+  float lo = __fadd_rn(__fadd_rn(__fadd_rn(t1, t2), __fadd_rn(ex, ey)), ez);
+  const float hi = __fadd_rn(s2, lo);
+  lo = __fsub_rn(lo, __fsub_rn(hi, s2));
+  const float r0 = __fsqrt_rn(hi);
+  const float rho = __fadd_rn(__fmaf_rn(-r0, r0, hi), lo);          // (hi + lo) - r0^2
+  const float up = __int_as_float(__float_as_int(r0) + 1), dn = __int_as_float(__float_as_int(r0) - 1);
+  const float u = __fsub_rn(up, r0), ud = __fsub_rn(r0, dn);       // ulps above and below r0
+  // (r0 + u/2)^2 - r0^2 = r0 u + u^2/4, (r0 - ud/2)^2 - r0^2 = -r0 ud + ud^2/4
+  if (rho > __fadd_rn(__fmul_rn(r0, u), __fmul_rn(__fmul_rn(u, u), 0.25f))) return up;
+  if (rho < __fadd_rn(__fmul_rn(-r0, ud), __fmul_rn(__fmul_rn(ud, ud), 0.25f))) return dn;
+  return r0;
+}
+
 __device__ float4 color_of(const float4& a, const float4& b, int mode, float parameter)
 {
   // (b - a).normalized() as Eigen evaluates it for Vector4f.
@@ -82,13 +118,11 @@ __device__ float4 color_of(const float4& a, const float4& b, int mode, float par
   }
   if (mode == PARS_COLOR_RGB) return make_float4(fabsf(d.x), fabsf(d.z), fabsf(d.y), 1.0f);
 
-  // to_spherical (coordinates.hpp:8-16): std::pow(float, int) promotes to
-  // double, so the radius is the FP64 root rounded to FP32, exactly as the
-  // reference computes it (acos near +-1 would magnify any difference in it).
-  // atan2 and acos are the FP32 functions, as the reference calls them (the
-  // host libm's atan2f / acosf there, CUDA's here: within 3 and 2 ulp).
-  const double tx = d.x, ty = d.y, tz = d.z;
-  const float radius = __double2float_rn(__dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(tx, tx), __dmul_rn(ty, ty)), __dmul_rn(tz, tz))));
+  // to_spherical (coordinates.hpp:8-16): the radius as the reference rounds
+  // it (acos near +-1 would magnify any difference in it); atan2 and acos are
+  // the FP32 functions, as the reference calls them (the host libm's atan2f /
+  // acosf there, CUDA's here: within 3 and 2 ulp).
+  const float radius = reference_radius(d.x, d.y, d.z);
   float s1 = atan2f(d.y, d.x);
   float s2 = acosf(__fdiv_rn(d.z, radius));
   // correct_range (color_generator.cpp:41-54).

@@ -7,11 +7,13 @@
 //  * admission: a request enters a batch only while the device memory that
 //    the running batches are estimated to need, plus the results held on the
 //    device, stays within the budget;
-//  * results: each request's buffers (vertices, colours, indices or the FTLE
-//    field) stay on the device, in one allocation from the service's
-//    stream-ordered pool, until the client copies them into its own host
-//    buffers and releases the request; when no queued request fits and no
-//    batch runs, held results move to host memory so that the queue moves on;
+//  * results: each request's buffers stay on the device until the client
+//    copies them into its own host buffers and releases the request — an FTLE
+//    field in one allocation from the service's stream-ordered pool, curves
+//    as ranges of their batch's curve buffers, which the batch's requests share
+//    (no device copy) and which return to the lanes once all have let go; when
+//    no queued request fits and no batch runs, held results move to host
+//    memory so that the queue moves on;
 //  * batching: a lane takes every queued request of the same kind that fits
 //    (up to max_batch) and runs them as one launch — FTLE requests as jobs of
 //    the persistent batched advection engine, streamline requests as blocks of
@@ -53,9 +55,26 @@ struct dataset
   float       offset[3], size[3], spacing[3];
 };
 
+// One integral_curves batch of a streamline request: its place in the
+// request's own layout (vertex_offset, index_offset; used once its buffers
+// have moved to host memory) and in the batch's shared curve store.
 struct curve_span
 {
   int64_t vertex_offset, vertex_count, index_offset, index_count;
+  int64_t store_vertex_offset, store_index_offset;
+};
+
+// The curve buffers of one streamline batch (vertices, colours, packed
+// indices), shared by the batch's requests until the last of them is
+// released or moved to host memory; the buffers then return to the service's
+// free list, from which the lanes take their next curve buffers.
+struct curve_store
+{
+  pars_gpu_service* svc = nullptr;
+  device_buffer     vertices, colors, indices;
+  std::size_t       counted = 0;   // bytes booked against the budget
+  std::size_t bytes() const { return vertices.bytes() + colors.bytes() + indices.bytes(); }
+  ~curve_store();
 };
 
 struct request
@@ -75,13 +94,15 @@ struct request
   clock_type::time_point submitted, started, finished;
   long long          steps = 0;
   int                ftle_shape[3] = {0, 0, 0};
-  // Results: one device allocation from the service's pool, laid out as
-  // vertices (float4 [vertex_total]), colours (float4 [vertex_total]) and
-  // indices (int32 [index_total]) for streamlines, float [voxels] for FTLE;
-  // `spilled` holds the same bytes once they were moved to host memory.
+  // Results.  FTLE: one device allocation from the service's pool (float
+  // [voxels]).  Streamlines: sub-ranges of the batch's curve store.  Once
+  // moved to host memory, `spilled` holds them in the request's own layout:
+  // vertices (float4 [vertex_total]), colours (float4 [vertex_total]), indices
+  // (int32 [index_total]) — or the FTLE values.
   std::mutex              result_mutex;
   char*                   result = nullptr;
   std::size_t             result_bytes = 0;
+  std::shared_ptr<curve_store> store;
   std::vector<char>       spilled;
   bool                    released = false;
   std::vector<curve_span> spans;   // streamlines: one per integral_curves batch
@@ -116,6 +137,8 @@ struct pars_gpu_service
   int                                  max_batch = 64;
   cudaMemPool_t                        pool = nullptr;  // result allocations
   cudaStream_t                         copy_stream = nullptr;   // client copies and frees
+  std::vector<std::unique_ptr<pars::curve_store>> spare_stores;   // curve buffers for the next batches
+  std::size_t                          spare_bytes = 0;
   pars_gpu_context*                    owner = nullptr;
   std::vector<pars_gpu_context*>       lanes;
   std::vector<std::thread>             workers;
@@ -139,6 +162,40 @@ namespace pars
 {
 namespace
 {
+// Keeps spare curve buffers up to a quarter of the budget; frees the rest.
+void return_buffers(pars_gpu_service& svc, std::unique_ptr<curve_store> spare)
+{
+  std::lock_guard<std::mutex> lock(svc.mutex);
+  const std::size_t bytes = spare->bytes();
+  if (svc.spare_bytes + bytes <= svc.budget / 4)
+  {
+    svc.spare_bytes += bytes;
+    svc.spare_stores.push_back(std::move(spare));
+  }
+}
+
+// The last request of the batch let go: unbook the bytes and keep the buffers
+// for the lanes (no work on them is pending: the batch's stream was drained
+// and every client copy is synchronised before its call returns).
+curve_store::~curve_store()
+{
+  if (!svc) return;
+  auto spare = std::make_unique<curve_store>();
+  spare->vertices = std::move(vertices);
+  spare->colors = std::move(colors);
+  spare->indices = std::move(indices);
+  if (counted)
+  {
+    {
+      std::lock_guard<std::mutex> lock(svc->mutex);
+      svc->held -= std::min(svc->held, counted);
+      svc->in_use -= std::min(svc->in_use, counted);
+    }
+    svc->work.notify_all();
+  }
+  return_buffers(*svc, std::move(spare));
+}
+
 // Device bytes a request needs while it runs (a conservative estimate).
 std::size_t estimate_bytes(const request& r, const dataset& d)
 {
@@ -283,9 +340,30 @@ void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std:
 
 // Streamline requests: one block per request in one tracing round loop, then
 // index and colour per batch (pipeline::execute, pipeline.cpp:107-260).
-void run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std::shared_ptr<request>>& batch, int stage_mode)
+// Returns the bytes of the batch's curve store (shared by its requests).
+std::size_t run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std::shared_ptr<request>>& batch, int stage_mode)
 {
   phase_clock clock {svc, c, c.profile};
+  std::size_t store_bytes = 0;
+  // curve buffers left by an earlier batch whose requests have all let go
+  {
+    std::unique_ptr<curve_store> spare;
+    {
+      std::lock_guard<std::mutex> lock(svc.mutex);
+      if (!svc.spare_stores.empty() && !c.curves.vertices.get())
+      {
+        spare = std::move(svc.spare_stores.back());
+        svc.spare_stores.pop_back();
+        svc.spare_bytes -= std::min(svc.spare_bytes, spare->bytes());
+      }
+    }
+    if (spare)
+    {
+      c.curves.vertices = std::move(spare->vertices);
+      c.curves.colors = std::move(spare->colors);
+      c.curves.indices = std::move(spare->indices);
+    }
+  }
   std::vector<trace_block> blocks;
   std::vector<step_rule> rules;
   std::vector<long long> block_count;
@@ -358,37 +436,26 @@ void run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vecto
   color_batches(c, curves, specs);
   curves.indexed = curves.colored = true;
   clock.mark("streamlines.index_color");
-  // Each request's curve batches move (device to device) into its own result.
-  std::vector<std::size_t> span_of(curves.batches.size());
-  for (std::size_t i = 0; i < curves.batches.size(); ++i)
+  // The curve buffers become the batch's store, shared by its requests: each
+  // request keeps its batches' ranges in it (no copy); the lane takes fresh
+  // buffers for its next batch.
+  auto store = std::make_shared<curve_store>();
+  store->svc = &svc;
+  store->vertices = std::move(curves.vertices);
+  store->colors = std::move(curves.colors);
+  store->indices = std::move(curves.indices);
+  for (const auto& b : curves.batches)
   {
-    const auto& b = curves.batches[i];
     request& r = *batch[b.rank];
-    span_of[i] = r.spans.size();
-    r.spans.push_back({r.vertex_total, b.vertex_count, r.index_total, b.index_count});
+    r.spans.push_back({r.vertex_total, b.vertex_count, r.index_total, b.index_count, b.vertex_offset, b.index_offset});
     r.vertex_total += b.vertex_count;
     r.index_total += b.index_count;
+    r.store = store;
   }
-  for (auto& rp : batch)
-    allocate_result(svc, c, *rp, std::size_t(rp->vertex_total) * 2 * sizeof(float4) + std::size_t(rp->index_total) * sizeof(int32_t));
-  for (std::size_t i = 0; i < curves.batches.size(); ++i)
-  {
-    const auto& b = curves.batches[i];
-    request& r = *batch[b.rank];
-    const curve_span& s = r.spans[span_of[i]];
-    char* colors = r.result + sizeof(float4) * r.vertex_total;
-    char* indices = r.result + 2 * sizeof(float4) * r.vertex_total;
-    if (b.vertex_count)
-    {
-      PARS_CUDA(cudaMemcpyAsync(r.result + sizeof(float4) * s.vertex_offset, curves.vertices.as<float4>() + b.vertex_offset,
-                                sizeof(float4) * b.vertex_count, cudaMemcpyDeviceToDevice, c.stream));
-      PARS_CUDA(cudaMemcpyAsync(colors + sizeof(float4) * s.vertex_offset, curves.colors.as<float4>() + b.vertex_offset,
-                                sizeof(float4) * b.vertex_count, cudaMemcpyDeviceToDevice, c.stream));
-    }
-    if (b.index_count)
-      PARS_CUDA(cudaMemcpyAsync(indices + sizeof(int32_t) * s.index_offset, curves.indices.as<int>() + b.index_offset,
-                                sizeof(int32_t) * b.index_count, cudaMemcpyDeviceToDevice, c.stream));
-  }
+  store_bytes = store->bytes();
+  curves.batches.clear();
+  curves.vertex_total = curves.index_total = 0;
+  curves.indexed = curves.colored = false;
   PARS_CUDA(cudaStreamSynchronize(c.stream));
   clock.mark("streamlines.results");
   // Steps per request: each curve holds its seed, one vertex per step and the
@@ -396,10 +463,12 @@ void run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vecto
   for (std::size_t k = 0; k < batch.size(); ++k)
     batch[k]->steps = batch[k]->s.seed_generation_iterations >= 2 ? std::max(0LL, (long long)batch[k]->vertex_total - 2 * block_count[k]) : 0;
   (void)summary;
+  return store_bytes;
 }
 
 // Moves every finished request's device result to host memory (the queue is
-// blocked on held results and no batch runs); returns the bytes freed.
+// blocked on held results and no batch runs); returns the FTLE bytes freed
+// (curve stores unbook themselves when their last request lets go).
 std::size_t spill_results(pars_gpu_service& svc, pars_gpu_context& c, const std::vector<std::shared_ptr<request>>& finished)
 {
   std::size_t freed = 0;
@@ -407,7 +476,33 @@ std::size_t spill_results(pars_gpu_service& svc, pars_gpu_context& c, const std:
   {
     request& r = *rp;
     std::lock_guard<std::mutex> lock(r.result_mutex);
-    if (!r.result || r.released) continue;
+    if (r.released) continue;
+    if (r.store)
+    {
+      // the request's own layout: vertices, colours, indices
+      const std::size_t colors = sizeof(float4) * r.vertex_total, indices = 2 * colors;
+      r.spilled.resize(indices + sizeof(int32_t) * r.index_total);
+      for (const auto& sp : r.spans)
+      {
+        if (sp.vertex_count)
+        {
+          PARS_CUDA(cudaMemcpyAsync(r.spilled.data() + sizeof(float4) * sp.vertex_offset,
+                                    r.store->vertices.as<float4>() + sp.store_vertex_offset, sizeof(float4) * sp.vertex_count,
+                                    cudaMemcpyDeviceToHost, c.stream));
+          PARS_CUDA(cudaMemcpyAsync(r.spilled.data() + colors + sizeof(float4) * sp.vertex_offset,
+                                    r.store->colors.as<float4>() + sp.store_vertex_offset, sizeof(float4) * sp.vertex_count,
+                                    cudaMemcpyDeviceToHost, c.stream));
+        }
+        if (sp.index_count)
+          PARS_CUDA(cudaMemcpyAsync(r.spilled.data() + indices + sizeof(int32_t) * sp.index_offset,
+                                    r.store->indices.as<int32_t>() + sp.store_index_offset, sizeof(int32_t) * sp.index_count,
+                                    cudaMemcpyDeviceToHost, c.stream));
+      }
+      PARS_CUDA(cudaStreamSynchronize(c.stream));
+      r.store.reset();
+      continue;
+    }
+    if (!r.result) continue;
     r.spilled.resize(r.result_bytes);
     if (r.result_bytes)
       PARS_CUDA(cudaMemcpyAsync(r.spilled.data(), r.result, r.result_bytes, cudaMemcpyDeviceToHost, c.stream));
@@ -481,16 +576,17 @@ void worker(pars_gpu_service* svc, int lane)
       c.profile = svc->profile;
     }
     bool ok = true;
+    std::size_t store_bytes = 0;
     try
     {
       if (kind == ftle) run_ftle_batch(*svc, c, batch);
-      else run_streamline_batch(*svc, c, batch, stage_mode);
+      else store_bytes = run_streamline_batch(*svc, c, batch, stage_mode);
     }
     catch (const error& e) { ok = false; for (auto& r : batch) fail(*r, e.status, e.what()); }
     catch (const std::exception& e) { ok = false; for (auto& r : batch) fail(*r, PARS_ERR_STATE, e.what()); }
     if (!ok)
     {
-      for (auto& r : batch) { free_result(*r, c.stream); r->result_bytes = 0; r->spans.clear(); }
+      for (auto& r : batch) { free_result(*r, c.stream); r->result_bytes = 0; r->spans.clear(); r->store.reset(); }
       cudaStreamSynchronize(c.stream);
     }
     {
@@ -517,6 +613,12 @@ void worker(pars_gpu_service* svc, int lane)
       svc->in_use -= reserved;
       for (auto& r : batch)
         if (r->result) { svc->in_use += r->result_bytes; svc->held += r->result_bytes; }
+      if (ok && store_bytes && !batch.empty() && batch[0]->store)
+      {
+        batch[0]->store->counted = store_bytes;
+        svc->in_use += store_bytes;
+        svc->held += store_bytes;
+      }
       --svc->running_batches;
       for (auto& r : batch) { r->state = done; r->finished = clock_type::now(); }
     }
@@ -599,17 +701,17 @@ int32_t pars_gpu_service_create(pars_gpu_service** service, int32_t device, int6
   if (!svc) return PARS_ERR_OUT_OF_MEMORY;
   svc->device = device;
   svc->budget = std::size_t(budget_bytes);
-  svc->lane_keep = std::min<std::size_t>(svc->budget / (4 * std::size_t(lanes)), std::size_t(8) << 30);
+  svc->lane_keep = svc->budget / (4 * std::size_t(lanes));
   svc->max_batch = max_batch;
   int32_t status = pars_gpu_create(&svc->owner, device);
   if (status == PARS_OK)
   {
-    // A pool that keeps up to lane_keep bytes of freed results for reuse.
+    // A pool that keeps up to a quarter of the budget of freed results mapped.
     cudaMemPoolProps props {};
     props.allocType = cudaMemAllocationTypePinned;
     props.location.type = cudaMemLocationTypeDevice;
     props.location.id = device;
-    uint64_t keep = svc->lane_keep;
+    uint64_t keep = svc->budget / 4;
     if (cudaSetDevice(device) != cudaSuccess || cudaMemPoolCreate(&svc->pool, &props) != cudaSuccess ||
         cudaMemPoolSetAttribute(svc->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess ||
         cudaStreamCreateWithFlags(&svc->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -648,13 +750,18 @@ int32_t pars_gpu_service_destroy(pars_gpu_service* svc)
   svc->work.notify_all();
   for (auto& t : svc->workers) t.join();
   cudaSetDevice(svc->device);
-  for (auto& t : svc->requests)
-  {
-    std::lock_guard<std::mutex> lock(t.second->result_mutex);
-    free_result(*t.second, svc->copy_stream);
-  }
+  std::vector<std::shared_ptr<request>> left;
+  for (auto& t : svc->requests) left.push_back(t.second);
   svc->requests.clear();
+  for (auto& r : left)
+  {
+    std::lock_guard<std::mutex> lock(r->result_mutex);
+    free_result(*r, svc->copy_stream);
+    r->store.reset();
+  }
+  left.clear();
   cudaStreamSynchronize(svc->copy_stream);
+  svc->spare_stores.clear();
   for (auto* c : svc->lanes) pars_gpu_destroy(c);
   pars_gpu_destroy(svc->owner);
   cudaStreamDestroy(svc->copy_stream);
@@ -771,10 +878,23 @@ int32_t pars_gpu_service_result_batch(pars_gpu_service* svc, int64_t ticket, int
     if (vertices) *vertices = s.vertex_count;
     if (indices) *indices = s.index_count;
     PARS_CUDA(cudaSetDevice(svc->device));
-    const std::size_t colors = sizeof(float4) * r->vertex_total, index_base = 2 * colors;
-    copy_result(*svc, *r, sizeof(float4) * s.vertex_offset, vertex_data, sizeof(float4) * s.vertex_count);
-    copy_result(*svc, *r, colors + sizeof(float4) * s.vertex_offset, color_data, sizeof(float4) * s.vertex_count);
-    copy_result(*svc, *r, index_base + sizeof(int32_t) * s.index_offset, index_data, sizeof(int32_t) * s.index_count);
+    if (r->store)
+    {
+      // straight from the batch's curve store
+      auto d2h = [&](void* out, const void* in, std::size_t bytes) {
+        if (out && bytes) PARS_CUDA(cudaMemcpyAsync(out, in, bytes, cudaMemcpyDeviceToHost, svc->copy_stream));
+      };
+      d2h(vertex_data, r->store->vertices.as<float4>() + s.store_vertex_offset, sizeof(float4) * s.vertex_count);
+      d2h(color_data, r->store->colors.as<float4>() + s.store_vertex_offset, sizeof(float4) * s.vertex_count);
+      d2h(index_data, r->store->indices.as<int32_t>() + s.store_index_offset, sizeof(int32_t) * s.index_count);
+    }
+    else
+    {
+      const std::size_t colors = sizeof(float4) * r->vertex_total, index_base = 2 * colors;
+      copy_result(*svc, *r, sizeof(float4) * s.vertex_offset, vertex_data, sizeof(float4) * s.vertex_count);
+      copy_result(*svc, *r, colors + sizeof(float4) * s.vertex_offset, color_data, sizeof(float4) * s.vertex_count);
+      copy_result(*svc, *r, index_base + sizeof(int32_t) * s.index_offset, index_data, sizeof(int32_t) * s.index_count);
+    }
     PARS_CUDA(cudaStreamSynchronize(svc->copy_stream));
   });
 }
@@ -823,6 +943,7 @@ int32_t pars_gpu_service_release(pars_gpu_service* svc, int64_t ticket)
         free_result(*r, svc->copy_stream);
         freed = r->result_bytes;
       }
+      r->store.reset();   // the last request of its batch hands the curve buffers back
       std::vector<char>().swap(r->spilled);
     }
     if (freed)

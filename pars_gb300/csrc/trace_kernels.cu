@@ -1,6 +1,6 @@
-// Streamline tracing kernels: a lane at a time runs the reference's
-// per-particle loop (particle_tracer.cpp:258-336) for one particle and writes
-// its slot range of the padded vertex layout; a warp per particle then prunes
+// Streamline tracing kernels: a lane runs the reference's per-particle loop
+// (particle_tracer.cpp:258-336) for one particle at a time and writes its slot
+// range of the padded vertex layout; a warp per particle then prunes
 // invalid vertices (particle_tracer.cpp:402-409) into the packed curve buffer.
 // Particles that leave their block are pushed onto a device exit queue (one
 // atomic per exiting particle), then stably sorted by (destination block,
@@ -18,142 +18,169 @@ namespace
 {
 constexpr unsigned full_mask = 0xffffffffu;
 
-// One persistent launch per round.  Warps take pools of particles from a
-// device counter; a lane whose particle has ended takes the next particle of
-// the pool at once (warp ballot + prefix), so lanes do not idle while the rest
-// of the warp finishes longer curves.  Every particle writes only its own slot
-// range, its counts and (when it leaves the block) an exit-queue entry keyed
-// by its index, so the result does not depend on which lane traced it.
+// The particle a lane traces.
+struct lane_particle
+{
+  long long    i = 0;
+  int          it = 0, N = 0, written = 0, kept = 0, block = 0;
+  float4       last = make_float4(0.f, 0.f, 0.f, 0.f);
+  float3       lo = make_float3(0.f, 0.f, 0.f);
+  corner_cache cache;
+  field_view   f {};
+  step_rule    rule {};
+  float4*      out = nullptr;
+};
+
+// Loads particle i and writes its seed vertex (slot 0).
+__device__ __forceinline__ void particle_start(const trace_launch& a, lane_particle& p, long long i)
+{
+  p.i = i;
+  p.block = a.block_of ? a.block_of[i] : 0;
+  p.f = a.blocks[p.block].field;
+  p.rule = a.block_rules ? a.block_rules[p.block] : a.rule;
+  const float4* record = reinterpret_cast<const float4*>(a.particles + i);
+  p.last = record[0];
+  p.N = __float_as_int(record[1].x);   // remaining_iterations
+  const slot_layout L = a.block_slots[p.block];
+  p.out = a.slots + L.origin + i * L.stride;
+  p.out[0] = p.last;
+  p.written = 1;
+  p.kept = is_invalid_vertex(p.last) ? 0 : 1;
+  p.lo = make_float3(0.f, 0.f, 0.f);
+  p.cache = corner_cache();
+  p.it = 1;
+}
+
+// One iteration of the reference's per-particle loop (particle_tracer.cpp:
+// 266-335); returns true when the particle has ended (its counts are then
+// stored, and a particle that left its block through a face with a neighbour
+// is pushed onto the exit queue with one atomic — the queue is sorted by
+// (destination, source index) afterwards, so slots may be taken in any order).
 // FROZEN = true: the reference's scheme and FP32 operation order (bit-exact).
 // FROZEN = false: re-sampled stages, consistent cell weights, compensated
 // position accumulation.
 template <bool FROZEN>
-__global__ void __launch_bounds__(128) trace_kernel(const trace_launch a, int pool_size)
+__device__ __forceinline__ bool particle_iteration(const trace_launch& a, lane_particle& p, unsigned int& steps)
+{
+  const float4 term = termination_vertex();
+  bool finish = false;
+  if (p.it >= p.N) finish = true;                                     // remaining_iterations <= 1
+  else if (p.it == p.N - 1) { p.out[p.it] = term; ++p.written; ++p.kept; finish = true; }
+  else
+  {
+    float3 v;
+    bool inside;
+    if (FROZEN) inside = sample_inside(p.f, p.last, v);
+    else        inside = sample_start(p.f, p.cache, p.last, v);
+    if (!inside)
+    {
+      p.out[p.it] = term; ++p.written; ++p.kept; finish = true;
+      if (a.route_exits)
+      {
+        const int face = exit_face(p.f, p.last, a.blocks[p.block].neighbor);
+        if (face >= 0)
+        {
+          const unsigned int slot = atomicAdd(a.exit_count, 1u);
+          pars_particle e;
+          e.position[0] = p.last.x; e.position[1] = p.last.y; e.position[2] = p.last.z; e.position[3] = p.last.w;
+          e.remaining_iterations = p.N - p.it;
+          e.vector_field_index = -1;
+          e.original_rank = 0;
+          e.original_voxel[0] = e.original_voxel[1] = e.original_voxel[2] = 0;
+          e.padding[0] = e.padding[1] = 0;
+          const int destination = a.blocks[p.block].neighbor[face];
+          a.exit_particles[slot] = e;
+          a.exit_keys[slot] = ((unsigned long long)destination << 40) | (unsigned long long)p.i;
+        }
+      }
+    }
+    else if (is_zero(v)) { p.out[p.it] = term; ++p.written; ++p.kept; finish = true; }
+    else
+    {
+      float4 next;
+      if (FROZEN) next = frozen_step(p.rule, p.last, v);
+      else { next = p.last; resampled_step_cached(p.f, p.cache, p.rule, next, p.lo, v); }
+      p.out[p.it] = next;
+      ++p.written;
+      p.kept += is_invalid_vertex(next) ? 0 : 1;
+      p.last = next;
+      ++steps;
+      ++p.it;
+    }
+  }
+  if (finish)
+  {
+    a.written[p.i] = p.written;
+    a.kept[p.i] = p.kept;
+  }
+  return finish;
+}
+
+__device__ __forceinline__ void add_steps(const trace_launch& a, unsigned int steps)
+{
+  const unsigned int warp_steps = __reduce_add_sync(full_mask, steps);
+  if ((threadIdx.x & 31) == 0 && warp_steps) atomicAdd(a.steps, (unsigned long long)warp_steps);
+}
+
+// One particle per thread: for launches with no more particles than resident
+// lanes, where refilling cannot help and warp votes would only add latency.
+template <bool FROZEN>
+__global__ void __launch_bounds__(128) trace_kernel(const trace_launch a)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned int steps = 0;
+  if (i < a.count)
+  {
+    lane_particle p;
+    particle_start(a, p, i);
+    while (!particle_iteration<FROZEN>(a, p, steps)) {}
+  }
+  add_steps(a, steps);
+}
+
+// Persistent: warps take pools of particles from a device counter, and a lane
+// whose particle has ended takes the next particle of the pool at once (warp
+// ballot + prefix), so lanes do not idle while the rest of the warp finishes
+// longer curves.  Every particle writes only its own slot range, its counts
+// and its exit-queue entry, so the result does not depend on which lane traced
+// it.
+template <bool FROZEN>
+__global__ void __launch_bounds__(128) trace_persistent_kernel(const trace_launch a, int pool_size)
 {
   const int lane = threadIdx.x & 31;
   const unsigned lanes_below = (1u << lane) - 1u;
-  const float4 term = termination_vertex();
-  // warp-uniform pool state
-  long long pool_next = 0, pool_end = 0;
+  long long pool_next = 0, pool_end = 0;   // warp-uniform
   bool exhausted = false;
-  unsigned int steps = 0;            // this lane's steps, all particles
-  // the lane's particle
+  unsigned int steps = 0;
   bool alive = false;
-  long long i = 0;
-  int it = 0, N = 0, written = 0, kept = 0, block = 0;
-  float4 last = make_float4(0.f, 0.f, 0.f, 0.f);
-  float3 lo = make_float3(0.f, 0.f, 0.f);
-  corner_cache cache;
-  field_view f {};
-  step_rule rule {};
-  float4* out = nullptr;
-
+  lane_particle p;
   for (;;)
   {
     unsigned need = __ballot_sync(full_mask, !alive);
     if (need && !exhausted)
     {
-      // ---- refill idle lanes ---------------------------------------------------
       while (need)
       {
         if (pool_next < pool_end)
         {
           const long long s = pool_next + __popc(need & lanes_below);
-          if (!alive && s < pool_end)
-          {
-            i = s;
-            block = a.block_of ? a.block_of[i] : 0;
-            f = a.blocks[block].field;
-            rule = a.block_rules ? a.block_rules[block] : a.rule;
-            const float4* record = reinterpret_cast<const float4*>(a.particles + i);
-            last = record[0];
-            N = __float_as_int(record[1].x);   // remaining_iterations
-            const slot_layout L = a.block_slots[block];
-            out = a.slots + L.origin + i * L.stride;
-            out[0] = last;
-            written = 1;
-            kept = is_invalid_vertex(last) ? 0 : 1;
-            lo = make_float3(0.f, 0.f, 0.f);
-            cache = corner_cache();
-            it = 1;
-            alive = true;
-          }
+          if (!alive && s < pool_end) { particle_start(a, p, s); alive = true; }
           pool_next = min(pool_end, pool_next + (long long)__popc(need));
           need = __ballot_sync(full_mask, !alive);
           continue;
         }
-        long long p = 0;
-        if (lane == 0) p = (long long)atomicAdd(a.next, (unsigned long long)pool_size);
-        p = __shfl_sync(full_mask, p, 0);
-        if (p >= a.count) { exhausted = true; break; }
-        pool_next = p;
-        pool_end = min(p + pool_size, a.count);
+        long long q = 0;
+        if (lane == 0) q = (long long)atomicAdd(a.next, (unsigned long long)pool_size);
+        q = __shfl_sync(full_mask, q, 0);
+        if (q >= a.count) { exhausted = true; break; }
+        pool_next = q;
+        pool_end = min(q + pool_size, a.count);
       }
     }
     if (need == full_mask) break;   // every lane idle, and the pools are exhausted
-
-    // ---- one iteration of the reference's per-particle loop -------------------
-    if (alive)
-    {
-      bool finish = false;
-      if (it >= N) finish = true;                                   // remaining_iterations <= 1
-      else if (it == N - 1) { out[it] = term; ++written; ++kept; finish = true; }
-      else
-      {
-        float3 v;
-        bool inside;
-        if (FROZEN) inside = sample_inside(f, last, v);
-        else        inside = sample_start(f, cache, last, v);
-        if (!inside)
-        {
-          out[it] = term; ++written; ++kept; finish = true;
-          if (a.route_exits)
-          {
-            const int face = exit_face(f, last, a.blocks[block].neighbor);
-            if (face >= 0)
-            {
-              // the exit queue is sorted by (destination, source index)
-              // afterwards, so its slots may be taken in any order
-              const unsigned int slot = atomicAdd(a.exit_count, 1u);
-              pars_particle p;
-              p.position[0] = last.x; p.position[1] = last.y; p.position[2] = last.z; p.position[3] = last.w;
-              p.remaining_iterations = N - it;
-              p.vector_field_index = -1;
-              p.original_rank = 0;
-              p.original_voxel[0] = p.original_voxel[1] = p.original_voxel[2] = 0;
-              p.padding[0] = p.padding[1] = 0;
-              const int destination = a.blocks[block].neighbor[face];
-              a.exit_particles[slot] = p;
-              a.exit_keys[slot] = ((unsigned long long)destination << 40) | (unsigned long long)i;
-            }
-          }
-        }
-        else if (is_zero(v)) { out[it] = term; ++written; ++kept; finish = true; }
-        else
-        {
-          float4 next;
-          if (FROZEN) next = frozen_step(rule, last, v);
-          else { next = last; resampled_step_cached(f, cache, rule, next, lo, v); }
-          out[it] = next;
-          ++written;
-          kept += is_invalid_vertex(next) ? 0 : 1;
-          last = next;
-          ++steps;
-          ++it;
-        }
-      }
-      if (finish)
-      {
-        a.written[i] = written;
-        a.kept[i] = kept;
-        alive = false;
-      }
-    }
+    if (alive && particle_iteration<FROZEN>(a, p, steps)) alive = false;
   }
-
-  // Warp-aggregated step count.
-  const unsigned int warp_steps = __reduce_add_sync(full_mask, steps);
-  if (lane == 0 && warp_steps) atomicAdd(a.steps, (unsigned long long)warp_steps);
+  add_steps(a, steps);
 }
 
 // One warp per particle: copy its written slots, minus invalid vertices, to
@@ -248,23 +275,30 @@ unsigned int grid_for(long long work, int threads)
 void launch_trace(pars_gpu_context& ctx, const trace_launch& a)
 {
   if (a.count <= 0) return;
-  const void* kernel = a.rule.frozen ? (const void*)trace_kernel<true> : (const void*)trace_kernel<false>;
-  int& per_sm = ctx.trace_ctas_per_sm[a.rule.frozen ? 0 : 1];
+  const bool frozen = a.rule.frozen != 0;
+  const void* persistent = frozen ? (const void*)trace_persistent_kernel<true> : (const void*)trace_persistent_kernel<false>;
+  int& per_sm = ctx.trace_ctas_per_sm[frozen ? 0 : 1];
   if (ctx.sm_count <= 0) PARS_CUDA(cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, ctx.device));
-  if (per_sm < 0) PARS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0));
+  if (per_sm < 0) PARS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent, 128, 0));
   const int sms = ctx.sm_count;
   const long long resident_warps = (long long)std::max(per_sm, 1) * sms * 4;
-  // Pools of 256 particles when every resident warp gets several; otherwise
-  // one particle per lane, spread over as many SMs as possible (narrow CTAs)
-  // because small launches are latency-bound.
-  const int pool = a.count >= resident_warps * 256 * 2 ? 256 : 32;
-  const long long warps = std::min(resident_warps, (a.count + pool - 1) / pool);
-  const int threads = warps >= 4LL * sms ? 128 : 32;
-  const unsigned grid = (unsigned)((warps * 32 + threads - 1) / threads);
   launch_scope scope(ctx, "trace_streamlines");
+  if (a.count <= resident_warps * 32)
+  {
+    // every lane gets at most one particle: one per thread, narrow CTAs for
+    // small counts so that the work spreads over all SMs
+    const int threads = a.count <= 128LL * sms ? 32 : 128;
+    const unsigned grid = (unsigned)((a.count + threads - 1) / threads);
+    if (frozen) trace_kernel<true><<<grid, threads, 0, ctx.stream>>>(a);
+    else        trace_kernel<false><<<grid, threads, 0, ctx.stream>>>(a);
+    return;
+  }
+  // pools of 256 particles when every resident warp gets several, else 32
+  const int pool = a.count >= resident_warps * 256 * 2 ? 256 : 32;
+  const unsigned grid = (unsigned)std::min<long long>((long long)per_sm * sms, (a.count / pool + 4) / 4 + 1);
   int pool_size = pool;
   void* args[] = {(void*)&a, (void*)&pool_size};
-  PARS_CUDA(cudaLaunchKernel(kernel, grid, threads, args, 0, ctx.stream));
+  PARS_CUDA(cudaLaunchKernel(persistent, grid, 128, args, 0, ctx.stream));
 }
 
 void launch_compact_vertices(pars_gpu_context& ctx, const float4* slots, const slot_layout* block_slots, const int* block_of,
