@@ -47,7 +47,8 @@ def parse_args():
     p.add_argument("--iterations", type=int, default=501)
     p.add_argument("--cpu-sample", type=int, default=1048576, help="seeds in the CPU baseline's bounded sample")
     p.add_argument("--requests", type=int, default=300, help="served workload: number of requests")
-    p.add_argument("--serve-arms", default="plain,batched", help="served workload: arms to run (plain, batched)")
+    p.add_argument("--serve-arms", default="plain,batched,cpu", help="served workload: arms to run (plain, batched, cpu)")
+    p.add_argument("--serve-cpu-seconds", type=float, default=15.0, help="served workload: CPU reference arm's sample length")
     p.add_argument("--serve-loads", default="0.5,0.9", help="served workload: offered loads as fractions of saturation")
     p.add_argument("--serve-lanes", type=int, default=1, help="served workload: service lanes of the batched arm")
     p.add_argument("--workload", choices=["ftle", "streamlines", "domain", "pathlines", "serve"], default="ftle",
@@ -293,6 +294,43 @@ def run_pathlines(args):
     ctx.close()
 
 
+def run_cpu_reference(specs, host_fields, seconds):
+    """The served stream through the reference's algorithm on the host cores:
+    the oracle port (frozen-velocity RK4 in FP32 with the reference's operation
+    order, OpenMP over particles on every host thread), request by request in
+    stream order -- seeds, trace, indices and hsv_constant_s colours for a
+    streamline request; flow map and FTLE for an FTLE request -- until
+    `seconds` of work have been done.  Returns the sample's rates."""
+    import oracle
+    from pars_gb300 import workloads
+    port = oracle.port()
+    f32 = np.float32
+    fields = {}
+    done, steps, vertices, t0 = 0, 0, 0, time.perf_counter()
+    for s in specs:
+        if time.perf_counter() - t0 >= seconds:
+            break
+        if s["dataset"] not in fields:
+            xyz, offset, size, spacing = host_fields[s["dataset"]]
+            fields[s["dataset"]] = workloads.Field(xyz.numpy(), offset, spacing, size)
+        f = fields[s["dataset"]]
+        stride = (f.spacing * f32(s["stride"])).astype(f32)
+        if s["kind"] == "streamlines":
+            seeds = port.seed_generate(f.offset, f.size, stride, s["iterations"])
+            curves = port.trace_single(f, seeds, 2, s["step"], "hsv_constant_s", 0.75)
+            steps += curves.steps
+            vertices += sum(len(b["vertices"]) for b in curves.batches)
+        else:
+            flow, n = port.flow_map(f, s["iterations"], float(f32(1.0) / f32(s["stride"])), 2, s["step"])
+            port.ftle_fp64(flow, stride, float(f32(s["step"]) * f32(s["iterations"])))
+            steps += n
+        done += 1
+    dt = time.perf_counter() - t0
+    return {"requests_per_s": done / dt, "particle_steps_per_s": steps / dt, "cores": port.max_threads(),
+            "kind": "port", "sample": f"the stream's first {done} requests ({steps} RK4 steps, {vertices} curve "
+                                      f"vertices) in {dt:.1f} s"}
+
+
 def run_serve(args):
     """The served mixed stream, end to end from host memory to host memory.
 
@@ -306,6 +344,8 @@ def run_serve(args):
               requests are submitted as reference `settings` messages at their
               Poisson arrival times; a client thread collects each finished
               request's buffers into the same pinned host buffers.
+    cpu     : the reference's algorithm on the host cores (run_cpu_reference),
+              a bounded sample of the same stream from the same host fields.
     Latency runs from a request's arrival to its results being in host
     memory.  Both paths at saturation (every request present at t = 0) and at
     offered loads of 50 % and 90 % of their own saturation throughput."""
@@ -513,6 +553,9 @@ def run_serve(args):
         span, _, _ = run_service(svc, None)
         results["batched"][f"saturation_requests_per_s_lanes{other}"] = len(messages) / span
         svc.close()
+
+    if "cpu" in arms:
+        results["cpu_reference"] = run_cpu_reference(specs, host_fields, args.serve_cpu_seconds)
     line = {"workload": f"served_{len(messages)}: {len(messages)} requests (seed 4), 70% streamlines / 30% FTLE on "
                         f"{len(ds)} ABC / double-gyre fields (edge 64-512), seeds 1k-2M (streamlines <= 16384), "
                         "200-2000 RK4 steps, Poisson arrivals; results collected into pinned host buffers",
@@ -521,6 +564,9 @@ def run_serve(args):
     if "plain" in results and "batched" in results:
         line["throughput_ratio_at_saturation"] = (results["batched"]["saturation_requests_per_s"] /
                                                   results["plain"]["saturation_requests_per_s"])
+    if "batched" in results and "cpu_reference" in results:
+        line["particle_steps_ratio_batched_to_cpu"] = (results["batched"]["saturation_particle_steps_per_s"] /
+                                                       results["cpu_reference"]["particle_steps_per_s"])
     print(json.dumps(line))
 
 

@@ -292,12 +292,16 @@ vec4 color_of(const vec4& tangent, int mode, float parameter)
 }
 
 // Colours the reference never writes stay NaN (it resizes without initialising).
+// Parallel over line segments like the reference's tbb::parallel_for: the
+// indices ascend, so the extra write to index + 1 (a curve's last vertex)
+// never meets another segment's write.
 void generate_colors(batch& b, int mode, float parameter)
 {
   const float nan = std::numeric_limits<float>::quiet_NaN();
   b.colors.assign(b.vertices.size(), vec4{{nan, nan, nan, nan}});
-  const std::size_t n = b.indices.size();
-  for (std::size_t i = 0; i < n; ++i)
+  const long long n = static_cast<long long>(b.indices.size());
+  #pragma omp parallel for schedule(static)
+  for (long long i = 0; i < n; ++i)
   {
     const int32_t index = b.indices[i];
     const vec4 tangent = normalized_difference(b.vertices[index], b.vertices[index + 1]);

@@ -170,6 +170,29 @@ def test_batches_split_like_compute_round_info(ctx, port):
     ctx.release_field(h)
 
 
+def test_many_particles_trace_like_the_reference(ctx, port):
+    """1,700,000 particles (more than the resident lanes take at one particle
+    each, so the persistent tracing kernel hands out pools of 256 and lanes
+    refill), remaining_iterations spread over 1..40 so that lanes finish at
+    different times: bit-exact curves, indices and rgb colours against the CPU
+    restatement of the reference."""
+    from pars_gb300 import workloads as W
+    f = W.abc_field(24)
+    rng = np.random.default_rng(13)
+    n = 1_700_000
+    seeds = np.zeros(n, port_dtype())
+    seeds["position"][:, :3] = rng.uniform(-0.2, 6.5, (n, 3)).astype(np.float32)
+    seeds["remaining_iterations"] = rng.integers(1, 41, n)
+    seeds["vector_field_index"] = -1
+    h = ctx.upload_field(f)
+    s = ctx.trace(h, seeds, 2, 0, 0.05)
+    got = gpu_curves(ctx, s, "rgb")
+    expected = port.trace_single(f, seeds, 2, 0.05, "rgb", 0.5)
+    assert s["steps"] > 0
+    compare(got, expected.batches)
+    ctx.release_field(h)
+
+
 def port_dtype():
     import oracle
     return oracle.PARTICLE_DTYPE

@@ -171,3 +171,45 @@ def test_released_results_are_gone(service):
     with pytest.raises(native.ParsGpuError) as e:
         service.ftle(t)
     assert e.value.status == -5
+
+
+def test_shared_curve_buffers_outlive_released_neighbours(service):
+    """Streamline requests of one batch share its curve buffers: releasing some
+    of them, and running more batches meanwhile, leaves the others' results
+    intact; once all are released the buffers serve later batches."""
+    from pars_gb300.requests import encode_settings
+    reqs = [r for r in _requests() if r["mode"] == "streamlines"][:4]
+    tickets = [service.submit(encode_settings(r)) for r in reqs]
+    for t in tickets:
+        assert service.wait(t) == 2
+    first = [service.streamlines(t) for t in tickets]
+    for t in tickets[:3]:
+        service.release(t)
+    for r in reqs[:3]:                       # more batches while the fourth is held
+        t = service.submit(encode_settings(r))
+        assert service.wait(t) == 2
+        service.release(t)
+    assert _same(service.streamlines(tickets[3]), first[3], "streamlines")
+    service.release(tickets[3])
+    again = [service.submit(encode_settings(r)) for r in reqs]
+    for t, expected in zip(again, first):
+        assert service.wait(t) == 2
+        assert _same(service.streamlines(t), expected, "streamlines")
+        service.release(t)
+
+
+def test_profile_reports_kernels_and_phases(service):
+    from pars_gb300.requests import encode_settings
+    service.profile_enable(True)
+    reqs = _requests()
+    tickets = [service.submit(encode_settings(r)) for r in reqs]
+    for t in tickets:
+        assert service.wait(t) == 2
+        service.release(t)
+    for name in ("trace_streamlines", "color_generate", "batch_advect", "ftle_fused",
+                 "streamlines.trace", "streamlines.index_color", "ftle.advect"):
+        ms, count = service.profile_get(name)
+        assert count >= 1 and ms > 0.0, name
+    requests, batches = service.profile_get("batches.streamlines")   # (requests held, batches)
+    assert requests == 6.0 and 1 <= batches <= 6
+    service.profile_enable(False)
