@@ -71,7 +71,7 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
   time_axis ta {};
   float h = 0.0f;
   int rk4 = 1, max_steps = 0;
-  double time_begin = 0.0;
+  slice_clock clock {};
 
   for (;;)
   {
@@ -125,7 +125,7 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
         job_steps = 0;
         job = pj;
         const batch_job_device& J = jobs[job];
-        f = J.field; ta = J.time; h = J.rule.h; rk4 = J.rule.rk4; max_steps = J.max_steps; time_begin = J.time_begin;
+        f = J.field; ta = J.time; h = J.rule.h; rk4 = J.rule.rk4; max_steps = J.max_steps; clock = J.clock;
         cache = lane_cache<UNSTEADY>();
       }
       pending = -1;
@@ -156,11 +156,11 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
         {
           step_rule r;
           r.frozen = 0; r.rk4 = rk4; r.h = h; r.count = 0;
-          // FP64 time of this step: start + n h (no accumulated rounding)
-          const double t = time_begin + double(steps) * double(h);
+          // time of this step: start + n h, from n (no accumulated rounding)
+          const slice_time t = step_time(clock, steps);
           const float3 k1 = sample_unsteady_cached(f, ta, cache.k, pos.x, pos.y, pos.z, t);
           if (is_zero(k1)) retire = true;
-          else { unsteady_step(f, ta, cache.k, r, pos, lo, k1, t); ++steps; ++job_steps; }
+          else { unsteady_step(f, ta, clock, cache.k, r, pos, lo, k1, t); ++steps; ++job_steps; }
         }
       }
       else

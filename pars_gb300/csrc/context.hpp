@@ -316,6 +316,7 @@ struct batch_job_device
   step_rule           rule;
   int                 max_steps;
   double              time_begin;
+  slice_clock         clock;          // set by execute_batch from time, time_begin and rule.h
   long long           seed_count;
   const float4*       seeds;          // explicit seeds, or nullptr for the lattice
   float               ox, oy, oz, sx, sy, sz;

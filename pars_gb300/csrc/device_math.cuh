@@ -326,9 +326,13 @@ __device__ __forceinline__ void resampled_step_cached(const field_view& f, corne
 // ---- Unsteady fields (pathlines) ----------------------------------------------
 // An unsteady field is a sequence of `nt` slices of one grid, slice k holding
 // the velocity at time t0 + k * slice_dt; between slices the velocity is
-// linear in time.  Times are carried in FP64 (the step counter times h plus
-// the start time, so no rounding accumulates); the time weight enters the
-// FP32 blend.
+// linear in time.  Time is carried as the slice coordinate s = (t - t0) /
+// slice_dt.  Step n of a job starting at time t_b samples s at
+// s_b + (n + c) * D (c = 0, 1/2, 1; D = h / slice_dt): computed from n every
+// step (no accumulated rounding) as an unevaluated pair of floats (hi + lo,
+// about 44 bits), which keeps the arithmetic on the FP32 pipes (a GB300 SM
+// issues FP64 at 1/64 of its FP32 rate); the time weight enters the FP32
+// blend.
 struct time_axis
 {
   int       nt;              // number of slices (1 = steady)
@@ -337,14 +341,68 @@ struct time_axis
   double    inv_slice_dt;    // 1 / slice spacing in time
 };
 
-__device__ __forceinline__ void slice_of(const time_axis& ta, double t, int& slice, float& wt)
+// A job's clock: s_b and D as float pairs (set on the host from FP64 values).
+struct slice_clock
+{
+  float s_hi = 0.0f, s_lo = 0.0f;   // slice coordinate at the job's start time
+  float d_hi = 0.0f, d_lo = 0.0f;   // slice coordinate per step
+};
+
+inline slice_clock make_slice_clock(const time_axis& ta, double time_begin, float h)
+{
+  slice_clock c;
+  const double s = (time_begin - ta.t0) * ta.inv_slice_dt, d = double(h) * ta.inv_slice_dt;
+  c.s_hi = float(s); c.s_lo = float(s - double(c.s_hi));
+  c.d_hi = float(d); c.d_lo = float(d - double(c.d_hi));
+  return c;
+}
+
+struct slice_time { float hi, lo; };
+
+// Knuth's TwoSum: a + b = s + e exactly.
+__device__ __forceinline__ void two_sum_rn(float a, float b, float& s, float& e)
+{
+  s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+// s_b + n * D.  n is split into a high part (multiple of 4096) and a low part
+// so that both convert to float exactly for any int n >= 0; their products
+// with d_hi are split into rounded value and exact error by an FMA.
+__device__ __forceinline__ slice_time step_time(const slice_clock& c, int n)
+{
+  const float nh = __int2float_rn(n & ~0xfff), nl = __int2float_rn(n & 0xfff);
+  const float p1 = __fmul_rn(nh, c.d_hi), e1 = fmaf(nh, c.d_hi, -p1);
+  const float p2 = __fmul_rn(nl, c.d_hi), e2 = fmaf(nl, c.d_hi, -p2);
+  float a, b, a2, b2;
+  two_sum_rn(c.s_hi, p1, a, b);
+  two_sum_rn(a, p2, a2, b2);
+  const float lo = (b + b2) + (e1 + e2) + fmaf(__int2float_rn(n), c.d_lo, c.s_lo);
+  return {a2, lo};
+}
+
+// t + c * D for c = 1/2 or 1 (c * d_hi and c * d_lo are exact).
+__device__ __forceinline__ slice_time advance_time(const slice_time& t, const slice_clock& c, float frac)
+{
+  float a, b;
+  two_sum_rn(t.hi, __fmul_rn(frac, c.d_hi), a, b);
+  return {a, b + (t.lo + __fmul_rn(frac, c.d_lo))};
+}
+
+// The slice pair around time t and the weight of the later slice: floor(s)
+// and s - floor(s) of s = hi + lo; before slice 0 the first slice, after the
+// last one the last slice.
+__device__ __forceinline__ void slice_of(const time_axis& ta, const slice_time& t, int& slice, float& wt)
 {
   if (ta.nt <= 1) { slice = 0; wt = 0.0f; return; }
-  const double s = (t - ta.t0) * ta.inv_slice_dt;
-  const double fs = floor(s);
-  if (!(fs >= 0.0)) { slice = 0; wt = 0.0f; }
-  else if (fs >= double(ta.nt - 1)) { slice = ta.nt - 2; wt = 1.0f; }
-  else { slice = int(fs); wt = float(s - fs); }
+  float fs = floorf(t.hi);
+  float w = __fadd_rn(__fsub_rn(t.hi, fs), t.lo);   // hi - floor(hi) is exact
+  if (w < 0.0f) { fs -= 1.0f; w = __fadd_rn(w, 1.0f); }
+  else if (w >= 1.0f) { fs += 1.0f; w = __fsub_rn(w, 1.0f); }
+  if (!(fs >= 0.0f)) { slice = 0; wt = 0.0f; }
+  else if (fs >= float(ta.nt - 1)) { slice = ta.nt - 2; wt = 1.0f; }
+  else { slice = int(fs); wt = w; }
 }
 
 // The corners of one cell in the two slices around the current time;
@@ -356,7 +414,7 @@ struct corner_cache2
 };
 
 __device__ __forceinline__ float3 sample_unsteady_cached(const field_view& fv, const time_axis& ta, corner_cache2& k,
-                                                         float px, float py, float pz, double t)
+                                                         float px, float py, float pz, const slice_time& t)
 {
   axis_cell cx = cell_consistent(px, fv.ox, fv.hx, fv.inv_hx), cy = cell_consistent(py, fv.oy, fv.hy, fv.inv_hy),
             cz = cell_consistent(pz, fv.oz, fv.hz, fv.inv_hz);
@@ -382,8 +440,9 @@ __device__ __forceinline__ float3 sample_unsteady_cached(const field_view& fv, c
 
 // One pathline step from (x, t): classical RK4 in space-time with re-sampled
 // stages at t, t + h/2, t + h/2, t + h, or the frozen rule (velocity at (x, t)).
-__device__ __forceinline__ void unsteady_step(const field_view& f, const time_axis& ta, corner_cache2& k, const step_rule& r,
-                                              float4& x, float3& lo, const float3& k1, double t)
+__device__ __forceinline__ void unsteady_step(const field_view& f, const time_axis& ta, const slice_clock& clock,
+                                              corner_cache2& k, const step_rule& r, float4& x, float3& lo,
+                                              const float3& k1, const slice_time& t)
 {
   if (r.frozen || !r.rk4)
   {
@@ -394,7 +453,7 @@ __device__ __forceinline__ void unsteady_step(const field_view& f, const time_ax
     return;
   }
   const float hh = 0.5f * r.h;
-  const double th = t + 0.5 * double(r.h), t1 = t + double(r.h);
+  const slice_time th = advance_time(t, clock, 0.5f), t1 = advance_time(t, clock, 1.0f);
   const float3 k2 = sample_unsteady_cached(f, ta, k, fmaf(hh, k1.x, x.x), fmaf(hh, k1.y, x.y), fmaf(hh, k1.z, x.z), th);
   const float3 k3 = sample_unsteady_cached(f, ta, k, fmaf(hh, k2.x, x.x), fmaf(hh, k2.y, x.y), fmaf(hh, k2.z, x.z), th);
   const float3 k4 = sample_unsteady_cached(f, ta, k, fmaf(r.h, k3.x, x.x), fmaf(r.h, k3.y, x.y), fmaf(r.h, k3.z, x.z), t1);

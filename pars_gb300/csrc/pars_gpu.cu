@@ -506,7 +506,11 @@ std::vector<unsigned long long> execute_batch(pars_gpu_context& ctx, std::vector
   const int steady = int(order.size());
   for (int j = 0; j < count; ++j) if (jobs[j].time.nt > 1) order.push_back(j);
   std::vector<batch_job_device> queue(count);
-  for (int k = 0; k < count; ++k) queue[k] = jobs[order[k]];
+  for (int k = 0; k < count; ++k)
+  {
+    queue[k] = jobs[order[k]];
+    queue[k].clock = make_slice_clock(queue[k].time, queue[k].time_begin, queue[k].rule.h);
+  }
   const int first[2] = {0, steady}, size[2] = {steady, count - steady};
 
   ctx.batch_jobs.reserve(sizeof(batch_job_device) * count);
