@@ -51,7 +51,7 @@ def parse_args():
     p.add_argument("--serve-cpu-seconds", type=float, default=15.0, help="served workload: CPU reference arm's sample length")
     p.add_argument("--serve-loads", default="0.5,0.9", help="served workload: offered loads as fractions of saturation")
     p.add_argument("--serve-lanes", type=int, default=1, help="served workload: service lanes of the batched arm")
-    p.add_argument("--workload", choices=["ftle", "streamlines", "domain", "pathlines", "serve"], default="ftle",
+    p.add_argument("--workload", choices=["ftle", "streamlines", "domain", "pathlines", "serve", "render"], default="ftle",
                    help="ftle: the headline line; the others print one line for the other workloads")
     return p.parse_args()
 
@@ -205,6 +205,77 @@ def run_streamlines(args):
                       "frozen_velocity_steps_per_s": out["frozen"], "ms_per_call_frozen": out["frozen_ms"],
                       "steps_per_call": ref.steps, "cpu_port_steps_per_s": cpu, "cpu_threads": port.max_threads()}))
     ctx.close()
+
+
+def run_render(args):
+    """The ray tracer (pars::ray_tracer's stage 6: set_integral_curves, trace,
+    serialize) on the benchmark generator's settings
+    (pars_benchmark_generator/source/main.cpp:7-28): image 1080 x 1920, one
+    iteration, streamline radius 0.1 voxel, camera looking along +z, curves
+    coloured hsv_constant_s 0.75.  Scenes: the 64^3 ABC streamlines (4096
+    seeds, <= 1000 RK4 steps, h = 0.01), the same with a stride-2 lattice
+    (32768 seeds), and the 64^3 scene with the field's normalised speed as the
+    volume.  One image = set_integral_curves (BVH build) + trace(1) +
+    serialize into host memory; the CPU restatement of the same shading on all
+    host threads is timed on each scene beside it."""
+    import oracle
+    from pars_gb300 import native, workloads
+    cfg = workloads.streamline_config()
+    f = cfg["field"]
+    ctx = native.Context(0)
+    h = ctx.upload_field(f)
+    port = oracle.port()
+    width, height = 1080, 1920
+    radius = float(np.float32(0.1) * f.spacing[0])
+    camera = ((float(np.pi), float(np.pi), -9.0), (0.0, 0.0, 1.0), (0.0, 1.0, 0.0))
+    speed = np.linalg.norm(f.xyz, axis=-1)
+    volume = ((speed / speed.max()).astype(np.float32), f.offset, f.spacing)
+    scenes = []
+    for name, stride, vol in (("streamlines_64", 4, None), ("streamlines_64_stride2", 2, None), ("streamlines_64_volume", 4, volume)):
+        seeds = ctx.seed_generate(f.offset, f.size, (f.spacing * np.float32(stride)).astype(np.float32), cfg["iterations"])
+        s = ctx.trace(h, seeds, native.RUNGE_KUTTA_4, native.STAGES_RESAMPLED, cfg["step"])
+        ctx.curves_index()
+        ctx.curves_color("hsv_constant_s", 0.75)
+        if vol is None:
+            ctx.ray_tracer_clear_volume()
+        else:
+            ctx.ray_tracer_set_volume(*vol)
+        ctx.ray_tracer_set_image_size(width, height)
+        ctx.ray_tracer_set_camera(*camera)
+
+        def image():
+            ctx.ray_tracer_set_integral_curves(radius)
+            ctx.ray_tracer_trace(1)
+            return ctx.ray_tracer_serialize()
+
+        for _ in range(max(args.warmup, 3)):
+            image()
+        ctx.profile_enable(True)
+        ctx.profile_reset()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rgba = image()
+        wall = (time.perf_counter() - t0) / args.steps
+        build_ms, _ = ctx.profile_get("bvh_build")
+        render_ms, _ = ctx.profile_get("render")
+        ctx.profile_enable(False)
+        batches = ctx.curves(s["batches"], vertices=True, colors=True, indices=True)
+        host = [(b["vertices"], b["colors"], b["indices"]) for b in batches]
+        segments = sum(len(b["indices"]) for b in batches)
+        c0 = time.perf_counter()
+        expected, _ = port.render(host, radius, camera, (width, height), frames=1, volume=vol)
+        cpu = time.perf_counter() - c0
+        scenes.append({"scene": name, "segments": segments, "volume": vol is not None,
+                       "ms_per_image": 1e3 * wall, "images_per_s": 1.0 / wall,
+                       "bvh_build_ms": build_ms / args.steps, "render_ms": render_ms / args.steps,
+                       "rays_per_s": width * height / (1e-3 * render_ms / args.steps),
+                       "cpu_restatement_ms_per_image": 1e3 * cpu, "cpu_threads": port.max_threads(),
+                       "pixels_equal_cpu": int(np.all(rgba == expected, axis=-1).sum()), "pixels": width * height})
+    ctx.release_field(h)
+    ctx.close()
+    print(json.dumps({"workload": "render: the benchmark generator's ray-tracing settings (1080 x 1920, 1 iteration, radius "
+                                  "0.1 voxel) on 64^3 ABC streamlines", "metric": "images/s", "unit": "images/s",
+                      "value": scenes[0]["images_per_s"], "scenes": scenes}))
 
 
 def run_domain(args):
@@ -573,7 +644,8 @@ def run_serve(args):
 def main():
     args = parse_args()
     if args.workload != "ftle":
-        {"streamlines": run_streamlines, "domain": run_domain, "pathlines": run_pathlines, "serve": run_serve}[args.workload](args)
+        {"streamlines": run_streamlines, "domain": run_domain, "pathlines": run_pathlines, "serve": run_serve,
+         "render": run_render}[args.workload](args)
         return
     rank, world, local = dist_env()
     from pars_gb300 import workloads

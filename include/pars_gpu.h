@@ -337,6 +337,7 @@ typedef struct pars_gpu_request_info
   double  queue_ms;       /* submit -> start */
   double  run_ms;         /* start -> finish */
   double  latency_ms;     /* submit -> finish */
+  int32_t image_size[2];  /* width, height of the request's image (0, 0 without one) */
 } pars_gpu_request_info;
 
 /* Decodes a `settings` message (host-only; no device needed). */
@@ -351,6 +352,17 @@ int32_t pars_gpu_service_add_dataset (pars_gpu_service* service, const char* nam
 int32_t pars_gpu_service_add_dataset_device(pars_gpu_service* service, const char* name, const float* device_xyz,
                                             const int32_t shape[3], const float offset[3], const float size[3],
                                             const float spacing[3]);
+/* Registers a scalar volume (HOST values [X][Y][Z] FP32) under `name`, the
+ * `volume_type` of requests whose mode contains "volume" (data_io.cpp:41-49). */
+int32_t pars_gpu_service_add_volume  (pars_gpu_service* service, const char* name, const float* values, const int32_t shape[3],
+                                      const float offset[3], const float spacing[3]);
+int32_t pars_gpu_service_add_volume_device(pars_gpu_service* service, const char* name, const float* device_values,
+                                           const int32_t shape[3], const float offset[3], const float spacing[3]);
+/* Streamline requests whose settings carry raytracing_image_size (both > 0,
+ * mode without "export") are also ray traced as pipeline.cpp:264-337 does:
+ * camera position / forward / up (3 values each), radius (0 -> 1), iterations,
+ * the volume named volume_type when the mode contains "volume" (a mode with
+ * "volume" but not "streamlines" renders the volume alone). */
 int32_t pars_gpu_service_submit      (pars_gpu_service* service, const uint8_t* message, int64_t length, int64_t* ticket);
 /* Waits up to timeout_ms (negative: no limit, 0: poll) and reports the state;
  * returns the request's failure status once it has failed. */
@@ -361,6 +373,11 @@ int32_t pars_gpu_service_result_batch(pars_gpu_service* service, int64_t ticket,
                                       int64_t* indices, float* vertex_data, float* color_data, int32_t* index_data);
 /* FTLE results: ftle_shape[0]*ftle_shape[1]*ftle_shape[2] floats to HOST `values`. */
 int32_t pars_gpu_service_result_ftle (pars_gpu_service* service, int64_t ticket, float* values);
+/* The request's image (the reply of ray_tracer::serialize): size = (width,
+ * height), (0, 0) without one; rgba (when not NULL) receives width*height*4
+ * bytes, sRGB RGBA8, rows from the top.  pars_gpu_image_encode makes the
+ * `image` message of it. */
+int32_t pars_gpu_service_result_image(pars_gpu_service* service, int64_t ticket, uint8_t* rgba, int32_t size[2]);
 /* Forgets a request (cancels it if it is still queued). */
 int32_t pars_gpu_service_release     (pars_gpu_service* service, int64_t ticket);
 /* Instrumentation (no counterpart in the reference's service; the reference
@@ -404,6 +421,52 @@ int32_t pars_gpu_ftle_no_alloc(const float* device_xyz, const int32_t shape[3], 
                                const float spacing[3], int32_t iterations, int32_t integrator, int32_t stage_mode,
                                float step_size, float time, int32_t mode, float* device_ftle, int64_t* device_steps,
                                void* stream);
+
+/* ---- ray tracer (replaces pars::ray_tracer, pars/include/pars/stages/ray_tracer.hpp:27-34) ----
+ * One ray tracer per context.  Scene: one capsule (cylinder plus end spheres)
+ * of the given radius per line index, coloured with vertex colour[index];
+ * optionally a scalar volume with the reference's transfer function (grey
+ * ramp, opacity 0.0001 -> 0.0255 over values 0 -> 1).  Camera: perspective,
+ * fovy 68 degrees.  Lights: ambient 1 and the two distant lights of
+ * ray_tracer.cpp:68-91.  Frames accumulate (one sample per pixel each, jittered
+ * after the first) until the scene, camera or image size changes.  The
+ * shading is this library's definition of that configuration (OSPRay is not
+ * involved); the image is sRGB-encoded RGBA8, rows from the top. */
+/* ray_tracer::set_volume (ray_tracer.cpp:130-163): values [X][Y][Z] FP32 (z fastest),
+ * host memory (_device: device memory; both are copied). */
+int32_t pars_gpu_ray_tracer_set_volume       (pars_gpu_context* context, const float* values, const int32_t shape[3],
+                                              const float offset[3], const float spacing[3]);
+int32_t pars_gpu_ray_tracer_set_volume_device(pars_gpu_context* context, const float* device_values, const int32_t shape[3],
+                                              const float offset[3], const float spacing[3]);
+int32_t pars_gpu_ray_tracer_clear_volume     (pars_gpu_context* context);
+/* ray_tracer::set_integral_curves (ray_tracer.cpp:164-211) on the context's
+ * device-resident curves (after pars_gpu_curves_index, and _color for
+ * colours; uncoloured curves render white).  The curves are used in place:
+ * tracing, indexing or colouring again makes _trace fail with PARS_ERR_STATE
+ * until this is called again.  radius > 0 (pipeline.cpp:306 passes 1 for 0). */
+int32_t pars_gpu_ray_tracer_set_integral_curves(pars_gpu_context* context, float radius);
+/* The same for host batches (pa::integral_curves vectors): per batch its
+ * vertex count, vertices (float4), colours (float4; colors or an entry NULL:
+ * white), index count and indices; batches without indices are skipped. */
+int32_t pars_gpu_ray_tracer_set_integral_curves_host(pars_gpu_context* context, int64_t batches, const int64_t* vertex_counts,
+                                                     const float* const* vertices, const float* const* colors,
+                                                     const int64_t* index_counts, const int32_t* const* indices, float radius);
+/* ray_tracer::set_camera (ray_tracer.cpp:213-220) and set_image_size (:221-229). */
+int32_t pars_gpu_ray_tracer_set_camera    (pars_gpu_context* context, const float position[3], const float forward[3],
+                                           const float up[3]);
+int32_t pars_gpu_ray_tracer_set_image_size(pars_gpu_context* context, int32_t width, int32_t height);
+/* ray_tracer::trace (ray_tracer.cpp:231-235): adds `iterations` frames. */
+int32_t pars_gpu_ray_tracer_trace         (pars_gpu_context* context, int32_t iterations);
+/* ray_tracer::serialize (ray_tracer.cpp:236-253): the image's size and, when
+ * rgba is not NULL, its width*height*4 bytes (sRGB RGBA8) of the average of
+ * the frames so far (background before the first frame). */
+int32_t pars_gpu_ray_tracer_serialize     (pars_gpu_context* context, uint8_t* rgba, int32_t size[2]);
+/* Frames accumulated since the last change. */
+int32_t pars_gpu_ray_tracer_frames        (pars_gpu_context* context, int64_t* frames);
+/* Encodes the `image` message (pars/proto/image.proto): *length receives the
+ * encoded size; out (when not NULL, with capacity >= that size) the bytes. */
+int32_t pars_gpu_image_encode(const int32_t size[2], const uint8_t* data, int64_t data_bytes, uint8_t* out, int64_t capacity,
+                              int64_t* length);
 
 /* ---- instrumentation ---------------------------------------------------------- */
 /* When enabled, each kernel launch is bracketed by CUDA events on the launch

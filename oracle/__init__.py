@@ -186,6 +186,42 @@ class Port(_Lib):
         L.orc_largest_eigenvalue_closed_form.argtypes = [_P, _LL, _P]
         L.orc_advect_unsteady_fp64.restype = None
         L.orc_advect_unsteady_fp64.argtypes = [_P, _P, _I, _P, _P, _D, _D, _P, _LL, _D, _D, _LL, _P, _P]
+        L.orc_render.restype = _I
+        L.orc_render.argtypes = [_P, _P, _P, _LL, _F, _P, _P, _P, _P, _P, _P, _P, _I, _I, _LL, _I, _P, _P]
+
+    def render(self, batches, radius, camera, size, frames=1, volume=None, accum=None, first_frame=0):
+        """The ray tracer's image: batches = [(vertices (n,4), colours (n,4) or
+        None, indices (m,))], camera = (position, forward, up), size = (width,
+        height), volume = (values [X,Y,Z], offset, spacing) or None.  Adds
+        `frames` frames to `accum` ([h, w, 4] float32 sums, new when None) and
+        returns (rgba [h, w, 4] uint8, accum)."""
+        width, height = size
+        verts, cols, prims, offset = [], [], [], 0
+        for v, c, i in batches:
+            v = np.ascontiguousarray(v, np.float32).reshape(-1, 4)
+            if len(i) == 0:
+                continue
+            verts.append(v)
+            cols.append(None if c is None else np.ascontiguousarray(c, np.float32).reshape(-1, 4))
+            prims.append(offset + np.asarray(i, np.int64))
+            offset += len(v)
+        vertices = np.concatenate(verts) if verts else np.zeros((1, 4), np.float32)
+        colors = np.concatenate(cols) if cols and all(c is not None for c in cols) else None
+        prim = np.concatenate(prims) if prims else np.zeros(1, np.int64)
+        n = sum(len(p) for p in prims)
+        if accum is None:
+            accum = np.zeros((height, width, 4), np.float32)
+        rgba = np.zeros((height, width, 4), np.uint8)
+        vol = vs = vo = vh = None
+        if volume is not None:
+            vol = np.ascontiguousarray(volume[0], np.float32)
+            vs = np.array(vol.shape, np.int32)
+            vo = np.ascontiguousarray(volume[1], np.float32)
+            vh = np.ascontiguousarray(volume[2], np.float32)
+        pos, fwd, up = (np.ascontiguousarray(x, np.float32) for x in camera)
+        self.lib.orc_render(_ptr(vertices), _ptr(colors), _ptr(prim), n, radius, _ptr(vol), _ptr(vs), _ptr(vo), _ptr(vh),
+                            _ptr(pos), _ptr(fwd), _ptr(up), width, height, first_frame, frames, _ptr(accum), _ptr(rgba))
+        return rgba, accum
 
     def advect_unsteady_fp64(self, xyz, offset, spacing, t0, slice_dt, start, time_begin, step, max_steps):
         """FP64 pathlines (classical RK4 in space-time) on an unsteady field

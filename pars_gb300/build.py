@@ -17,7 +17,10 @@ BUILD = os.path.join(HERE, "_build")
 LIBRARY = os.path.join(HERE, "libpars_gpu.so")
 
 SOURCES = ["pars_gpu.cu", "trace_kernels.cu", "curve_kernels.cu", "ftle_kernels.cu", "field_kernels.cu", "batch_kernels.cu",
-           "service.cu"]
+           "service.cu", "render_kernels.cu"]
+# Per-source flags: the ray tracer rounds every operation separately (no FMA
+# contraction), as its CPU restatement does.
+SOURCE_FLAGS = {"render_kernels.cu": ["--fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
@@ -47,7 +50,7 @@ def build(verbose=False, extra_flags=()):
         o = os.path.join(BUILD, src.replace(".cu", ".o"))
         objects.append(o)
         if _stale(o, [s] + headers):
-            jobs.append([nvcc(), *ARCH, *FLAGS, *extra_flags, "-c", s, "-o", o])
+            jobs.append([nvcc(), *ARCH, *FLAGS, *SOURCE_FLAGS.get(src, []), *extra_flags, "-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

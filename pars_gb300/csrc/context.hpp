@@ -4,7 +4,9 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -142,6 +144,43 @@ struct curves_store
   bool                      indexed = false;
   bool                      colored = false;
   std::vector<curves_batch> batches;
+  long long                 generation = 0;   // bumped whenever the curves or their indices / colours change
+};
+
+// The ray tracer's state (render_kernels.cu): the scene's capsules and their
+// BVH, the volume, the camera, and the accumulated frames.
+struct render_state
+{
+  render_state();
+  // scene: one capsule per line index; prim_vertex[k] = its segment's start vertex
+  long long     prims = 0;
+  const float4* vertices = nullptr;
+  const float4* colors = nullptr;               // nullptr: white
+  float         radius = 1.0f;
+  long long     curves_generation = -1;         // >= 0: the context's curves at that generation
+  device_buffer own_vertices, own_colors, prim_vertex, batch_bounds;
+  // BVH (linear, Karras 2012)
+  bool          tree_valid = false;
+  bool          status_pending = false;         // the build's status word is not read yet
+  device_buffer bounds, leaf_lo_unsorted, leaf_hi_unsorted, keys, values, leaf_lo, leaf_hi, leaf_vertex, nodes,
+                node_parent, leaf_parent, arrivals;
+  // volume: float [x][y][z] (volume_data: the tracer's own copy in `volume`,
+  // or a buffer the caller keeps alive, such as a service dataset)
+  bool          has_volume = false;
+  const float*  volume_data = nullptr;
+  device_buffer volume;
+  int           volume_shape[3] = {0, 0, 0};
+  float         volume_offset[3] = {0, 0, 0}, volume_spacing[3] = {1, 1, 1};
+  // camera and image
+  bool          camera_set = false;
+  float         position[3] = {0, 0, 0}, corner[3] = {0, 0, 0}, du[3] = {0, 0, 0}, dv[3] = {0, 0, 0};
+  float         forward[3] = {0, 0, 1}, up[3] = {0, 1, 0};
+  int           width = 0, height = 0;
+  // accumulated frames
+  bool          accum_valid = false;
+  long long     frames = 0;
+  device_buffer accum, jitter, status, image, thresholds;
+  float         srgb_thresholds[255];
 };
 
 struct profile_entry
@@ -168,6 +207,7 @@ struct pars_gpu_context
   std::map<int, std::unique_ptr<pars::field_entry>>  fields;
   std::map<int, std::unique_ptr<pars::domain_entry>> domains;
   pars::curves_store                      curves;
+  std::unique_ptr<pars::render_state>     render;     // created by the first ray-tracer call
   // scratch
   pars::device_buffer                     particles_in, particles_next, slots, kept, written, offsets, block_of,
                                           block_of_next, exits, exit_keys, exit_keys_sorted, exit_order,
@@ -350,4 +390,24 @@ void launch_flow_map(pars_gpu_context& ctx, const field_view& f, const step_rule
                      const float offset[3], const float fm_spacing[3], const int seeds_per_dimension[3],
                      const int fm_shape[3], float4* flow, unsigned long long* steps);
 void launch_ftle(pars_gpu_context& ctx, const field_view& flow, double time, int mode, float* out);
+
+// Ray tracer (render_kernels.cu).
+void render_jitter(long long frame, float& jx, float& jy);
+void render_camera(const float position[3], const float forward[3], const float up[3], int width, int height,
+                   float corner[3], float du[3], float dv[3]);
+void render_clear(render_state& r);
+void render_use_context_curves(pars_gpu_context& ctx, render_state& r);
+// Prims of curve spans inside caller-owned buffers: each span is (start vertex
+// of its batch in `vertices`, first index in `indices`, index count).
+void render_use_spans(pars_gpu_context& ctx, render_state& r, const float4* vertices, const float4* colors, const int* indices,
+                      const std::vector<std::array<long long, 3>>& spans);
+// Camera and image size (ray_tracer.cpp:213-229); clears the accumulation.
+void render_set_view(render_state& r, const float position[3], const float forward[3], const float up[3], int width, int height);
+void render_build(pars_gpu_context& ctx, render_state& r);
+void render_frames(pars_gpu_context& ctx, render_state& r, int iterations);
+void render_encode(pars_gpu_context& ctx, render_state& r, uint8_t* host_rgba);
+
+// Runs body under the context's lock and turns exceptions into a status (the
+// wrapper of every C entry point on a context).
+int32_t run_guarded(pars_gpu_context* ctx, const std::function<void()>& body);
 }

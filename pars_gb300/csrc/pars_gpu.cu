@@ -90,6 +90,7 @@ void release_scratch(pars_gpu_context& ctx)
   ctx.curves.index_total = 0;
   ctx.curves.indexed = ctx.curves.colored = false;
   ctx.curves.batches.clear();
+  ++ctx.curves.generation;
   ctx.ftle_count = 0;
 }
 
@@ -174,6 +175,15 @@ int32_t guarded(pars_gpu_context* ctx, body_type&& body)
   catch (const std::exception& e) { ctx->last_error = e.what(); return PARS_ERR_STATE; }
 }
 
+}
+
+int32_t run_guarded(pars_gpu_context* ctx, const std::function<void()>& body)
+{
+  return guarded(ctx, body);
+}
+
+namespace
+{
 field_entry& find_field(pars_gpu_context& ctx, int32_t handle)
 {
   auto it = ctx.fields.find(handle);
@@ -302,6 +312,7 @@ void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, c
   curves.vertex_total = 0;
   curves.index_total = 0;
   curves.indexed = curves.colored = false;
+  ++curves.generation;
   const int nblocks = int(blocks.size());
   int key_bits = 40;
   while ((1 << (key_bits - 40)) < nblocks) ++key_bits;
@@ -991,6 +1002,7 @@ int32_t pars_gpu_curves_index(pars_gpu_context* ctx)
     index_batches(*ctx, c);
     c.indexed = true;
     c.colored = false;
+    ++c.generation;
   });
 }
 
@@ -1002,6 +1014,7 @@ int32_t pars_gpu_curves_color(pars_gpu_context* ctx, int32_t mode, float paramet
     PARS_REQUIRE(mode >= PARS_COLOR_HSL_CONSTANT_S && mode <= PARS_COLOR_RGB, "unknown colour mode");
     color_batches(*ctx, c, std::vector<color_spec>(c.batches.size(), color_spec{mode, parameter}));
     c.colored = true;
+    ++c.generation;
   });
 }
 

@@ -21,7 +21,10 @@
 //  * overlap: while one lane's batch runs, another lane admits the requests
 //    that arrived meanwhile and launches them on its own stream.
 // Datasets (the requests' dataset_filepath) are fields registered with the
-// service and kept resident across requests.
+// service and kept resident across requests; scalar volumes (volume_type)
+// likewise.  A streamline request that carries an image size is also ray
+// traced (pipeline.cpp:264-337): its image is rendered on the lane right after
+// its batch and kept in host memory with the request.
 #include <algorithm>
 #include <array>
 #include <chrono>
@@ -53,6 +56,15 @@ struct dataset
   field_view  view;
   int         shape[3];
   float       offset[3], size[3], spacing[3];
+};
+
+// A scalar volume for the ray tracer (the reference's load_local_scalar_field
+// of `volume_type`, data_io.cpp:41-49,76-81): float [X][Y][Z] on the device.
+struct volume_dataset
+{
+  device_buffer data;
+  int           shape[3];
+  float         offset[3], spacing[3];
 };
 
 // One integral_curves batch of a streamline request: its place in the
@@ -107,6 +119,12 @@ struct request
   bool                    released = false;
   std::vector<curve_span> spans;   // streamlines: one per integral_curves batch
   int64_t                 vertex_total = 0, index_total = 0;
+  // ray tracing (streamline requests with an image size)
+  bool                    trace_curves = true;   // false for a "volume"-only request
+  bool                    wants_image = false;
+  int                     volume = -1;           // volume dataset, -1 without
+  std::vector<uint8_t>    image;                 // sRGB RGBA8, rows from the top
+  int32_t                 image_size[2] = {0, 0};
 };
 
 int integrator_of(const std::string& name)
@@ -148,6 +166,8 @@ struct pars_gpu_service
   std::map<int64_t, std::shared_ptr<pars::request>> requests;
   std::vector<pars::dataset>           datasets;
   std::map<std::string, int>           dataset_index;
+  std::vector<std::unique_ptr<pars::volume_dataset>> volumes;
+  std::map<std::string, int>           volume_index;
   bool                                 stopping = false;
   bool                                 spilling = false;
   // instrumentation: per-kernel CUDA-event totals of all lanes and wall time
@@ -197,8 +217,13 @@ curve_store::~curve_store()
 }
 
 // Device bytes a request needs while it runs (a conservative estimate).
-std::size_t estimate_bytes(const request& r, const dataset& d)
+std::size_t estimate_bytes(const request& r, const dataset* dp)
 {
+  std::size_t image = 0;
+  if (r.wants_image)
+    image = std::size_t(r.s.raytracing_image_size[0]) * std::size_t(r.s.raytracing_image_size[1]) * (sizeof(float4) + 4);
+  if (!dp) return image + (1 << 20);
+  const dataset& d = *dp;
   if (r.kind == ftle)
   {
     const float scale = 1.0f / float(std::max(1, r.s.seed_generation_stride.empty() ? 1 : r.s.seed_generation_stride[0]));
@@ -214,8 +239,11 @@ std::size_t estimate_bytes(const request& r, const dataset& d)
   }
   const std::size_t slots = seeds * std::size_t(std::max(1, r.s.seed_generation_iterations));
   // padded slots + packed vertices + colours + indices + particle records,
-  // and the result (vertices, colours, indices)
-  return slots * (sizeof(float4) * 5 + sizeof(int32_t) * 2) + seeds * (sizeof(pars_particle) * 2 + 32) + (1 << 20);
+  // and the result (vertices, colours, indices); with an image, the tracer's
+  // BVH (about 200 B per segment) and frame buffers
+  std::size_t bytes = slots * (sizeof(float4) * 5 + sizeof(int32_t) * 2) + seeds * (sizeof(pars_particle) * 2 + 32) + (1 << 20);
+  if (r.wants_image) bytes += slots * 200 + image;
+  return bytes;
 }
 
 void fail(request& r, int32_t status, const std::string& message)
@@ -341,6 +369,44 @@ void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std:
 // Streamline requests: one block per request in one tracing round loop, then
 // index and colour per batch (pipeline::execute, pipeline.cpp:107-260).
 // Returns the bytes of the batch's curve store (shared by its requests).
+// Renders one request's curves (its spans of the batch's store) and, when it
+// names one, its volume: set_integral_curves, set_volume, set_camera,
+// set_image_size, trace and serialize of ray_tracer.cpp on the lane's tracer.
+void render_request(pars_gpu_service& svc, pars_gpu_context& c, request& r, const curve_store& store)
+{
+  if (!c.render) c.render = std::make_unique<render_state>();
+  render_state& rs = *c.render;
+  std::vector<std::array<long long, 3>> spans;
+  for (const auto& s : r.spans) spans.push_back({s.store_vertex_offset, s.store_index_offset, s.index_count});
+  render_use_spans(c, rs, store.vertices.as<const float4>(), store.colors.as<const float4>(), store.indices.as<const int>(), spans);
+  const float radius = r.s.raytracing_streamline_radius;
+  rs.radius = radius != 0.0f ? radius : 1.0f;                       // pipeline.cpp:306
+  rs.has_volume = false;
+  rs.volume_data = nullptr;
+  if (r.volume >= 0)
+  {
+    const volume_dataset& v = *svc.volumes[r.volume];
+    rs.has_volume = true;
+    rs.volume_data = v.data.as<const float>();
+    for (int i = 0; i < 3; ++i)
+    {
+      rs.volume_shape[i] = v.shape[i];
+      rs.volume_offset[i] = v.offset[i];
+      rs.volume_spacing[i] = v.spacing[i];
+    }
+  }
+  render_set_view(rs, r.s.raytracing_camera_position.data(), r.s.raytracing_camera_forward.data(), r.s.raytracing_camera_up.data(),
+                  r.s.raytracing_image_size[0], r.s.raytracing_image_size[1]);
+  render_frames(c, rs, std::max(0, r.s.raytracing_iterations));
+  r.image.resize(std::size_t(rs.width) * rs.height * 4);
+  render_encode(c, rs, r.image.data());
+  r.image_size[0] = rs.width;
+  r.image_size[1] = rs.height;
+  rs.vertices = rs.colors = nullptr;       // the store may go once the request lets go
+  rs.prims = 0;
+  rs.tree_valid = false;
+}
+
 std::size_t run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std::shared_ptr<request>>& batch, int stage_mode)
 {
   phase_clock clock {svc, c, c.profile};
@@ -373,23 +439,30 @@ std::size_t run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std
   for (auto& rp : batch)
   {
     request& r = *rp;
-    const dataset& d = svc.datasets[r.dataset];
-    std::array<int, 3> pd;
-    long long n = 1;
-    for (int i = 0; i < 3; ++i)
-    {
-      const int stride = r.s.seed_generation_stride.size() > std::size_t(i) ? std::max(1, r.s.seed_generation_stride[i]) : 1;
-      const float st = d.spacing[i] * float(stride);               // pipeline.cpp:117
-      const float q = d.size[i] / st;                              // seed_generator.cpp:11
-      pd[i] = (q > 0.0f && q < 2147483647.0f) ? int(q) : 0;
-      n *= pd[i];
-    }
-    per_dim.push_back(pd);
-    trace_block b;
-    b.field = d.view;
+    std::array<int, 3> pd {0, 0, 0};
+    long long n = 0;
+    trace_block b {};
     for (int f = 0; f < 6; ++f) b.neighbor[f] = -1;
+    if (r.trace_curves)
+    {
+      const dataset& d = svc.datasets[r.dataset];
+      n = 1;
+      for (int i = 0; i < 3; ++i)
+      {
+        const int stride = r.s.seed_generation_stride.size() > std::size_t(i) ? std::max(1, r.s.seed_generation_stride[i]) : 1;
+        const float st = d.spacing[i] * float(stride);               // pipeline.cpp:117
+        const float q = d.size[i] / st;                              // seed_generator.cpp:11
+        pd[i] = (q > 0.0f && q < 2147483647.0f) ? int(q) : 0;
+        n *= pd[i];
+      }
+      b.field = d.view;
+    }
+    else
+      b.field = svc.datasets.empty() ? field_view {} : svc.datasets[0].view;   // no particles sample it
+    per_dim.push_back(pd);
     blocks.push_back(b);
-    rules.push_back(make_step_rule(r.integrator, stage_mode, r.s.particle_tracing_step_size));
+    rules.push_back(r.trace_curves ? make_step_rule(r.integrator, stage_mode, r.s.particle_tracing_step_size)
+                                   : make_step_rule(PARS_RUNGE_KUTTA_4, stage_mode, 1.0f));
     block_count.push_back(n);
     block_max.push_back(n > 0 ? r.s.seed_generation_iterations : 0);
     total += n;
@@ -401,6 +474,7 @@ std::size_t run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std
   for (std::size_t k = 0; k < batch.size(); ++k)
   {
     request& r = *batch[k];
+    if (block_count[k] == 0) continue;
     const dataset& d = svc.datasets[r.dataset];
     float stride[3];
     for (int i = 0; i < 3; ++i)
@@ -456,8 +530,18 @@ std::size_t run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std
   curves.batches.clear();
   curves.vertex_total = curves.index_total = 0;
   curves.indexed = curves.colored = false;
+  ++curves.generation;
   PARS_CUDA(cudaStreamSynchronize(c.stream));
   clock.mark("streamlines.results");
+  // ray tracing (pipeline.cpp:264-337): one image per request that asks for one
+  bool rendered = false;
+  for (auto& rp : batch)
+  {
+    if (!rp->wants_image) continue;
+    render_request(svc, c, *rp, *store);
+    rendered = true;
+  }
+  if (rendered) clock.mark("streamlines.render");
   // Steps per request: each curve holds its seed, one vertex per step and the
   // termination vertex (remaining_iterations >= 2; one block, one round).
   for (std::size_t k = 0; k < batch.size(); ++k)
@@ -794,6 +878,44 @@ int32_t pars_gpu_service_add_dataset_device(pars_gpu_service* svc, const char* n
   });
 }
 
+namespace
+{
+void add_volume(pars_gpu_service* svc, const char* name, const float* values, bool device, const int32_t shape[3],
+                const float offset[3], const float spacing[3])
+{
+  PARS_REQUIRE(name && values && shape && offset && spacing, "name, values, shape, offset and spacing are required");
+  auto v = std::make_unique<volume_dataset>();
+  std::size_t count = 1;
+  for (int i = 0; i < 3; ++i)
+  {
+    PARS_REQUIRE(shape[i] >= 2 && spacing[i] > 0.0f, "volume extents must be >= 2 and spacings positive");
+    v->shape[i] = shape[i];
+    v->offset[i] = offset[i];
+    v->spacing[i] = spacing[i];
+    count *= std::size_t(shape[i]);
+  }
+  PARS_CUDA(cudaSetDevice(svc->device));
+  v->data.reserve(sizeof(float) * count);
+  PARS_CUDA(cudaMemcpy(v->data.get(), values, sizeof(float) * count, device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
+  std::lock_guard<std::mutex> lock(svc->mutex);
+  PARS_REQUIRE(svc->volume_index.count(name) == 0, "a volume with this name exists");
+  svc->volume_index[name] = int(svc->volumes.size());
+  svc->volumes.push_back(std::move(v));
+}
+}
+
+int32_t pars_gpu_service_add_volume(pars_gpu_service* svc, const char* name, const float* values, const int32_t shape[3],
+                                    const float offset[3], const float spacing[3])
+{
+  return service_guard(svc, [&] { add_volume(svc, name, values, false, shape, offset, spacing); });
+}
+
+int32_t pars_gpu_service_add_volume_device(pars_gpu_service* svc, const char* name, const float* device_values,
+                                           const int32_t shape[3], const float offset[3], const float spacing[3])
+{
+  return service_guard(svc, [&] { add_volume(svc, name, device_values, true, shape, offset, spacing); });
+}
+
 int32_t pars_gpu_service_submit(pars_gpu_service* svc, const uint8_t* message, int64_t length, int64_t* ticket)
 {
   return service_guard(svc, [&] {
@@ -802,21 +924,49 @@ int32_t pars_gpu_service_submit(pars_gpu_service* svc, const uint8_t* message, i
     std::string problem;
     if (!decode_settings(message, std::size_t(length), r->s, problem)) throw error(PARS_ERR_INVALID_ARGUMENT, problem);
     // mode substrings as pipeline.cpp:21-23 and service.cpp:79 read them
-    r->kind = r->s.mode.find("ftle") != std::string::npos ? ftle : streamlines;
-    if (r->s.mode.find("fractional_anisotropy") != std::string::npos) r->ftle_mode = PARS_FTLE_FRACTIONAL_ANISOTROPY;
-    r->stage_mode = r->s.mode.find("reference") != std::string::npos ? PARS_STAGES_FROZEN : PARS_STAGES_RESAMPLED;
+    const std::string& mode = r->s.mode;
+    r->kind = mode.find("ftle") != std::string::npos ? ftle : streamlines;
+    if (mode.find("fractional_anisotropy") != std::string::npos) r->ftle_mode = PARS_FTLE_FRACTIONAL_ANISOTROPY;
+    r->stage_mode = mode.find("reference") != std::string::npos ? PARS_STAGES_FROZEN : PARS_STAGES_RESAMPLED;
     if (r->kind == ftle && r->stage_mode == PARS_STAGES_FROZEN)
       throw error(PARS_ERR_UNSUPPORTED, "served FTLE integrates with re-sampled stages");
-    r->integrator = integrator_of(r->s.particle_tracing_integrator);
-    if (r->integrator != PARS_EULER && r->integrator != PARS_RUNGE_KUTTA_4)
-      throw error(PARS_ERR_UNSUPPORTED, "integrator '" + r->s.particle_tracing_integrator + "' is not supported");
+    const bool with_volume = mode.find("volume") != std::string::npos;
+    if (r->kind == streamlines)
+    {
+      // "volume" without "streamlines" renders the volume alone (pipeline.cpp:21-22, 76-92)
+      r->trace_curves = mode.find("streamlines") != std::string::npos || !with_volume;
+      const auto& size = r->s.raytracing_image_size;
+      r->wants_image = mode.find("export") == std::string::npos && size.size() >= 2 && size[0] > 0 && size[1] > 0;
+      if (r->wants_image)
+      {
+        PARS_REQUIRE((long long)size[0] * size[1] <= (1LL << 28), "raytracing_image_size too large");
+        PARS_REQUIRE(r->s.raytracing_camera_position.size() >= 3 && r->s.raytracing_camera_forward.size() >= 3 &&
+                     r->s.raytracing_camera_up.size() >= 3, "ray tracing needs camera position, forward and up");
+      }
+      PARS_REQUIRE(r->trace_curves || r->wants_image, "a volume request needs an image size");
+    }
+    if (r->trace_curves || r->kind == ftle)
+    {
+      r->integrator = integrator_of(r->s.particle_tracing_integrator);
+      if (r->integrator != PARS_EULER && r->integrator != PARS_RUNGE_KUTTA_4)
+        throw error(PARS_ERR_UNSUPPORTED, "integrator '" + r->s.particle_tracing_integrator + "' is not supported");
+      PARS_REQUIRE(r->s.particle_tracing_step_size != 0.0f, "particle_tracing_step_size must be non-zero");
+    }
     r->color_mode = color_of(r->s.color_generation_mode);
-    PARS_REQUIRE(r->s.particle_tracing_step_size != 0.0f, "particle_tracing_step_size must be non-zero");
     std::unique_lock<std::mutex> lock(svc->mutex);
-    auto d = svc->dataset_index.find(r->s.dataset_filepath);
-    if (d == svc->dataset_index.end()) throw error(PARS_ERR_NOT_FOUND, "unknown dataset '" + r->s.dataset_filepath + "'");
-    r->dataset = d->second;
-    r->estimate = estimate_bytes(*r, svc->datasets[r->dataset]);
+    if (r->trace_curves || r->kind == ftle)
+    {
+      auto d = svc->dataset_index.find(r->s.dataset_filepath);
+      if (d == svc->dataset_index.end()) throw error(PARS_ERR_NOT_FOUND, "unknown dataset '" + r->s.dataset_filepath + "'");
+      r->dataset = d->second;
+    }
+    if (r->wants_image && with_volume)
+    {
+      auto v = svc->volume_index.find(r->s.volume_type);
+      if (v == svc->volume_index.end()) throw error(PARS_ERR_NOT_FOUND, "unknown volume '" + r->s.volume_type + "'");
+      r->volume = v->second;
+    }
+    r->estimate = estimate_bytes(*r, r->dataset >= 0 ? &svc->datasets[r->dataset] : nullptr);
     if (r->estimate > svc->budget) throw error(PARS_ERR_BUDGET, "request needs more device memory than the service budget");
     r->ticket = svc->next_ticket++;
     r->submitted = clock_type::now();
@@ -854,6 +1004,7 @@ int32_t pars_gpu_service_result_info(pars_gpu_service* svc, int64_t ticket, pars
     info->batches = r->state == done ? (int64_t)r->spans.size() : 0;
     for (int i = 0; i < 3; ++i) info->ftle_shape[i] = r->ftle_shape[i];
     info->steps = r->steps;
+    if (r->state == done) { info->image_size[0] = r->image_size[0]; info->image_size[1] = r->image_size[1]; }
     using ms = std::chrono::duration<double, std::milli>;
     if (r->state >= running) info->queue_ms = ms(r->started - r->submitted).count();
     if (r->state == done) { info->run_ms = ms(r->finished - r->started).count(); info->latency_ms = ms(r->finished - r->submitted).count(); }
@@ -915,6 +1066,22 @@ int32_t pars_gpu_service_result_ftle(pars_gpu_service* svc, int64_t ticket, floa
     PARS_CUDA(cudaSetDevice(svc->device));
     copy_result(*svc, *r, 0, values, r->result_bytes);
     PARS_CUDA(cudaStreamSynchronize(svc->copy_stream));
+  });
+}
+
+int32_t pars_gpu_service_result_image(pars_gpu_service* svc, int64_t ticket, uint8_t* rgba, int32_t size[2])
+{
+  return service_guard(svc, [&] {
+    std::shared_ptr<request> r;
+    {
+      std::lock_guard<std::mutex> lock(svc->mutex);
+      r = find_request(svc, ticket);
+      if (r->state != done) throw error(PARS_ERR_STATE, "request has not finished");
+    }
+    std::lock_guard<std::mutex> lock(r->result_mutex);
+    if (r->released) throw error(PARS_ERR_NOT_FOUND, "request was released");
+    if (size) { size[0] = r->image_size[0]; size[1] = r->image_size[1]; }
+    if (rgba && !r->image.empty()) std::memcpy(rgba, r->image.data(), r->image.size());
   });
 }
 

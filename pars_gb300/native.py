@@ -68,7 +68,8 @@ class SettingsSummary(ctypes.Structure):
 class RequestInfo(ctypes.Structure):
     _fields_ = [("state", ctypes.c_int32), ("status", ctypes.c_int32), ("kind", ctypes.c_int32),
                 ("ftle_shape", ctypes.c_int32 * 3), ("batches", ctypes.c_int64), ("steps", ctypes.c_int64),
-                ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+                ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("image_size", ctypes.c_int32 * 2)]
 
 
 class ParsGpuError(RuntimeError):
@@ -131,8 +132,22 @@ SIGNATURES = {
     "pars_gpu_service_result_batch": [_P, _I64, _I64, ctypes.POINTER(_I64), ctypes.POINTER(_I64), _P, _P, _P],
     "pars_gpu_service_result_ftle": [_P, _I64, _P],
     "pars_gpu_service_release": [_P, _I64],
+    "pars_gpu_service_add_volume": [_P, ctypes.c_char_p, _P, _P, _P, _P],
+    "pars_gpu_service_add_volume_device": [_P, ctypes.c_char_p, _P, _P, _P, _P],
+    "pars_gpu_service_result_image": [_P, _I64, _P, _P],
     "pars_gpu_service_profile_enable": [_P, _I32],
     "pars_gpu_service_profile_get": [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)],
+    "pars_gpu_ray_tracer_set_volume": [_P, _P, _P, _P, _P],
+    "pars_gpu_ray_tracer_set_volume_device": [_P, _P, _P, _P, _P],
+    "pars_gpu_ray_tracer_clear_volume": [_P],
+    "pars_gpu_ray_tracer_set_integral_curves": [_P, _F],
+    "pars_gpu_ray_tracer_set_integral_curves_host": [_P, _I64, _P, _P, _P, _P, _P, _F],
+    "pars_gpu_ray_tracer_set_camera": [_P, _P, _P, _P],
+    "pars_gpu_ray_tracer_set_image_size": [_P, _I32, _I32],
+    "pars_gpu_ray_tracer_trace": [_P, _I32],
+    "pars_gpu_ray_tracer_serialize": [_P, _P, _P],
+    "pars_gpu_ray_tracer_frames": [_P, ctypes.POINTER(_I64)],
+    "pars_gpu_image_encode": [_P, _P, _I64, _P, _I64, ctypes.POINTER(_I64)],
     "pars_gpu_profile_enable": [_P, _I32],
     "pars_gpu_profile_reset": [_P],
     "pars_gpu_profile_get": [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)],
@@ -404,6 +419,62 @@ class Context:
         self._call("pars_gpu_batch_tuned", job_class, ctypes.byref(v), ctypes.byref(t))
         return v.value, t.value
 
+    # -- ray tracer (pars::ray_tracer) -------------------------------------------------
+    def ray_tracer_set_volume(self, values, offset, spacing):
+        """values: [X, Y, Z] FP32 host array."""
+        v = np.ascontiguousarray(values, np.float32)
+        s, o, sp = _i3(v.shape), _f3(offset), _f3(spacing)     # kept alive across the call
+        self._call("pars_gpu_ray_tracer_set_volume", _ptr(v), _ptr(s), _ptr(o), _ptr(sp))
+
+    def ray_tracer_set_volume_device(self, device_ptr, shape, offset, spacing):
+        s, o, sp = _i3(shape), _f3(offset), _f3(spacing)
+        self._call("pars_gpu_ray_tracer_set_volume_device", device_ptr, _ptr(s), _ptr(o), _ptr(sp))
+
+    def ray_tracer_clear_volume(self):
+        self._call("pars_gpu_ray_tracer_clear_volume")
+
+    def ray_tracer_set_integral_curves(self, radius):
+        """The context's device-resident curves (indexed, optionally coloured)."""
+        self._call("pars_gpu_ray_tracer_set_integral_curves", radius)
+
+    def ray_tracer_set_integral_curves_host(self, batches, radius):
+        """batches: list of (vertices (n,4), colours (n,4) or None, indices (m,))."""
+        keep = [(np.ascontiguousarray(v, np.float32).reshape(-1, 4),
+                 None if c is None else np.ascontiguousarray(c, np.float32).reshape(-1, 4),
+                 np.ascontiguousarray(i, np.int32)) for v, c, i in batches]
+        n = len(keep)
+        vc = np.array([len(v) for v, _, _ in keep] or [0], np.int64)
+        ic = np.array([len(i) for _, _, i in keep] or [0], np.int64)
+        vp = (_P * max(n, 1))(*[v.ctypes.data for v, _, _ in keep])
+        with_colors = n > 0 and all(c is not None for _, c, _ in keep)
+        cp = (_P * max(n, 1))(*[c.ctypes.data for _, c, _ in keep]) if with_colors else None
+        ip = (_P * max(n, 1))(*[i.ctypes.data if len(i) else None for _, _, i in keep])
+        self._call("pars_gpu_ray_tracer_set_integral_curves_host", n, _ptr(vc), ctypes.cast(vp, _P),
+                   ctypes.cast(cp, _P) if cp is not None else None, _ptr(ic), ctypes.cast(ip, _P), radius)
+
+    def ray_tracer_set_camera(self, position, forward, up):
+        p, f, u = _f3(position), _f3(forward), _f3(up)          # kept alive across the call
+        self._call("pars_gpu_ray_tracer_set_camera", _ptr(p), _ptr(f), _ptr(u))
+
+    def ray_tracer_set_image_size(self, width, height):
+        self._call("pars_gpu_ray_tracer_set_image_size", width, height)
+
+    def ray_tracer_trace(self, iterations=1):
+        self._call("pars_gpu_ray_tracer_trace", iterations)
+
+    def ray_tracer_serialize(self):
+        """The image as a [height, width, 4] uint8 array (sRGB RGBA8, rows from the top)."""
+        size = np.zeros(2, np.int32)
+        self._call("pars_gpu_ray_tracer_serialize", None, _ptr(size))
+        out = np.zeros((size[1], size[0], 4), np.uint8)
+        self._call("pars_gpu_ray_tracer_serialize", _ptr(out), _ptr(size))
+        return out
+
+    def ray_tracer_frames(self):
+        n = _I64()
+        self._call("pars_gpu_ray_tracer_frames", ctypes.byref(n))
+        return n.value
+
     # -- instrumentation ----------------------------------------------------------------
     def profile_enable(self, on=True):
         self._call("pars_gpu_profile_enable", 1 if on else 0)
@@ -420,6 +491,22 @@ class Context:
         n = _I64()
         self._call("pars_gpu_launch_count", ctypes.byref(n))
         return n.value
+
+
+def image_encode(rgba):
+    """The `image` message (pars/proto/image.proto) of a [height, width, 4] uint8 image."""
+    lib = library()
+    rgba = np.ascontiguousarray(rgba, np.uint8)
+    size = np.array([rgba.shape[1], rgba.shape[0]], np.int32)
+    n = _I64()
+    status = lib.pars_gpu_image_encode(_ptr(size), _ptr(rgba), rgba.size, None, 0, ctypes.byref(n))
+    if status:
+        raise ParsGpuError(status, "pars_gpu_image_encode")
+    out = np.zeros(n.value, np.uint8)
+    status = lib.pars_gpu_image_encode(_ptr(size), _ptr(rgba), rgba.size, _ptr(out), n.value, ctypes.byref(n))
+    if status:
+        raise ParsGpuError(status, "pars_gpu_image_encode")
+    return out.tobytes()
 
 
 def decode_settings(message):
@@ -526,6 +613,24 @@ class Service:
     def ftle_into(self, ticket, values_ptr):
         """Copies an FTLE result to a host address."""
         self._check(self.lib.pars_gpu_service_result_ftle(self.handle, ticket, values_ptr), "pars_gpu_service_result_ftle")
+
+    def add_volume(self, name, values, offset, spacing):
+        """A scalar volume [X, Y, Z] for requests whose mode contains "volume"."""
+        v = np.ascontiguousarray(values, np.float32)
+        s, o, sp = _i3(v.shape), _f3(offset), _f3(spacing)
+        self._check(self.lib.pars_gpu_service_add_volume(self.handle, name.encode(), _ptr(v), _ptr(s), _ptr(o), _ptr(sp)),
+                    "pars_gpu_service_add_volume")
+
+    def image(self, ticket):
+        """The request's image, [height, width, 4] uint8 (None without one)."""
+        size = np.zeros(2, np.int32)
+        self._check(self.lib.pars_gpu_service_result_image(self.handle, ticket, None, _ptr(size)), "pars_gpu_service_result_image")
+        if size[0] == 0:
+            return None
+        out = np.zeros((size[1], size[0], 4), np.uint8)
+        self._check(self.lib.pars_gpu_service_result_image(self.handle, ticket, _ptr(out), _ptr(size)),
+                    "pars_gpu_service_result_image")
+        return out
 
     def release(self, ticket):
         self._check(self.lib.pars_gpu_service_release(self.handle, ticket), "pars_gpu_service_release")
