@@ -422,6 +422,33 @@ int32_t pars_gpu_ftle_no_alloc(const float* device_xyz, const int32_t shape[3], 
                                float step_size, float time, int32_t mode, float* device_ftle, int64_t* device_steps,
                                void* stream);
 
+/* ---- field files (replaces pa::data_io, pa/source/stages/data_io.cpp) -------------------
+ * HDF5 is not part of this library; datasets live in "pars raw" files: a
+ * 64-byte header (magic "PARSRAW1", uint32 components (3: vector field, 1:
+ * scalar field), uint32 0, int64 shape[3], float spacing[3], zero padding)
+ * and FP32 data [shape0][shape1][shape2][components], little endian.  Host-only
+ * unless a context is passed. */
+/* data_io::load_dimensions (data_io.cpp:36-40): components, shape and raw spacing. */
+int32_t pars_gpu_raw_info (const char* path, int32_t* components, int64_t shape[3], float spacing[3]);
+/* Writes a whole dataset (e.g. converted from HDF5). */
+int32_t pars_gpu_raw_write(const char* path, int32_t components, const int64_t shape[3], const float spacing[3],
+                           const float* data);
+/* data_io::load_local_vector_field (data_io.cpp:50-58, 90-114): the ghosted
+ * block of rank `rank` of `ranks` (pars_gpu_partition) as a resident field:
+ * spacing divided by its maximum, offset = voxel offset x spacing, size = block
+ * size x spacing.  *partition (may be NULL) receives the block's geometry. */
+int32_t pars_gpu_field_load(pars_gpu_context* context, const char* path, int32_t ranks, int32_t rank, int32_t* field,
+                            pars_partition_info* partition);
+/* data_io::load_scalar_field (data_io.cpp:41-49, 76-89) into HOST values
+ * [shape0][shape1][shape2] (NULL: geometry only). */
+int32_t pars_gpu_scalar_load(const char* path, int32_t ranks, int32_t rank, float* values, int32_t shape[3], float offset[3],
+                             float spacing[3], float size[3]);
+/* data_io::save_ftle_field (data_io.cpp:117-140): writes a block of FTLE values
+ * ([shape0][shape1][shape2] at voxel `offset`) into the scalar file of the
+ * whole `domain`, creating it (zero-filled, with `spacing`) when missing. */
+int32_t pars_gpu_ftle_save(const char* path, const int32_t domain[3], const int32_t offset[3], const int32_t shape[3],
+                           const float* values, const float spacing[3]);
+
 /* ---- ray tracer (replaces pars::ray_tracer, pars/include/pars/stages/ray_tracer.hpp:27-34) ----
  * One ray tracer per context.  Scene: one capsule (cylinder plus end spheres)
  * of the given radius per line index, coloured with vertex colour[index];

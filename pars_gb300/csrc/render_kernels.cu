@@ -72,37 +72,42 @@ __device__ __forceinline__ float key_float(unsigned int k)
 }
 
 // ---- BVH build ------------------------------------------------------------------
-// bounds[0..2]: min of the segment centres, [3..5]: their max, [6]: max |coordinate|
-__global__ void scene_bounds_kernel(const float4* __restrict__ vertices, const long long* __restrict__ prim_vertex, long long prims,
-                                    unsigned int* __restrict__ bounds)
+// bounds[0..2]: min of the segment centres, [3..5]: their max, [6]: max
+// |coordinate|.  Grid-stride over the prims, reduced per block (shuffles, then
+// shared memory), so the seven global atomics are taken once per block.
+constexpr int bounds_threads = 256;
+
+__global__ void __launch_bounds__(bounds_threads) scene_bounds_kernel(const float4* __restrict__ vertices,
+                                                                      const long long* __restrict__ prim_vertex, long long prims,
+                                                                      unsigned int* __restrict__ bounds)
 {
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY}, big = 0.0f;
-  if (k < prims)
+  float v[7] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY, 0.0f};
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < prims; k += (long long)gridDim.x * blockDim.x)
   {
     const long long g = prim_vertex[k];
     const float4 a = vertices[g], b = vertices[g + 1];
     const float c[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
-    for (int i = 0; i < 3; ++i) { lo[i] = c[i]; hi[i] = c[i]; }
-    big = fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(a.z), fabsf(b.x))), fmaxf(fabsf(b.y), fabsf(b.z)));
+    for (int i = 0; i < 3; ++i) { v[i] = fminf(v[i], c[i]); v[3 + i] = fmaxf(v[3 + i], c[i]); }
+    v[6] = fmaxf(v[6], fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(a.z), fabsf(b.x))), fmaxf(fabsf(b.y), fabsf(b.z))));
   }
   for (int off = 16; off > 0; off >>= 1)
-  {
-    for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 7; ++i)
     {
-      lo[i] = fminf(lo[i], __shfl_down_sync(0xffffffffu, lo[i], off));
-      hi[i] = fmaxf(hi[i], __shfl_down_sync(0xffffffffu, hi[i], off));
+      const float o = __shfl_down_sync(0xffffffffu, v[i], off);
+      v[i] = i < 3 ? fminf(v[i], o) : fmaxf(v[i], o);
     }
-    big = fmaxf(big, __shfl_down_sync(0xffffffffu, big, off));
-  }
-  if ((threadIdx.x & 31) == 0)
+  __shared__ float partial[bounds_threads / 32][7];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0)
+    for (int i = 0; i < 7; ++i) partial[warp][i] = v[i];
+  __syncthreads();
+  if (threadIdx.x < 7)
   {
-    for (int i = 0; i < 3; ++i)
-    {
-      atomicMin(bounds + i, float_key(lo[i]));
-      atomicMax(bounds + 3 + i, float_key(hi[i]));
-    }
-    atomicMax(bounds + 6, float_key(big));
+    const int i = threadIdx.x;
+    float r = partial[0][i];
+    for (int w = 1; w < bounds_threads / 32; ++w) r = i < 3 ? fminf(r, partial[w][i]) : fmaxf(r, partial[w][i]);
+    if (i < 3) atomicMin(bounds + i, float_key(r));
+    else atomicMax(bounds + i, float_key(r));
   }
 }
 
@@ -627,7 +632,10 @@ void render_build(pars_gpu_context& ctx, render_state& r)
   unsigned int init[8] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u, 0u, 0u};
   PARS_CUDA(cudaMemcpyAsync(r.bounds.get(), init, sizeof(init), cudaMemcpyHostToDevice, ctx.stream));
   const unsigned int blocks = blocks_for(n, 256);
-  scene_bounds_kernel<<<blocks, 256, 0, ctx.stream>>>(r.vertices, r.prim_vertex.as<long long>(), n, r.bounds.as<unsigned int>());
+  if (ctx.sm_count <= 0) PARS_CUDA(cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, ctx.device));
+  const unsigned int bound_blocks = std::min<unsigned int>(blocks_for(n, bounds_threads), unsigned(std::max(ctx.sm_count, 1)) * 4);
+  scene_bounds_kernel<<<bound_blocks, bounds_threads, 0, ctx.stream>>>(r.vertices, r.prim_vertex.as<long long>(), n,
+                                                                       r.bounds.as<unsigned int>());
   r.leaf_lo_unsorted.reserve(sizeof(float4) * n);
   r.leaf_hi_unsorted.reserve(sizeof(float4) * n);
   r.keys.reserve(sizeof(unsigned long long) * n * 2);

@@ -137,6 +137,11 @@ SIGNATURES = {
     "pars_gpu_service_result_image": [_P, _I64, _P, _P],
     "pars_gpu_service_profile_enable": [_P, _I32],
     "pars_gpu_service_profile_get": [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)],
+    "pars_gpu_raw_info": [ctypes.c_char_p, ctypes.POINTER(_I32), _P, _P],
+    "pars_gpu_raw_write": [ctypes.c_char_p, _I32, _P, _P, _P],
+    "pars_gpu_field_load": [_P, ctypes.c_char_p, _I32, _I32, ctypes.POINTER(_I32), ctypes.POINTER(PartitionInfo)],
+    "pars_gpu_scalar_load": [ctypes.c_char_p, _I32, _I32, _P, _P, _P, _P, _P],
+    "pars_gpu_ftle_save": [ctypes.c_char_p, _P, _P, _P, _P, _P],
     "pars_gpu_ray_tracer_set_volume": [_P, _P, _P, _P, _P],
     "pars_gpu_ray_tracer_set_volume_device": [_P, _P, _P, _P, _P],
     "pars_gpu_ray_tracer_clear_volume": [_P],
@@ -419,6 +424,14 @@ class Context:
         self._call("pars_gpu_batch_tuned", job_class, ctypes.byref(v), ctypes.byref(t))
         return v.value, t.value
 
+    # -- field files -----------------------------------------------------------------
+    def field_load(self, path, ranks=1, rank=0):
+        """Loads a rank's ghosted block of a vector field file; returns (handle, partition dict)."""
+        h, info = _I32(), PartitionInfo()
+        self._call("pars_gpu_field_load", os.fsencode(path), ranks, rank, ctypes.byref(h), ctypes.byref(info))
+        return h.value, {"grid": np.array(info.grid_size), "block": np.array(info.block_size), "offset": np.array(info.offset),
+                         "ghosted": np.array(info.ghosted_block_size), "neighbors": np.array(info.neighbor_rank)}
+
     # -- ray tracer (pars::ray_tracer) -------------------------------------------------
     def ray_tracer_set_volume(self, values, offset, spacing):
         """values: [X, Y, Z] FP32 host array."""
@@ -491,6 +504,50 @@ class Context:
         n = _I64()
         self._call("pars_gpu_launch_count", ctypes.byref(n))
         return n.value
+
+
+# -- field files (pa::data_io) ----------------------------------------------------------
+def raw_write(path, data, spacing):
+    """Writes a dataset: data [X, Y, Z, 3] (vector field) or [X, Y, Z] (scalar)."""
+    data = np.ascontiguousarray(data, np.float32)
+    components = 3 if data.ndim == 4 else 1
+    shape = np.array(data.shape[:3], np.int64)
+    sp = _f3(spacing)
+    status = library().pars_gpu_raw_write(os.fsencode(path), components, _ptr(shape), _ptr(sp), _ptr(data))
+    if status:
+        raise ParsGpuError(status, "pars_gpu_raw_write")
+
+
+def raw_info(path):
+    """(components, shape, raw spacing) of a field file."""
+    c, shape, sp = _I32(), np.zeros(3, np.int64), np.zeros(3, np.float32)
+    status = library().pars_gpu_raw_info(os.fsencode(path), ctypes.byref(c), _ptr(shape), _ptr(sp))
+    if status:
+        raise ParsGpuError(status, "pars_gpu_raw_info")
+    return c.value, tuple(int(x) for x in shape), sp
+
+
+def scalar_load(path, ranks=1, rank=0):
+    """A rank's ghosted block of a scalar field file: (values [X, Y, Z], offset, spacing, size)."""
+    lib = library()
+    shape, o, sp, sz = np.zeros(3, np.int32), np.zeros(3, np.float32), np.zeros(3, np.float32), np.zeros(3, np.float32)
+    status = lib.pars_gpu_scalar_load(os.fsencode(path), ranks, rank, None, _ptr(shape), _ptr(o), _ptr(sp), _ptr(sz))
+    if status:
+        raise ParsGpuError(status, "pars_gpu_scalar_load")
+    values = np.zeros(tuple(shape), np.float32)
+    status = lib.pars_gpu_scalar_load(os.fsencode(path), ranks, rank, _ptr(values), _ptr(shape), _ptr(o), _ptr(sp), _ptr(sz))
+    if status:
+        raise ParsGpuError(status, "pars_gpu_scalar_load")
+    return values, o, sp, sz
+
+
+def ftle_save(path, domain, offset, values, spacing=(1.0, 1.0, 1.0)):
+    """Writes a block of FTLE values at voxel `offset` into the file of the whole `domain`."""
+    values = np.ascontiguousarray(values, np.float32)
+    d, o, s, sp = _i3(domain), _i3(offset), _i3(values.shape), _f3(spacing)
+    status = library().pars_gpu_ftle_save(os.fsencode(path), _ptr(d), _ptr(o), _ptr(s), _ptr(values), _ptr(sp))
+    if status:
+        raise ParsGpuError(status, "pars_gpu_ftle_save")
 
 
 def image_encode(rgba):
