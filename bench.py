@@ -243,13 +243,25 @@ def run_render(args):
         ctx.ray_tracer_set_image_size(width, height)
         ctx.ray_tracer_set_camera(*camera)
 
+        phases = {"set_integral_curves": 0.0, "trace": 0.0, "serialize": 0.0}
+        frame = np.zeros((height, width, 4), np.uint8)          # the client's image buffer, reused
+
         def image():
+            t = [time.perf_counter()]
             ctx.ray_tracer_set_integral_curves(radius)
+            t.append(time.perf_counter())
             ctx.ray_tracer_trace(1)
-            return ctx.ray_tracer_serialize()
+            t.append(time.perf_counter())
+            out = ctx.ray_tracer_serialize(out=frame)
+            t.append(time.perf_counter())
+            for k, phase in enumerate(phases):
+                phases[phase] += t[k + 1] - t[k]
+            return out
 
         for _ in range(max(args.warmup, 3)):
             image()
+        for phase in phases:
+            phases[phase] = 0.0
         ctx.profile_enable(True)
         ctx.profile_reset()
         t0 = time.perf_counter()
@@ -267,6 +279,7 @@ def run_render(args):
         cpu = time.perf_counter() - c0
         scenes.append({"scene": name, "segments": segments, "volume": vol is not None,
                        "ms_per_image": 1e3 * wall, "images_per_s": 1.0 / wall,
+                       "call_ms": {k: 1e3 * v / args.steps for k, v in phases.items()},
                        "bvh_build_ms": build_ms / args.steps, "render_ms": render_ms / args.steps,
                        "rays_per_s": width * height / (1e-3 * render_ms / args.steps),
                        "cpu_restatement_ms_per_image": 1e3 * cpu, "cpu_threads": port.max_threads(),

@@ -475,11 +475,15 @@ class Context:
     def ray_tracer_trace(self, iterations=1):
         self._call("pars_gpu_ray_tracer_trace", iterations)
 
-    def ray_tracer_serialize(self):
-        """The image as a [height, width, 4] uint8 array (sRGB RGBA8, rows from the top)."""
+    def ray_tracer_serialize(self, out=None):
+        """The image as a [height, width, 4] uint8 array (sRGB RGBA8, rows from
+        the top), into `out` when given (a C-contiguous array of that shape)."""
         size = np.zeros(2, np.int32)
         self._call("pars_gpu_ray_tracer_serialize", None, _ptr(size))
-        out = np.zeros((size[1], size[0], 4), np.uint8)
+        if out is None:
+            out = np.zeros((size[1], size[0], 4), np.uint8)
+        if out.shape != (size[1], size[0], 4) or out.dtype != np.uint8 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a C-contiguous uint8 array of shape (height, width, 4)")
         self._call("pars_gpu_ray_tracer_serialize", _ptr(out), _ptr(size))
         return out
 
