@@ -173,7 +173,9 @@ int32_t pars_gpu_partition(int32_t ranks, int32_t rank, const int32_t domain_siz
 /* ---- particle_tracer (pa/source/stages/particle_tracer.cpp:39-56, 210-337, 402-409)
  * Traces host particles through one block (`field`, no neighbours: particles
  * leaving it are dropped) and prunes, leaving the curves on the device.
- * integrator: PARS_EULER or PARS_RUNGE_KUTTA_4 (others: PARS_ERR_UNSUPPORTED). */
+ * integrator: any pars_integrator with PARS_STAGES_FROZEN (the reference's
+ * scheme, every stepper of integrators.hpp:16-23); PARS_EULER or
+ * PARS_RUNGE_KUTTA_4 with PARS_STAGES_RESAMPLED (others: PARS_ERR_UNSUPPORTED). */
 int32_t pars_gpu_trace(pars_gpu_context* context, int32_t field, const pars_particle* particles, int64_t count,
                        int32_t integrator, int32_t stage_mode, float step_size, pars_gpu_trace_summary* summary);
 /* Same with the particles already in DEVICE memory. */
@@ -224,7 +226,8 @@ int32_t pars_gpu_color_generate(pars_gpu_context* context, const float* vertices
  * one particle per voxel of an int(shape * scale) grid with spacing
  * spacing / scale, advected with particle_advector's rules
  * (particle_advector.cpp:74-139; at most iterations - 1 steps).  The flow map
- * becomes a new field handle (*flow_map) resident on the device. */
+ * becomes a new field handle (*flow_map) resident on the device.  Integrators
+ * as for pars_gpu_trace. */
 int32_t pars_gpu_flow_map_generate(pars_gpu_context* context, int32_t field, int32_t iterations, float resolution_scale,
                                    int32_t integrator, int32_t stage_mode, float step_size, int32_t* flow_map, int64_t* steps);
 /* FTLE of a flow-map field: central-difference gradient (one-sided at the
@@ -256,7 +259,7 @@ int32_t pars_gpu_unsteady_field_upload_device(pars_gpu_context* context, const f
 typedef struct pars_gpu_batch_job
 {
   int32_t      field;               /* field handle (steady or unsteady) */
-  int32_t      integrator;          /* PARS_EULER or PARS_RUNGE_KUTTA_4 */
+  int32_t      integrator;          /* PARS_EULER or PARS_RUNGE_KUTTA_4 (re-sampled stages) */
   int32_t      stage_mode;          /* PARS_STAGES_RESAMPLED (PARS_STAGES_FROZEN: velocity of the step start) */
   int32_t      max_steps;
   float        step_size;

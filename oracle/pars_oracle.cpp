@@ -144,41 +144,101 @@ inline bool is_zero(const float* v)
 
 // ---------------------------------------------------------------------------
 // Integrator step with the reference's frozen velocity (particle_tracer.cpp:
-// 315-334): the right-hand side returns the velocity sampled at the step start
-// for every stage, so an explicit RK scheme reduces to
-//   out = 1 * x + (b_1 h) v + ... + (b_s h) v      (left to right, FP32)
-// with b_i = float(p)/float(q) formed in FP32 and multiplied by h.
+// 315-334, particle_advector.cpp:115-130): the right-hand side returns the
+// velocity sampled at the step start for every stage.  For the eight steppers
+// of integrators.hpp:16-23, with the odeint 1.69 schemes written out from
+// their published tableaux (FP32, left to right, b_i = float(p)/float(q)):
+//  * explicit RK (euler, runge_kutta4, cash_karp54, dopri5, fehlberg78) and
+//    adams_bashforth_moulton<2> (AB2 predictor, trapezoidal corrector):
+//      out = 1 * x + (b_1 h) v + ... + (b_s h) v, zero weights included;
+//  * modified_midpoint (two substeps, H = h/2):
+//      z1 = x + H v,  z2 = x + (2H) v,  out = 0.5 z2 + 0.5 z1 + (0.5 H) v;
+//  * adams_bashforth<2>: the first step of a particle is runge_kutta4, later
+//    steps out = x + (1.5 h) v_n + (-0.5 h) v_{n-1}; the reference copies the
+//    stepper per particle and per tracing call, so the history starts afresh.
 // ---------------------------------------------------------------------------
-enum integrator_kind { euler = 0, runge_kutta_4 = 2 };
+enum integrator_kind { euler = 0, modified_midpoint = 1, runge_kutta_4 = 2, cash_karp_54 = 3, dormand_prince_5 = 4,
+                       fehlberg_78 = 5, adams_bashforth_2 = 6, adams_bashforth_moulton_2 = 7 };
 enum stage_mode { frozen = 0, resampled = 1 };
+enum frozen_method { weighted_sum = 0, midpoint = 1, multistep = 2 };
 
 struct frozen_weights
 {
+  int   method = weighted_sum;
   int   count = 0;
-  float c[4]  = {0, 0, 0, 0};
+  float c[16] = {};
+};
+
+// Per-particle history of the multistep scheme.
+struct frozen_history
+{
+  float v[3] = {0, 0, 0};
+  bool  started = false;
 };
 
 frozen_weights make_frozen_weights(int integrator, float h)
 {
   frozen_weights w;
-  if (integrator == euler) { w.count = 1; w.c[0] = h; }
-  else
+  auto fill = [&](std::initializer_list<std::pair<int, int>> b) {
+    w.count = 0;
+    for (auto& q : b) w.c[w.count++] = (float(q.first) / float(q.second)) * h;
+  };
+  switch (integrator)
   {
-    const float b[4] = {1.0f / 6.0f, 1.0f / 3.0f, 1.0f / 3.0f, 1.0f / 6.0f};
-    w.count = 4;
-    for (int i = 0; i < 4; ++i) w.c[i] = b[i] * h;
+  case euler: w.count = 1; w.c[0] = h; break;
+  case modified_midpoint:
+  {
+    const float H = h / 2.0f;
+    w.method = midpoint;
+    w.c[0] = H; w.c[1] = 2.0f * H; w.c[2] = 0.5f * H;
+    break;
+  }
+  case cash_karp_54: fill({{37, 378}, {0, 1}, {250, 621}, {125, 594}, {0, 1}, {512, 1771}}); break;
+  case dormand_prince_5: fill({{35, 384}, {0, 1}, {500, 1113}, {125, 192}, {-2187, 6784}, {11, 84}}); break;
+  case fehlberg_78:
+    fill({{41, 840}, {0, 1}, {0, 1}, {0, 1}, {0, 1}, {34, 105}, {9, 35}, {9, 35}, {9, 280}, {9, 280}, {41, 840}, {0, 1}, {0, 1}});
+    break;
+  case adams_bashforth_moulton_2: w.count = 2; w.c[0] = h * (1.0f / 2.0f); w.c[1] = h * (1.0f / 2.0f); break;
+  case adams_bashforth_2:
+    fill({{1, 6}, {1, 3}, {1, 3}, {1, 6}});           // first step: runge_kutta4
+    w.method = multistep;
+    w.c[4] = h * (3.0f / 2.0f);
+    w.c[5] = h * (-1.0f / 2.0f);
+    break;
+  default: fill({{1, 6}, {1, 3}, {1, 3}, {1, 6}}); break;   // runge_kutta_4
   }
   return w;
 }
 
-inline void frozen_step(const frozen_weights& w, const float* x, const float* v, float* out)
+inline void frozen_step(const frozen_weights& w, const float* x, const float* v, float* out, frozen_history& hist)
 {
   const float dxdt[4] = {v[0], v[1], v[2], 0.0f};
-  for (int c = 0; c < 4; ++c)
+  if (w.method == midpoint)
   {
-    float acc = 1.0f * x[c];
-    for (int i = 0; i < w.count; ++i) acc = acc + w.c[i] * dxdt[c];
-    out[c] = acc;
+    for (int c = 0; c < 4; ++c)
+    {
+      const float z1 = 1.0f * x[c] + w.c[0] * dxdt[c];
+      const float z2 = 1.0f * x[c] + w.c[1] * dxdt[c];
+      out[c] = 0.5f * z2 + 0.5f * z1 + w.c[2] * dxdt[c];
+    }
+    return;
+  }
+  if (w.method == multistep && hist.started)
+  {
+    const float previous[4] = {hist.v[0], hist.v[1], hist.v[2], 0.0f};
+    for (int c = 0; c < 4; ++c) out[c] = 1.0f * x[c] + w.c[4] * dxdt[c] + w.c[5] * previous[c];
+  }
+  else
+    for (int c = 0; c < 4; ++c)
+    {
+      float acc = 1.0f * x[c];
+      for (int i = 0; i < w.count; ++i) acc = acc + w.c[i] * dxdt[c];
+      out[c] = acc;
+    }
+  if (w.method == multistep)
+  {
+    for (int c = 0; c < 3; ++c) hist.v[c] = v[c];
+    hist.started = true;
   }
 }
 
@@ -325,6 +385,7 @@ long long trace_particle(const field& f, const frozen_weights& w, const particle
   std::memcpy(last.v, p.position, 16);
   out.push_back(last);
   long long steps = 0;
+  frozen_history hist;
   for (long long i = 1; i < (long long)p.remaining_iterations; ++i)
   {
     if (i == (long long)p.remaining_iterations - 1) { out.push_back(termination_vertex); break; }
@@ -339,7 +400,7 @@ long long trace_particle(const field& f, const frozen_weights& w, const particle
     interpolate(f, last.v, v);
     if (is_zero(v)) { out.push_back(termination_vertex); break; }
     vec4 next;
-    frozen_step(w, last.v, v, next.v);
+    frozen_step(w, last.v, v, next.v, hist);
     out.push_back(next);
     last = next;
     ++steps;
@@ -825,6 +886,7 @@ long long orc_flow_map(const float* xyz, const int dims[3], const float offset[3
     for (int i = 0; i < 3; ++i) pos[i] = offset[i] + fm_spacing[i] * float(idx[i]);
     pos[3] = 0.0f;
     bool finished = false;
+    frozen_history hist;
     for (long long i = 1; i < iterations; ++i)
     {
       if (!contains(f, pos)) { finished = true; break; }
@@ -832,7 +894,7 @@ long long orc_flow_map(const float* xyz, const int dims[3], const float offset[3
       interpolate(f, pos, v);
       if (is_zero(v)) { finished = true; break; }
       float next[4];
-      frozen_step(w, pos, v, next);
+      frozen_step(w, pos, v, next, hist);
       std::memcpy(pos, next, 16);
       ++steps;
       if (i + 1 == iterations) { finished = true; break; }

@@ -259,32 +259,74 @@ __device__ __forceinline__ bool is_zero(const float3& v)
   return fabsf(v.x) <= precision && fabsf(v.y) <= precision && fabsf(v.z) <= precision;
 }
 
-// Integrator parameters.  FROZEN: out = 1*x + c_0 v + ... + c_{k-1} v with
-// c_i = b_i * h (b_i in FP32), accumulated left to right.  RESAMPLED: classical
-// RK4 (or Euler) with a sample at each stage point.
+// Integrator parameters.  RESAMPLED: classical RK4 (or Euler) with a sample
+// at each stage point.  FROZEN (the reference's scheme: every stage sees the
+// velocity v sampled at the step start), by method:
+//  * weighted sum (Euler, RK4, Cash-Karp 5(4), Dormand-Prince 5, Fehlberg 7(8),
+//    Adams-Bashforth-Moulton 2): out = 1*x + c_0 v + ... + c_{k-1} v with
+//    c_i = b_i * h (b_i in FP32), accumulated left to right, zero weights
+//    included;
+//  * modified midpoint (two substeps, H = h/2): z1 = x + c_0 v, z2 = x + c_1 v,
+//    out = 0.5 z2 + 0.5 z1 + c_2 v (c_0 = H, c_1 = 2H, c_2 = 0.5H);
+//  * Adams-Bashforth 2: the particle's first step is the weighted sum (RK4
+//    weights), later ones out = x + c_4 v_n + c_5 v_{n-1} (c_4 = 1.5 h,
+//    c_5 = -0.5 h), with the previous step's velocity kept per particle.
+enum frozen_method { frozen_weighted_sum = 0, frozen_midpoint = 1, frozen_multistep = 2 };
+
 struct step_rule
 {
   int   frozen;      // 1 = frozen velocity, 0 = resampled stages
-  int   rk4;         // 1 = RK4, 0 = Euler
-  int   count;       // number of frozen coefficients
-  float c[4];        // frozen coefficients b_i * h
+  int   rk4;         // resampled: 1 = RK4, 0 = Euler
+  int   count;       // frozen weighted sum: number of coefficients
+  int   method;      // frozen_method
+  float c[16];       // frozen coefficients
   float h;           // step size
 };
 
-__device__ __forceinline__ float frozen_component(const step_rule& r, float x, float v)
+// The multistep scheme's per-particle history.
+struct frozen_history
 {
-  float acc = x;   // 1 * x is exact
-  #pragma unroll
-  for (int i = 0; i < 4; ++i)
-    if (i < r.count) acc = __fadd_rn(acc, __fmul_rn(r.c[i], v));
-  return acc;
+  float3 v = make_float3(0.f, 0.f, 0.f);
+  int    started = 0;
+};
+
+__device__ __forceinline__ float midpoint_component(const step_rule& r, float x, float v)
+{
+  const float z1 = __fadd_rn(x, __fmul_rn(r.c[0], v));
+  const float z2 = __fadd_rn(x, __fmul_rn(r.c[1], v));
+  return __fadd_rn(__fadd_rn(__fmul_rn(0.5f, z2), __fmul_rn(0.5f, z1)), __fmul_rn(r.c[2], v));
+}
+
+__device__ __forceinline__ float multistep_component(const step_rule& r, float x, float v, float previous)
+{
+  return __fadd_rn(__fadd_rn(x, __fmul_rn(r.c[4], v)), __fmul_rn(r.c[5], previous));
 }
 
 // FROZEN step from x with the velocity v = v(x): the reference's operation order.
-__device__ __forceinline__ float4 frozen_step(const step_rule& r, const float4& x, const float3& v)
+__device__ __forceinline__ float4 frozen_step(const step_rule& r, const float4& x, const float3& v, frozen_history& hist)
 {
-  return make_float4(frozen_component(r, x.x, v.x), frozen_component(r, x.y, v.y),
-                     frozen_component(r, x.z, v.z), frozen_component(r, x.w, 0.0f));
+  float4 out;
+  if (r.method == frozen_midpoint)
+    out = make_float4(midpoint_component(r, x.x, v.x), midpoint_component(r, x.y, v.y), midpoint_component(r, x.z, v.z),
+                      midpoint_component(r, x.w, 0.0f));
+  else if (r.method == frozen_multistep && hist.started)
+    out = make_float4(multistep_component(r, x.x, v.x, hist.v.x), multistep_component(r, x.y, v.y, hist.v.y),
+                      multistep_component(r, x.z, v.z, hist.v.z), multistep_component(r, x.w, 0.0f, 0.0f));
+  else
+  {
+    // each component: 1 * x (exact) + c_0 v + c_1 v + ..., left to right
+    out = x;
+    for (int i = 0; i < r.count; ++i)
+    {
+      const float c = r.c[i];
+      out.x = __fadd_rn(out.x, __fmul_rn(c, v.x));
+      out.y = __fadd_rn(out.y, __fmul_rn(c, v.y));
+      out.z = __fadd_rn(out.z, __fmul_rn(c, v.z));
+      out.w = __fadd_rn(out.w, __fmul_rn(c, 0.0f));
+    }
+  }
+  if (r.method == frozen_multistep) { hist.v = v; hist.started = 1; }
+  return out;
 }
 
 // Adds delta to the compensated position (hi, lo) with Knuth's error-free
@@ -446,7 +488,7 @@ __device__ __forceinline__ void unsteady_step(const field_view& f, const time_ax
 {
   if (r.frozen || !r.rk4)
   {
-    const float scale = r.frozen && r.rk4 ? (r.c[0] + r.c[1] + r.c[2] + r.c[3]) : r.h;
+    const float scale = r.h;
     compensated_add(x.x, lo.x, scale * k1.x);
     compensated_add(x.y, lo.y, scale * k1.y);
     compensated_add(x.z, lo.z, scale * k1.z);

@@ -33,7 +33,7 @@ struct flow_map_args
 };
 
 template <bool FROZEN>
-__global__ void __launch_bounds__(256) flow_map_kernel(const flow_map_args a)
+__global__ void __launch_bounds__(256) flow_map_kernel(const __grid_constant__ flow_map_args a)
 {
   const long long total = (long long)a.px * a.py * a.pz;
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -48,6 +48,7 @@ __global__ void __launch_bounds__(256) flow_map_kernel(const flow_map_args a)
     bool finished = false;
     float3 lo = make_float3(0.0f, 0.0f, 0.0f);
     corner_cache cache;
+    frozen_history hist;
     for (int it = 1; it < a.iterations; ++it)
     {
       float3 v;
@@ -56,7 +57,7 @@ __global__ void __launch_bounds__(256) flow_map_kernel(const flow_map_args a)
       else        inside = sample_start(a.f, cache, pos, v);
       if (!inside) { finished = true; break; }
       if (is_zero(v)) { finished = true; break; }
-      if (FROZEN) pos = frozen_step(a.rule, pos, v);
+      if (FROZEN) pos = frozen_step(a.rule, pos, v, hist);
       else resampled_step_cached(a.f, cache, a.rule, pos, lo, v);
       ++steps;
       if (it + 1 == a.iterations) { finished = true; break; }

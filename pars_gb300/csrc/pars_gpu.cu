@@ -222,27 +222,60 @@ std::unique_ptr<field_entry> make_field(const int32_t shape[3], const float offs
   return entry;
 }
 
+// FP32 quotient p / q and product with h, each rounded once (kept out of
+// constant folding at another precision).
+float weight_times(int p, int q, float h)
+{
+  const volatile float num = float(p), den = float(q);
+  const volatile float b = num / den;
+  const volatile float c = b * h;
+  return c;
+}
+
 step_rule make_rule(int integrator, int stage_mode, float h)
 {
-  if (integrator != PARS_EULER && integrator != PARS_RUNGE_KUTTA_4)
-    throw error(PARS_ERR_UNSUPPORTED, "integrator " + std::to_string(integrator) + " is not supported (Euler and RK4 are)");
   PARS_REQUIRE(stage_mode == PARS_STAGES_FROZEN || stage_mode == PARS_STAGES_RESAMPLED, "unknown stage mode");
+  PARS_REQUIRE(integrator >= PARS_EULER && integrator <= PARS_ADAMS_BASHFORTH_MOULTON_2, "unknown integrator");
+  if (stage_mode == PARS_STAGES_RESAMPLED && integrator != PARS_EULER && integrator != PARS_RUNGE_KUTTA_4)
+    throw error(PARS_ERR_UNSUPPORTED, "integrator " + std::to_string(integrator) +
+                " runs with frozen stages only (re-sampled stages: Euler and RK4)");
   step_rule r {};
   r.frozen = stage_mode == PARS_STAGES_FROZEN ? 1 : 0;
   r.rk4 = integrator == PARS_RUNGE_KUTTA_4 ? 1 : 0;
   r.h = h;
-  // Frozen coefficients b_i * h, b_i formed in FP32 (1.0f/6.0f etc.) as the
-  // generic RK scale-sum does; host FP32 products are IEEE round-to-nearest.
-  if (r.rk4)
+  r.method = frozen_weighted_sum;
+  // Frozen coefficients (the odeint 1.69 schemes of integrators.hpp:16-23 with
+  // every stage seeing the step-start velocity): b_i * h, b_i = float(p) /
+  // float(q) in FP32, as the generic RK scale-sum forms them.
+  auto weights = [&](std::initializer_list<std::pair<int, int>> b) {
+    r.count = 0;
+    for (const auto& q : b) r.c[r.count++] = q.first == 0 ? 0.0f * h : weight_times(q.first, q.second, h);
+  };
+  switch (integrator)
   {
-    const volatile float b0 = 1.0f / 6.0f, b1 = 1.0f / 3.0f;
-    r.count = 4;
-    r.c[0] = b0 * h; r.c[1] = b1 * h; r.c[2] = b1 * h; r.c[3] = b0 * h;
+  case PARS_EULER: r.count = 1; r.c[0] = h; break;
+  case PARS_MODIFIED_MIDPOINT:
+  {
+    const volatile float H = h / 2.0f;
+    r.method = frozen_midpoint;
+    r.c[0] = H;
+    r.c[1] = 2.0f * H;
+    r.c[2] = 0.5f * H;
+    break;
   }
-  else
-  {
-    r.count = 1;
-    r.c[0] = h;
+  case PARS_RUNGE_KUTTA_CASH_KARP_54: weights({{37, 378}, {0, 1}, {250, 621}, {125, 594}, {0, 1}, {512, 1771}}); break;
+  case PARS_RUNGE_KUTTA_DORMAND_PRINCE_5: weights({{35, 384}, {0, 1}, {500, 1113}, {125, 192}, {-2187, 6784}, {11, 84}}); break;
+  case PARS_RUNGE_KUTTA_FEHLBERG_78:
+    weights({{41, 840}, {0, 1}, {0, 1}, {0, 1}, {0, 1}, {34, 105}, {9, 35}, {9, 35}, {9, 280}, {9, 280}, {41, 840}, {0, 1}, {0, 1}});
+    break;
+  case PARS_ADAMS_BASHFORTH_2:
+    weights({{1, 6}, {1, 3}, {1, 3}, {1, 6}});          // the first step is RK4
+    r.method = frozen_multistep;
+    r.c[4] = weight_times(3, 2, h);
+    r.c[5] = weight_times(-1, 2, h);
+    break;
+  case PARS_ADAMS_BASHFORTH_MOULTON_2: weights({{1, 2}, {1, 2}}); break;
+  default: weights({{1, 6}, {1, 3}, {1, 3}, {1, 6}}); break;    // RK4
   }
   return r;
 }

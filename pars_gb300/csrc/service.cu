@@ -948,8 +948,10 @@ int32_t pars_gpu_service_submit(pars_gpu_service* svc, const uint8_t* message, i
     if (r->trace_curves || r->kind == ftle)
     {
       r->integrator = integrator_of(r->s.particle_tracing_integrator);
-      if (r->integrator != PARS_EULER && r->integrator != PARS_RUNGE_KUTTA_4)
-        throw error(PARS_ERR_UNSUPPORTED, "integrator '" + r->s.particle_tracing_integrator + "' is not supported");
+      if (r->integrator < 0) throw error(PARS_ERR_UNSUPPORTED, "unknown integrator '" + r->s.particle_tracing_integrator + "'");
+      // every integrator with the reference's frozen stages; re-sampled stages: Euler and RK4
+      if (r->stage_mode == PARS_STAGES_RESAMPLED && r->integrator != PARS_EULER && r->integrator != PARS_RUNGE_KUTTA_4)
+        throw error(PARS_ERR_UNSUPPORTED, "integrator '" + r->s.particle_tracing_integrator + "' runs in \"reference\" mode only");
       PARS_REQUIRE(r->s.particle_tracing_step_size != 0.0f, "particle_tracing_step_size must be non-zero");
     }
     r->color_mode = color_of(r->s.color_generation_mode);

@@ -27,7 +27,9 @@ struct lane_particle
   float3       lo = make_float3(0.f, 0.f, 0.f);
   corner_cache cache;
   field_view   f {};
-  step_rule    rule {};
+  step_rule    rule {};                      // re-sampled stages: the rule's h and scheme
+  const step_rule* frozen_rule = nullptr;    // frozen scheme: the rule in parameter / global memory
+  frozen_history   hist;                     // frozen multistep scheme: the previous step's velocity
   float4*      out = nullptr;
 };
 
@@ -38,6 +40,8 @@ __device__ __forceinline__ void particle_start(const trace_launch& a, lane_parti
   p.block = a.block_of ? a.block_of[i] : 0;
   p.f = a.blocks[p.block].field;
   p.rule = a.block_rules ? a.block_rules[p.block] : a.rule;
+  p.frozen_rule = a.block_rules ? a.block_rules + p.block : &a.rule;
+  p.hist = frozen_history();
   const float4* record = reinterpret_cast<const float4*>(a.particles + i);
   p.last = record[0];
   p.N = __float_as_int(record[1].x);   // remaining_iterations
@@ -98,7 +102,7 @@ __device__ __forceinline__ bool particle_iteration(const trace_launch& a, lane_p
     else
     {
       float4 next;
-      if (FROZEN) next = frozen_step(p.rule, p.last, v);
+      if (FROZEN) next = frozen_step(*p.frozen_rule, p.last, v, p.hist);
       else { next = p.last; resampled_step_cached(p.f, p.cache, p.rule, next, p.lo, v); }
       p.out[p.it] = next;
       ++p.written;
@@ -125,7 +129,7 @@ __device__ __forceinline__ void add_steps(const trace_launch& a, unsigned int st
 // One particle per thread: for launches with no more particles than resident
 // lanes, where refilling cannot help and warp votes would only add latency.
 template <bool FROZEN>
-__global__ void __launch_bounds__(128) trace_kernel(const trace_launch a)
+__global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ trace_launch a)
 {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned int steps = 0;
@@ -145,7 +149,7 @@ __global__ void __launch_bounds__(128) trace_kernel(const trace_launch a)
 // and its exit-queue entry, so the result does not depend on which lane traced
 // it.
 template <bool FROZEN>
-__global__ void __launch_bounds__(128) trace_persistent_kernel(const trace_launch a, int pool_size)
+__global__ void __launch_bounds__(128) trace_persistent_kernel(const __grid_constant__ trace_launch a, int pool_size)
 {
   const int lane = threadIdx.x & 31;
   const unsigned lanes_below = (1u << lane) - 1u;

@@ -6,7 +6,9 @@ inputs; the inputs and outputs are saved as compressed .npz files.  The
 fixtures pin the CPU restatement (oracle/pars_oracle.cpp) and, through it, the
 GPU kernels.  Needs the reference checkout, so it runs only where that exists:
 
-    oracle/build_ref.sh && python tests/golden/make_golden.py
+    oracle/build_ref.sh && python tests/golden/make_golden.py [integrators]
+
+("integrators" writes only integrators_abc24.npz.)
 """
 import os
 import sys
@@ -168,5 +170,35 @@ def main():
     print("golden fixtures written to", HERE)
 
 
+INTEGRATORS = ["euler", "modified_midpoint", "runge_kutta_4", "runge_kutta_cash_karp_54", "runge_kutta_dormand_prince_5",
+               "runge_kutta_fehlberg_78", "adams_bashforth_2", "adams_bashforth_moulton_2"]
+
+
+def integrators():
+    """Streamlines and flow maps with each of the eight steppers of
+    pa/include/pa/math/integrators.hpp:16-23 (frozen velocity, as the reference
+    integrates), through the reference's tracer and advector."""
+    ref = oracle.reference()
+    if ref is None:
+        raise SystemExit("oracle/_ref/libpars_ref.so is missing: run oracle/build_ref.sh first")
+    f = W.abc_field(24)
+    seeds = ref.seed_generate(f.offset, f.size, (f.spacing * np.float32(4)).astype(np.float32), 82)
+    g = W.abc_field(16, noise_sigma=0.01, seed=0)
+    out = {"seeds": seeds.view(np.uint8)}
+    out.update(field_arrays("field_", f))
+    out.update(field_arrays("flow_field_", g))
+    for k, name in enumerate(INTEGRATORS):
+        curves = ref.trace_single(f, seeds, k, 0.02, None, 0.5)
+        out[f"{name}_batches"] = np.array(len(curves.batches))
+        for b, batch in enumerate(curves.batches):
+            out[f"{name}_{b}_vertices"] = batch["vertices"]
+        out[f"{name}_flow"] = ref.flow_map(g, 41, 1.0, k, 0.02)
+    np.savez_compressed(os.path.join(HERE, "integrators_abc24.npz"), **out)
+    print("integrator fixtures written to", HERE)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["integrators"]:
+        integrators()
+    else:
+        main()

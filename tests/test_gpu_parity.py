@@ -94,6 +94,35 @@ def test_streamlines_match_reference_fixture(ctx, integrator, name):
     ctx.release_field(h)
 
 
+INTEGRATORS = ["euler", "modified_midpoint", "runge_kutta_4", "runge_kutta_cash_karp_54", "runge_kutta_dormand_prince_5",
+               "runge_kutta_fehlberg_78", "adams_bashforth_2", "adams_bashforth_moulton_2"]
+
+
+@pytest.mark.parametrize("k,name", list(enumerate(INTEGRATORS)))
+def test_every_integrator_matches_reference_fixture(ctx, k, name):
+    """All eight steppers of integrators.hpp:16-23 with the reference's frozen
+    stages, streamlines and flow maps, bit for bit; re-sampled stages take
+    Euler and RK4 only."""
+    from pars_gb300 import native
+    g = golden("integrators_abc24.npz")
+    h = ctx.upload_field(golden_field(g))
+    seeds = particles_from(g, "seeds")
+    s = ctx.trace(h, seeds, k, native.STAGES_FROZEN, 0.02)
+    got = ctx.curves(s["batches"], vertices=True)
+    assert len(got) == int(g[f"{name}_batches"])
+    for b, batch in enumerate(got):
+        assert np.array_equal(batch["vertices"], g[f"{name}_{b}_vertices"]), b
+    hf = ctx.upload_field(golden_field(g, "flow_field_"))
+    fm, _ = ctx.flow_map_generate(hf, 41, 1.0, k, native.STAGES_FROZEN, 0.02)
+    assert np.array_equal(ctx.download_field(fm), g[f"{name}_flow"])
+    if k not in (native.EULER, native.RUNGE_KUTTA_4):
+        with pytest.raises(native.ParsGpuError) as e:
+            ctx.trace(h, seeds, k, native.STAGES_RESAMPLED, 0.02)
+        assert e.value.status == -4
+    for x in (fm, hf, h):
+        ctx.release_field(x)
+
+
 @pytest.mark.parametrize("color", ["hsv_constant_s", "hsl_constant_l"])
 def test_streamline_hsx_colors_match_reference_fixture(ctx, color):
     g = golden("trace_abc24.npz")

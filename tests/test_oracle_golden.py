@@ -120,3 +120,23 @@ def test_reference_build_agrees_when_present(port):
     for x, y in zip(a.batches, b.batches):
         assert np.array_equal(x["vertices"], y["vertices"])
         assert_colors_equal(y["colors"], x["colors"])
+
+
+INTEGRATORS = ["euler", "modified_midpoint", "runge_kutta_4", "runge_kutta_cash_karp_54", "runge_kutta_dormand_prince_5",
+               "runge_kutta_fehlberg_78", "adams_bashforth_2", "adams_bashforth_moulton_2"]
+
+
+@pytest.mark.parametrize("k,name", list(enumerate(INTEGRATORS)))
+def test_every_integrator_matches_reference(port, k, name):
+    """The eight steppers of integrators.hpp:16-23 with the reference's frozen
+    velocity: streamlines (particle_tracer) and flow maps (particle_advector),
+    bit for bit against the reference build (odeint stand-in of oracle/ref_shim)."""
+    g = golden("integrators_abc24.npz")
+    f = golden_field(g)
+    seeds = particles_from(g, "seeds")
+    curves = port.trace_single(f, seeds, k, 0.02, None, 0.5)
+    assert len(curves.batches) == int(g[f"{name}_batches"])
+    for b, batch in enumerate(curves.batches):
+        assert np.array_equal(batch["vertices"], g[f"{name}_{b}_vertices"])
+    flow, _ = port.flow_map(golden_field(g, "flow_field_"), 41, 1.0, k, 0.02)
+    assert np.array_equal(flow, g[f"{name}_flow"])
