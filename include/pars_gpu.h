@@ -452,6 +452,15 @@ int32_t pars_gpu_scalar_load(const char* path, int32_t ranks, int32_t rank, floa
 int32_t pars_gpu_ftle_save(const char* path, const int32_t domain[3], const int32_t offset[3], const int32_t shape[3],
                            const float* values, const float spacing[3]);
 
+/* data_io::save_integral_curves (data_io.cpp:142-196): the curves as VTK XML
+ * PolyData (.vtp, raw appended data): non-termination vertices as points with
+ * colour bytes (x 255, rounded, clamped; "Colors"), one polyline per run ended
+ * by a termination vertex.  _export_vtk takes host batches (colors or an
+ * entry may be NULL), _curves_export_vtk the context's device curves. */
+int32_t pars_gpu_export_vtk(const char* path, int64_t batches, const int64_t* vertex_counts, const float* const* vertices,
+                            const float* const* colors);
+int32_t pars_gpu_curves_export_vtk(pars_gpu_context* context, const char* path);
+
 /* ---- ray tracer (replaces pars::ray_tracer, pars/include/pars/stages/ray_tracer.hpp:27-34) ----
  * One ray tracer per context.  Scene: one capsule (cylinder plus end spheres)
  * of the given radius per line index, coloured with vertex colour[index];

@@ -142,6 +142,8 @@ SIGNATURES = {
     "pars_gpu_field_load": [_P, ctypes.c_char_p, _I32, _I32, ctypes.POINTER(_I32), ctypes.POINTER(PartitionInfo)],
     "pars_gpu_scalar_load": [ctypes.c_char_p, _I32, _I32, _P, _P, _P, _P, _P],
     "pars_gpu_ftle_save": [ctypes.c_char_p, _P, _P, _P, _P, _P],
+    "pars_gpu_export_vtk": [ctypes.c_char_p, _I64, _P, _P, _P],
+    "pars_gpu_curves_export_vtk": [_P, ctypes.c_char_p],
     "pars_gpu_ray_tracer_set_volume": [_P, _P, _P, _P, _P],
     "pars_gpu_ray_tracer_set_volume_device": [_P, _P, _P, _P, _P],
     "pars_gpu_ray_tracer_clear_volume": [_P],
@@ -424,6 +426,10 @@ class Context:
         self._call("pars_gpu_batch_tuned", job_class, ctypes.byref(v), ctypes.byref(t))
         return v.value, t.value
 
+    def curves_export_vtk(self, path):
+        """The context's curves as VTK XML PolyData (data_io::save_integral_curves)."""
+        self._call("pars_gpu_curves_export_vtk", os.fsencode(path))
+
     # -- field files -----------------------------------------------------------------
     def field_load(self, path, ranks=1, rank=0):
         """Loads a rank's ghosted block of a vector field file; returns (handle, partition dict)."""
@@ -552,6 +558,20 @@ def ftle_save(path, domain, offset, values, spacing=(1.0, 1.0, 1.0)):
     status = library().pars_gpu_ftle_save(os.fsencode(path), _ptr(d), _ptr(o), _ptr(s), _ptr(values), _ptr(sp))
     if status:
         raise ParsGpuError(status, "pars_gpu_ftle_save")
+
+
+def export_vtk(path, batches):
+    """Writes curves (a list of (vertices (n,4), colours (n,4) or None)) as VTK
+    XML PolyData, as data_io::save_integral_curves assembles them."""
+    keep = [(np.ascontiguousarray(v, np.float32).reshape(-1, 4),
+             None if c is None else np.ascontiguousarray(c, np.float32).reshape(-1, 4)) for v, c in batches]
+    n = len(keep)
+    counts = np.array([len(v) for v, _ in keep] or [0], np.int64)
+    vp = (_P * max(n, 1))(*[v.ctypes.data for v, _ in keep])
+    cp = (_P * max(n, 1))(*[None if c is None else c.ctypes.data for _, c in keep])
+    status = library().pars_gpu_export_vtk(os.fsencode(path), n, _ptr(counts), ctypes.cast(vp, _P), ctypes.cast(cp, _P))
+    if status:
+        raise ParsGpuError(status, "pars_gpu_export_vtk")
 
 
 def image_encode(rgba):
