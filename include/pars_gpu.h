@@ -343,6 +343,13 @@ typedef struct pars_gpu_request_info
   int32_t image_size[2];  /* width, height of the request's image (0, 0 without one) */
 } pars_gpu_request_info;
 
+/* The binary `settings` message of its JSON form (the benchmark's settings
+ * files, pars/source/service.cpp:72-77; the proto3 JSON mapping: field names
+ * or lowerCamelCase names, numbers or numeric strings, unknown keys rejected).
+ * *message_length receives the size; message (when not NULL, capacity large
+ * enough) the bytes.  Host-only. */
+int32_t pars_gpu_settings_from_json  (const char* json, int64_t length, uint8_t* message, int64_t capacity,
+                                      int64_t* message_length);
 /* Decodes a `settings` message (host-only; no device needed). */
 int32_t pars_gpu_settings_decode     (const uint8_t* message, int64_t length, pars_gpu_settings_summary* settings);
 int32_t pars_gpu_service_create      (pars_gpu_service** service, int32_t device, int64_t budget_bytes, int32_t lanes,

@@ -754,6 +754,25 @@ using namespace pars;
 #pragma GCC visibility push(default)
 extern "C" {
 
+int32_t pars_gpu_settings_from_json(const char* json, int64_t length, uint8_t* message, int64_t capacity, int64_t* message_length)
+{
+  if ((!json && length > 0) || length < 0 || !message_length) return PARS_ERR_INVALID_ARGUMENT;
+  try
+  {
+    settings s;
+    std::string problem;
+    if (!settings_from_json(json, std::size_t(length), s, problem)) return PARS_ERR_INVALID_ARGUMENT;
+    const std::vector<uint8_t> bytes = encode_settings(s);
+    *message_length = int64_t(bytes.size());
+    if (!message) return PARS_OK;
+    if (capacity < int64_t(bytes.size())) return PARS_ERR_INVALID_ARGUMENT;
+    if (!bytes.empty()) std::memcpy(message, bytes.data(), bytes.size());
+    return PARS_OK;
+  }
+  catch (const std::bad_alloc&) { return PARS_ERR_OUT_OF_MEMORY; }
+  catch (...) { return PARS_ERR_STATE; }
+}
+
 int32_t pars_gpu_settings_decode(const uint8_t* bytes, int64_t length, pars_gpu_settings_summary* out)
 {
   if ((!bytes && length > 0) || length < 0 || !out) return PARS_ERR_INVALID_ARGUMENT;

@@ -122,6 +122,7 @@ SIGNATURES = {
     "pars_gpu_batch_variants": [_P, ctypes.POINTER(_I32)],
     "pars_gpu_batch_tuned": [_P, _I32, ctypes.POINTER(_I32), ctypes.POINTER(_I32)],
     "pars_gpu_settings_decode": [_P, _I64, ctypes.POINTER(SettingsSummary)],
+    "pars_gpu_settings_from_json": [ctypes.c_char_p, _I64, _P, _I64, ctypes.POINTER(_I64)],
     "pars_gpu_service_create": [ctypes.POINTER(_P), _I32, _I64, _I32, _I32],
     "pars_gpu_service_destroy": [_P],
     "pars_gpu_service_add_dataset": [_P, ctypes.c_char_p, _P, _P, _P, _P, _P],
@@ -588,6 +589,21 @@ def image_encode(rgba):
     if status:
         raise ParsGpuError(status, "pars_gpu_image_encode")
     return out.tobytes()
+
+
+def settings_from_json(text):
+    """The binary `settings` message of its JSON form (the benchmark's settings files)."""
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    lib = library()
+    n = _I64()
+    status = lib.pars_gpu_settings_from_json(data, len(data), None, 0, ctypes.byref(n))
+    if status:
+        raise ParsGpuError(status, "pars_gpu_settings_from_json")
+    out = np.zeros(max(n.value, 1), np.uint8)
+    status = lib.pars_gpu_settings_from_json(data, len(data), _ptr(out), n.value, ctypes.byref(n))
+    if status:
+        raise ParsGpuError(status, "pars_gpu_settings_from_json")
+    return out[: n.value].tobytes()
 
 
 def decode_settings(message):

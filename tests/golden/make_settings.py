@@ -1,7 +1,9 @@
 """Writes tests/golden/settings.npz: `pars.settings` requests serialized by
 the protobuf library itself, from a descriptor built with the field names,
-numbers and types of the reference's pars/proto/settings.proto:5-27.  The
-fixtures pin the library's settings decoder and pars_gb300.requests' encoder.
+numbers and types of the reference's pars/proto/settings.proto:5-27, and the
+JSON forms protobuf's json_format writes and reads (the benchmark's settings
+files, service.cpp:72-77).  The fixtures pin the library's settings decoder,
+its JSON reader and pars_gb300.requests' encoder.
 Needs the `protobuf` package (present in the development container):
 
     python tests/golden/make_settings.py
@@ -10,7 +12,7 @@ import json
 import os
 
 import numpy as np
-from google.protobuf import descriptor_pb2, descriptor_pool, message_factory
+from google.protobuf import descriptor_pb2, descriptor_pool, json_format, message_factory
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -54,6 +56,14 @@ CASES = [
 ]
 
 
+JSON_VARIANTS = [
+    '{"seedGenerationIterations": "1002", "particleTracingStepSize": "0.5", "mode": "ftle"}',
+    '{"raytracing_camera_position": ["NaN", 1, "-Infinity"], "raytracingImageSize": [1920, "1080"], "volume_type": null}',
+    '{"particleTracingLoadBalance": true, "colorGenerationFreeParameter": 7.5e-1, "dataset_filepath": "a\\u00e9b\\n"}',
+    '{"seed_generation_stride": [], "raytracingIterations": 0, "particle_tracing_step_size": -0.0}',
+]
+
+
 def main():
     cls = settings_class()
     out = {}
@@ -66,6 +76,11 @@ def main():
                 setattr(msg, name, value)
         out[f"case{k}"] = np.frombuffer(msg.SerializeToString(), np.uint8)
         out[f"case{k}_json"] = np.array(json.dumps(case))
+        out[f"case{k}_protojson"] = np.array(json_format.MessageToJson(msg))
+    # JSON that json_format.Parse accepts, with the message it makes
+    for k, text in enumerate(JSON_VARIANTS):
+        out[f"variant{k}_json"] = np.array(text)
+        out[f"variant{k}"] = np.frombuffer(json_format.Parse(text, cls()).SerializeToString(), np.uint8)
     np.savez_compressed(os.path.join(HERE, "settings.npz"), **out)
     print("wrote settings.npz")
 

@@ -51,3 +51,27 @@ def test_decoder_rejects_malformed_messages(bad):
     from pars_gb300 import native
     with pytest.raises(native.ParsGpuError):
         native.decode_settings(bad)
+
+
+def test_json_settings_make_the_protobuf_message():
+    """pars_gpu_settings_from_json against protobuf's json_format: the JSON the
+    runtime writes (lowerCamelCase), the snake_case files the benchmark
+    generator writes, and the variants json_format.Parse accepts (numeric
+    strings, NaN / -Infinity, null, escapes, -0.0) give the runtime's bytes."""
+    from pars_gb300 import native
+    g = golden("settings.npz")
+    for k in range(3):
+        expected = g[f"case{k}"].tobytes()
+        assert native.settings_from_json(str(g[f"case{k}_protojson"])) == expected
+        assert native.settings_from_json(str(g[f"case{k}_json"])) == expected
+    for k in range(4):
+        assert native.settings_from_json(str(g[f"variant{k}_json"])) == g[f"variant{k}"].tobytes(), k
+
+
+def test_json_settings_errors():
+    from pars_gb300 import native
+    for bad in ('{"mode": 3}', '{"unknown_field": 1}', '{"seedGenerationIterations": 1.5}', '[1, 2]',
+                '{"mode": "x",}', '{"raytracingImageSize": [1e20]}', '{"particleTracingStepSize": 1e39}', '{"mode": "x"} y'):
+        with pytest.raises(native.ParsGpuError) as e:
+            native.settings_from_json(bad)
+        assert e.value.status == -1, bad
