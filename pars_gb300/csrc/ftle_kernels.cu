@@ -7,12 +7,15 @@
 //   position when it leaves the grid, meets a zero velocity, or has taken
 //   iterations - 1 steps) and written to its voxel (flow_map_generator.cpp:44-52).
 // FTLE: per voxel, the flow map's central-difference gradient J (FP32, one-sided
-//   at the borders), the Cauchy-Green tensor C = J^T J and its largest
-//   eigenvalue in FP64 by the trigonometric closed form (O. K. Smith, CACM 4(4),
-//   1961; its cosine refined by Newton steps, see largest_eigenvalue), then
-//   log(sqrt(lambda)) / |T| = 0.5 log(lambda) / |T| in FP64, stored as FP32 — the intent of
-//   vector_field::gradient + ftle_map_generator::generate
-//   (vector_field.cpp:49-93, ftle_map_generator.cpp:22-60).
+//   at the borders), the Cauchy-Green tensor C = J^T J (FP32) and its
+//   eigenvalues by four sweeps of the cyclic Jacobi method (FP32 rotations;
+//   Jacobi is backward stable, so every eigenvalue carries an error of a few
+//   FP32 ulps of ||C||, also where two of them nearly coincide and closed
+//   forms lose half their digits), then log(sqrt(lambda_max)) / |T| =
+//   0.5 log(lambda_max) / |T| — the intent of vector_field::gradient +
+//   ftle_map_generator::generate (vector_field.cpp:49-93,
+//   ftle_map_generator.cpp:22-60).  All FP32: a GB300 SM issues FP64 at 1/64
+//   of its FP32 rate, and FP64 evaluation made this kernel FP64-pipe bound.
 #include "context.hpp"
 
 namespace pars
@@ -72,71 +75,41 @@ __global__ void __launch_bounds__(256) flow_map_kernel(const __grid_constant__ f
   if ((threadIdx.x & 31) == 0 && warp_steps) atomicAdd(a.steps, (unsigned long long)warp_steps);
 }
 
-// Eigenvalues of a symmetric 3x3 matrix in descending order (trigonometric form).
-__device__ void symmetric_eigenvalues(double a00, double a01, double a02, double a11, double a12, double a22, double out[3])
+// Eigenvalues of the symmetric 3x3 matrix a (in place on its diagonal) by
+// cyclic Jacobi rotations (Jacobi 1846; the rotation of Rutishauser's
+// formulation, Numer. Math. 9, 1966): each rotation zeroes a_pq with
+// t = sgn(theta) / (|theta| + sqrt(theta^2 + 1)), theta = (a_qq - a_pp) / (2 a_pq).
+// Four sweeps of the three pivots: the off-diagonal mass shrinks
+// quadratically, and the FP32 eigenvalues settle after three.
+__device__ __forceinline__ void jacobi_eigenvalues(float& a00, float& a11, float& a22, float a01, float a02, float a12)
 {
-  const double p1 = a01 * a01 + a02 * a02 + a12 * a12;
-  if (p1 == 0.0)
+  #pragma unroll
+  for (int sweep = 0; sweep < 4; ++sweep)
   {
-    double x = a00, y = a11, z = a22, t;
-    if (x < y) { t = x; x = y; y = t; }
-    if (y < z) { t = y; y = z; z = t; }
-    if (x < y) { t = x; x = y; y = t; }
-    out[0] = x; out[1] = y; out[2] = z;
-    return;
-  }
-  const double q  = (a00 + a11 + a22) / 3.0;
-  const double d0 = a00 - q, d1 = a11 - q, d2 = a22 - q;
-  const double p  = sqrt((d0 * d0 + d1 * d1 + d2 * d2 + 2.0 * p1) / 6.0);
-  const double inv = 1.0 / p;
-  const double b00 = d0 * inv, b11 = d1 * inv, b22 = d2 * inv, b01 = a01 * inv, b02 = a02 * inv, b12 = a12 * inv;
-  const double det = b00 * (b11 * b22 - b12 * b12) - b01 * (b01 * b22 - b12 * b02) + b02 * (b01 * b12 - b11 * b02);
-  double r = 0.5 * det;
-  r = r < -1.0 ? -1.0 : (r > 1.0 ? 1.0 : r);
-  const double phi = acos(r) / 3.0;
-  out[0] = q + 2.0 * p * cos(phi);
-  out[2] = q + 2.0 * p * cos(phi + 2.0943951023931954923);   // 2 pi / 3
-  out[1] = 3.0 * q - out[0] - out[2];
-}
-
-// Largest eigenvalue of a symmetric 3x3 matrix in FP64 (the trigonometric
-// form above, lambda = q + 2 p cos(acos(r) / 3)), with c = cos(acos(r) / 3)
-// found as the largest root of 4 c^3 - 3 c = r (cos 3t = 4 cos^3 t - 3 cos t)
-// in [1/2, 1]: an FP32 start from acosf / cosf, then Newton steps on the
-// cubic in FP64 whose derivative 12 c^2 - 3 is inverted in FP32 (each step
-// multiplies the error by about the FP32 relative error of that reciprocal,
-// plus the quadratic term), which is far cheaper than FP64 acos and cos.  Near
-// the double root c = 1/2 (r -> -1: the two largest eigenvalues meet) the
-// derivative vanishes, and the FP64 trigonometric evaluation is used instead.
-__device__ __forceinline__ double largest_eigenvalue(double a00, double a01, double a02, double a11, double a12, double a22)
-{
-  const double p1 = a01 * a01 + a02 * a02 + a12 * a12;
-  if (p1 == 0.0) return fmax(a00, fmax(a11, a22));
-  const double q  = (a00 + a11 + a22) * (1.0 / 3.0);
-  const double d0 = a00 - q, d1 = a11 - q, d2 = a22 - q;
-  const double s  = (d0 * d0 + d1 * d1 + d2 * d2 + 2.0 * p1) * (1.0 / 6.0);
-  const double inv = rsqrt(s);   // 1 / p
-  const double p  = s * inv;
-  const double b00 = d0 * inv, b11 = d1 * inv, b22 = d2 * inv, b01 = a01 * inv, b02 = a02 * inv, b12 = a12 * inv;
-  const double det = b00 * (b11 * b22 - b12 * b12) - b01 * (b01 * b22 - b12 * b02) + b02 * (b01 * b12 - b11 * b02);
-  double r = 0.5 * det;
-  r = r < -1.0 ? -1.0 : (r > 1.0 ? 1.0 : r);
-  const float cf = cosf(acosf(float(r)) * (1.0f / 3.0f));
-  double c;
-  if (cf > 0.52f)
-  {
-    c = cf;
     #pragma unroll
-    for (int k = 0; k < 3; ++k)
+    for (int pivot = 0; pivot < 3; ++pivot)
     {
-      const double f = fma(4.0 * c, c * c, fma(-3.0, c, -r));   // 4 c^3 - 3 c - r
-      const float slope = fmaf(12.0f * float(c), float(c), -3.0f);
-      c = fma(-f, double(__frcp_rn(slope)), c);
+      // (p, q, r) = (0, 1, 2), (0, 2, 1), (1, 2, 0)
+      float& app = pivot == 2 ? a11 : a00;
+      float& aqq = pivot == 0 ? a11 : a22;
+      float& apq = pivot == 0 ? a01 : (pivot == 1 ? a02 : a12);
+      float& arp = pivot == 0 ? a02 : (pivot == 1 ? a01 : a01);
+      float& arq = pivot == 0 ? a12 : (pivot == 1 ? a12 : a02);
+      if (apq == 0.0f) continue;
+      const float theta = __fdiv_rn(aqq - app, 2.0f * apq);
+      float t;
+      if (fabsf(theta) > 1e18f) t = __fdiv_rn(0.5f, theta);
+      else t = copysignf(__frcp_rn(fabsf(theta) + __fsqrt_rn(fmaf(theta, theta, 1.0f))), theta);
+      const float c = __frsqrt_rn(fmaf(t, t, 1.0f)), s = t * c;
+      app = fmaf(-t, apq, app);
+      aqq = fmaf(t, apq, aqq);
+      apq = 0.0f;
+      const float rp = arp, rq = arq;
+      // pivot (1, 2): a01 is row 0's p-entry and a02 its q-entry
+      arp = fmaf(c, rp, -s * rq);
+      arq = fmaf(s, rp, c * rq);
     }
   }
-  else
-    c = cos(acos(r) * (1.0 / 3.0));
-  return fma(2.0 * p, c, q);
 }
 
 struct ftle_args
@@ -144,7 +117,7 @@ struct ftle_args
   const float4* flow;
   int           nx, ny, nz;
   float         hx, hy, hz;
-  double        inverse_time;     // 1 / |T|
+  float         inverse_time;     // 1 / |T|
   int           mode;
   float*        out;
 };
@@ -180,29 +153,29 @@ __global__ void __launch_bounds__(256) ftle_kernel(const ftle_args a)
     J[1][j] = __fdiv_rn(__fsub_rn(B.y, A.y), denominator);
     J[2][j] = __fdiv_rn(__fsub_rn(B.z, A.z), denominator);
   }
-  // Cauchy-Green tensor in FP64.
-  double C[3][3];
+  // Cauchy-Green tensor C = J^T J (FP32) and its eigenvalues.
+  float C[3][3];
   #pragma unroll
   for (int r = 0; r < 3; ++r)
     #pragma unroll
     for (int c = r; c < 3; ++c)
-      C[r][c] = double(J[0][r]) * double(J[0][c]) + double(J[1][r]) * double(J[1][c]) + double(J[2][r]) * double(J[2][c]);
-  double value;
+      C[r][c] = fmaf(J[2][r], J[2][c], fmaf(J[1][r], J[1][c], J[0][r] * J[0][c]));
+  float l0 = C[0][0], l1 = C[1][1], l2 = C[2][2];
+  jacobi_eigenvalues(l0, l1, l2, C[0][1], C[0][2], C[1][2]);
+  float value;
   if constexpr (MODE == PARS_FTLE_REGULAR)
   {
     // log(sqrt(lambda_max)) / |T|
-    const double lambda = largest_eigenvalue(C[0][0], C[0][1], C[0][2], C[1][1], C[1][2], C[2][2]);
-    value = 0.5 * log(lambda) * a.inverse_time;
+    const float lambda = fmaxf(l0, fmaxf(l1, l2));
+    value = 0.5f * logf(lambda) * a.inverse_time;
   }
   else
   {
-    double lambda[3];
-    symmetric_eigenvalues(C[0][0], C[0][1], C[0][2], C[1][1], C[1][2], C[2][2], lambda);
-    const double d01 = lambda[0] - lambda[1], d12 = lambda[1] - lambda[2], d20 = lambda[2] - lambda[0];
-    value = sqrt(0.5) * sqrt(d01 * d01 + d12 * d12 + d20 * d20) /
-            sqrt(lambda[0] * lambda[0] + lambda[1] * lambda[1] + lambda[2] * lambda[2]);
+    // fractional anisotropy of the eigenvalues (ftle_map_generator.cpp:51-54)
+    const float d01 = l0 - l1, d12 = l1 - l2, d20 = l2 - l0;
+    value = 0.70710678f * sqrtf(d01 * d01 + d12 * d12 + d20 * d20) / sqrtf(l0 * l0 + l1 * l1 + l2 * l2);
   }
-  a.out[i] = float(value);
+  a.out[i] = value;
 }
 
 void launch_ftle_kernel(const ftle_args& a, unsigned grid, cudaStream_t stream)
@@ -235,7 +208,7 @@ void launch_ftle(pars_gpu_context& ctx, const field_view& flow, double time, int
   ftle_args a;
   a.flow = flow.data; a.nx = flow.nx; a.ny = flow.ny; a.nz = flow.nz;
   a.hx = flow.hx; a.hy = flow.hy; a.hz = flow.hz;
-  a.inverse_time = 1.0 / fabs(time);
+  a.inverse_time = float(1.0 / fabs(time));
   a.mode = mode;
   a.out = out;
   const long long total = (long long)a.nx * a.ny * a.nz;
@@ -355,7 +328,7 @@ extern "C" int32_t pars_gpu_ftle_no_alloc(const float* device_xyz, const int32_t
   ftle_args t;
   t.flow = flow; t.nx = shape[0]; t.ny = shape[1]; t.nz = shape[2];
   t.hx = spacing[0]; t.hy = spacing[1]; t.hz = spacing[2];
-  t.inverse_time = 1.0 / fabs(double(time));
+  t.inverse_time = float(1.0 / fabs(double(time)));
   t.mode = mode;
   t.out = device_ftle;
   launch_ftle_kernel(t, (unsigned)((voxels + 255) / 256), s);
