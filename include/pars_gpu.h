@@ -173,9 +173,12 @@ int32_t pars_gpu_partition(int32_t ranks, int32_t rank, const int32_t domain_siz
 /* ---- particle_tracer (pa/source/stages/particle_tracer.cpp:39-56, 210-337, 402-409)
  * Traces host particles through one block (`field`, no neighbours: particles
  * leaving it are dropped) and prunes, leaving the curves on the device.
- * integrator: any pars_integrator with PARS_STAGES_FROZEN (the reference's
- * scheme, every stepper of integrators.hpp:16-23); PARS_EULER or
- * PARS_RUNGE_KUTTA_4 with PARS_STAGES_RESAMPLED (others: PARS_ERR_UNSUPPORTED). */
+ * integrator: any pars_integrator (integrators.hpp:16-23), with the
+ * reference's frozen stages (PARS_STAGES_FROZEN) or re-sampled ones
+ * (PARS_STAGES_RESAMPLED: each stage samples the field where it falls --
+ * modified midpoint as Gragg's two substeps, Cash-Karp 5(4) and
+ * Dormand-Prince 5 with 5th-order weights, Fehlberg 7(8) with 8th-order
+ * weights, two-step Adams-Bashforth(-Moulton) after an RK4 first step). */
 int32_t pars_gpu_trace(pars_gpu_context* context, int32_t field, const pars_particle* particles, int64_t count,
                        int32_t integrator, int32_t stage_mode, float step_size, pars_gpu_trace_summary* summary);
 /* Same with the particles already in DEVICE memory. */
@@ -259,7 +262,7 @@ int32_t pars_gpu_unsteady_field_upload_device(pars_gpu_context* context, const f
 typedef struct pars_gpu_batch_job
 {
   int32_t      field;               /* field handle (steady or unsteady) */
-  int32_t      integrator;          /* PARS_EULER or PARS_RUNGE_KUTTA_4 (re-sampled stages) */
+  int32_t      integrator;          /* PARS_EULER or PARS_RUNGE_KUTTA_4 (re-sampled stages; the engine's schemes) */
   int32_t      stage_mode;          /* PARS_STAGES_RESAMPLED (PARS_STAGES_FROZEN: velocity of the step start) */
   int32_t      max_steps;
   float        step_size;

@@ -575,11 +575,117 @@ inline bool is_zero_fp64(const double* v)
   const double precision = 1e-5;
   return std::fabs(v[0]) <= precision && std::fabs(v[1]) <= precision && std::fabs(v[2]) <= precision;
 }
-// One FP64 step; `mode` frozen reuses k1 for every stage.
-inline void step_fp64(const field& f, int integrator, int mode, double h, const double* x, const double* k1, double* out)
+// Explicit tableaux of the other integrators in FP64 (exact fractions):
+// modified midpoint (two substeps: z1 = x + h/2 f(x), z2 = x + h f(z1),
+// (z2 + z1 + h/2 f(z2)) / 2, as a 3-stage scheme), Cash-Karp 5(4) and
+// Dormand-Prince 5 (5th-order weights), Fehlberg 7(8) (8th-order weights).
+struct tableau_fp64
 {
-  if (integrator == euler) { for (int c = 0; c < 3; ++c) out[c] = x[c] + h * k1[c]; return; }
-  if (mode == frozen) { for (int c = 0; c < 3; ++c) out[c] = x[c] + h * k1[c]; return; }
+  int    stages = 0;
+  double a[13][13] = {};
+  double b[13] = {};
+};
+
+tableau_fp64 tableau_for(int integrator)
+{
+  struct entry { int i, j; double p, q; };
+  tableau_fp64 t;
+  auto set = [&](int stages, std::initializer_list<entry> a, std::initializer_list<entry> b) {
+    t.stages = stages;
+    for (const auto& e : a) t.a[e.i][e.j] = e.p / e.q;
+    for (const auto& e : b) t.b[e.i] = e.p / e.q;
+  };
+  switch (integrator)
+  {
+  case modified_midpoint: set(3, {{1, 0, 1, 2}, {2, 1, 1, 1}}, {{0, 0, 1, 4}, {1, 0, 1, 2}, {2, 0, 1, 4}}); break;
+  case cash_karp_54:
+    set(6, {{1, 0, 1, 5}, {2, 0, 3, 40}, {2, 1, 9, 40}, {3, 0, 3, 10}, {3, 1, -9, 10}, {3, 2, 6, 5}, {4, 0, -11, 54}, {4, 1, 5, 2},
+            {4, 2, -70, 27}, {4, 3, 35, 27}, {5, 0, 1631, 55296}, {5, 1, 175, 512}, {5, 2, 575, 13824}, {5, 3, 44275, 110592},
+            {5, 4, 253, 4096}},
+        {{0, 0, 37, 378}, {2, 0, 250, 621}, {3, 0, 125, 594}, {5, 0, 512, 1771}});
+    break;
+  case dormand_prince_5:
+    set(6, {{1, 0, 1, 5}, {2, 0, 3, 40}, {2, 1, 9, 40}, {3, 0, 44, 45}, {3, 1, -56, 15}, {3, 2, 32, 9}, {4, 0, 19372, 6561},
+            {4, 1, -25360, 2187}, {4, 2, 64448, 6561}, {4, 3, -212, 729}, {5, 0, 9017, 3168}, {5, 1, -355, 33}, {5, 2, 46732, 5247},
+            {5, 3, 49, 176}, {5, 4, -5103, 18656}},
+        {{0, 0, 35, 384}, {2, 0, 500, 1113}, {3, 0, 125, 192}, {4, 0, -2187, 6784}, {5, 0, 11, 84}});
+    break;
+  case fehlberg_78:
+    set(13, {{1, 0, 2, 27}, {2, 0, 1, 36}, {2, 1, 1, 12}, {3, 0, 1, 24}, {3, 2, 1, 8}, {4, 0, 5, 12}, {4, 2, -25, 16},
+             {4, 3, 25, 16}, {5, 0, 1, 20}, {5, 3, 1, 4}, {5, 4, 1, 5}, {6, 0, -25, 108}, {6, 3, 125, 108}, {6, 4, -65, 27},
+             {6, 5, 125, 54}, {7, 0, 31, 300}, {7, 4, 61, 225}, {7, 5, -2, 9}, {7, 6, 13, 900}, {8, 0, 2, 1}, {8, 3, -53, 6},
+             {8, 4, 704, 45}, {8, 5, -107, 9}, {8, 6, 67, 90}, {8, 7, 3, 1}, {9, 0, -91, 108}, {9, 3, 23, 108},
+             {9, 4, -976, 135}, {9, 5, 311, 54}, {9, 6, -19, 60}, {9, 7, 17, 6}, {9, 8, -1, 12}, {10, 0, 2383, 4100},
+             {10, 3, -341, 164}, {10, 4, 4496, 1025}, {10, 5, -301, 82}, {10, 6, 2133, 4100}, {10, 7, 45, 82},
+             {10, 8, 45, 164}, {10, 9, 18, 41}, {11, 0, 3, 205}, {11, 5, -6, 41}, {11, 6, -3, 205}, {11, 7, -3, 41},
+             {11, 8, 3, 41}, {11, 9, 6, 41}, {12, 0, -1777, 4100}, {12, 3, -341, 164}, {12, 4, 4496, 1025},
+             {12, 5, -289, 82}, {12, 6, 2193, 4100}, {12, 7, 51, 82}, {12, 8, 33, 164}, {12, 9, 12, 41}, {12, 11, 1, 1}},
+        {{5, 0, 34, 105}, {6, 0, 9, 35}, {7, 0, 9, 35}, {8, 0, 9, 280}, {9, 0, 9, 280}, {11, 0, 41, 840}, {12, 0, 41, 840}});
+    break;
+  default: break;
+  }
+  return t;
+}
+
+// Per-particle history of the two-step Adams schemes in FP64.
+struct history_fp64
+{
+  double v[3] = {0, 0, 0};
+  bool   started = false;
+};
+
+void rk4_fp64(const field& f, double h, const double* x, const double* k1, double* out);
+
+// One FP64 step.  `mode` frozen: every stage sees k1 (out = x + h k1; the
+// two-step Adams-Bashforth scheme x + h (3/2 k1 - 1/2 k_prev) after its RK4
+// start).  Re-sampled: each scheme with its stages sampled where they fall.
+inline void step_fp64(const field& f, int integrator, int mode, double h, const double* x, const double* k1, double* out,
+                      history_fp64& hist)
+{
+  if (integrator == adams_bashforth_2 || integrator == adams_bashforth_moulton_2)
+  {
+    double predicted[3];
+    if (hist.started) for (int c = 0; c < 3; ++c) predicted[c] = x[c] + h * (1.5 * k1[c] - 0.5 * hist.v[c]);
+    else if (mode == frozen) for (int c = 0; c < 3; ++c) predicted[c] = x[c] + h * k1[c];
+    else rk4_fp64(f, h, x, k1, predicted);
+    for (int c = 0; c < 3; ++c) hist.v[c] = k1[c];
+    hist.started = true;
+    if (integrator == adams_bashforth_2 || mode == frozen) { std::memcpy(out, predicted, 24); return; }
+    double kp[3];
+    interpolate_fp64(f, predicted, kp);
+    for (int c = 0; c < 3; ++c) out[c] = x[c] + 0.5 * h * (k1[c] + kp[c]);
+    return;
+  }
+  if (integrator == euler || mode == frozen) { for (int c = 0; c < 3; ++c) out[c] = x[c] + h * k1[c]; return; }
+  if (integrator != runge_kutta_4)
+  {
+    const tableau_fp64 t = tableau_for(integrator);
+    double k[13][3];
+    std::memcpy(k[0], k1, 24);
+    for (int s = 1; s < t.stages; ++s)
+    {
+      double p[3];
+      for (int c = 0; c < 3; ++c)
+      {
+        double acc = 0.0;
+        for (int j = 0; j < s; ++j) acc += t.a[s][j] * k[j][c];
+        p[c] = x[c] + h * acc;
+      }
+      interpolate_fp64(f, p, k[s]);
+    }
+    for (int c = 0; c < 3; ++c)
+    {
+      double acc = 0.0;
+      for (int s = 0; s < t.stages; ++s) acc += t.b[s] * k[s][c];
+      out[c] = x[c] + h * acc;
+    }
+    return;
+  }
+  rk4_fp64(f, h, x, k1, out);
+}
+
+void rk4_fp64(const field& f, double h, const double* x, const double* k1, double* out)
+{
   double k2[3], k3[3], k4[3], t[3];
   for (int c = 0; c < 3; ++c) t[c] = x[c] + 0.5 * h * k1[c];
   interpolate_fp64(f, t, k2);
@@ -937,6 +1043,7 @@ void orc_advect_fp64(const float* xyz, const int dims[3], const float offset[3],
       return (double(z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
     };
     long long s = 0;
+    history_fp64 hist;
     for (; s < max_steps; ++s)
     {
       if (!contains_fp64(f, x)) break;
@@ -944,7 +1051,7 @@ void orc_advect_fp64(const float* xyz, const int dims[3], const float offset[3],
       interpolate_fp64(f, x, k1);
       if (is_zero_fp64(k1)) break;
       double next[3];
-      step_fp64(f, integrator, mode, step, x, k1, next);
+      step_fp64(f, integrator, mode, step, x, k1, next, hist);
       if (noise > 0.0)
         for (int c = 0; c < 3; ++c)
         {

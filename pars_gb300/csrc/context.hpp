@@ -225,9 +225,10 @@ struct pars_gpu_context
   // per job class (0 = steady, 1 = unsteady); -1 = not tuned yet
   pars::device_buffer                     batch_jobs, batch_counters;
   int                                     batch_variant[2] = {-1, -1};
-  // tracing kernel: resident CTAs of 128 threads per SM (frozen, re-sampled)
+  // tracing kernel: resident CTAs of 128 threads per SM (frozen, re-sampled
+  // RK4 / Euler, re-sampled general schemes)
   // and the device's SM count, queried once
-  int                                     trace_ctas_per_sm[2] = {-1, -1};
+  int                                     trace_ctas_per_sm[3] = {-1, -1, -1};
   int                                     sm_count = 0;
   // batched engine: resident CTAs per SM per job class and launch shape
   int                                     batch_ctas_per_sm[2][4] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}};

@@ -273,14 +273,24 @@ __device__ __forceinline__ bool is_zero(const float3& v)
 //    c_5 = -0.5 h), with the previous step's velocity kept per particle.
 enum frozen_method { frozen_weighted_sum = 0, frozen_midpoint = 1, frozen_multistep = 2 };
 
+// Re-sampled stages of the other integrators ("true form"): explicit RK
+// tableaux (modified midpoint as a 3-stage scheme, Cash-Karp 5(4) and
+// Dormand-Prince 5 with their 5th-order weights, Fehlberg 7(8) with its
+// 8th-order weights -- the orders odeint's steppers propagate) and the
+// two-step Adams-Bashforth / Adams-Bashforth-Moulton schemes (RK4 for a
+// particle's first step).
+enum resampled_scheme { scheme_classic = 0, scheme_tableau = 1, scheme_adams_bashforth = 2, scheme_adams_moulton = 3 };
+
 struct step_rule
 {
   int   frozen;      // 1 = frozen velocity, 0 = resampled stages
-  int   rk4;         // resampled: 1 = RK4, 0 = Euler
+  int   rk4;         // resampled classic scheme: 1 = RK4, 0 = Euler
   int   count;       // frozen weighted sum: number of coefficients
   int   method;      // frozen_method
   float c[16];       // frozen coefficients
   float h;           // step size
+  int   scheme;      // resampled_scheme
+  int   tableau;     // scheme_tableau: index into rk_tableaux
 };
 
 // The multistep scheme's per-particle history.
@@ -343,6 +353,64 @@ __device__ __forceinline__ void compensated_add(float& hi, float& lo, float delt
   hi = s;
 }
 
+// Butcher tableaux of the re-sampled general schemes (stage matrix a, weights
+// b), FP32 quotients of the published fractions.
+struct rk_tableau
+{
+  int   stages;
+  float a[13][13];
+  float b[13];
+};
+
+struct rk_entry { int i, j, p, q; };
+
+template <int NA, int NB>
+constexpr rk_tableau make_tableau(int stages, const rk_entry (&a)[NA], const rk_entry (&b)[NB])
+{
+  rk_tableau t {};
+  t.stages = stages;
+  for (int k = 0; k < NA; ++k) t.a[a[k].i][a[k].j] = float(a[k].p) / float(a[k].q);
+  for (int k = 0; k < NB; ++k) t.b[b[k].i] = float(b[k].p) / float(b[k].q);
+  return t;
+}
+
+// Gragg's modified midpoint with two substeps (odeint's modified_midpoint):
+// z1 = x + (h/2) f(x), z2 = x + h f(z1), out = (z2 + z1 + (h/2) f(z2)) / 2.
+constexpr rk_entry midpoint_a[] = {{1, 0, 1, 2}, {2, 1, 1, 1}};
+constexpr rk_entry midpoint_b[] = {{0, 0, 1, 4}, {1, 0, 1, 2}, {2, 0, 1, 4}};
+constexpr rk_entry cash_karp_a[] = {
+  {1, 0, 1, 5}, {2, 0, 3, 40}, {2, 1, 9, 40}, {3, 0, 3, 10}, {3, 1, -9, 10}, {3, 2, 6, 5},
+  {4, 0, -11, 54}, {4, 1, 5, 2}, {4, 2, -70, 27}, {4, 3, 35, 27},
+  {5, 0, 1631, 55296}, {5, 1, 175, 512}, {5, 2, 575, 13824}, {5, 3, 44275, 110592}, {5, 4, 253, 4096}};
+constexpr rk_entry cash_karp_b[] = {{0, 0, 37, 378}, {2, 0, 250, 621}, {3, 0, 125, 594}, {5, 0, 512, 1771}};
+constexpr rk_entry dormand_prince_a[] = {
+  {1, 0, 1, 5}, {2, 0, 3, 40}, {2, 1, 9, 40}, {3, 0, 44, 45}, {3, 1, -56, 15}, {3, 2, 32, 9},
+  {4, 0, 19372, 6561}, {4, 1, -25360, 2187}, {4, 2, 64448, 6561}, {4, 3, -212, 729},
+  {5, 0, 9017, 3168}, {5, 1, -355, 33}, {5, 2, 46732, 5247}, {5, 3, 49, 176}, {5, 4, -5103, 18656}};
+constexpr rk_entry dormand_prince_b[] = {{0, 0, 35, 384}, {2, 0, 500, 1113}, {3, 0, 125, 192}, {4, 0, -2187, 6784}, {5, 0, 11, 84}};
+constexpr rk_entry fehlberg_a[] = {
+  {1, 0, 2, 27}, {2, 0, 1, 36}, {2, 1, 1, 12}, {3, 0, 1, 24}, {3, 2, 1, 8},
+  {4, 0, 5, 12}, {4, 2, -25, 16}, {4, 3, 25, 16}, {5, 0, 1, 20}, {5, 3, 1, 4}, {5, 4, 1, 5},
+  {6, 0, -25, 108}, {6, 3, 125, 108}, {6, 4, -65, 27}, {6, 5, 125, 54},
+  {7, 0, 31, 300}, {7, 4, 61, 225}, {7, 5, -2, 9}, {7, 6, 13, 900},
+  {8, 0, 2, 1}, {8, 3, -53, 6}, {8, 4, 704, 45}, {8, 5, -107, 9}, {8, 6, 67, 90}, {8, 7, 3, 1},
+  {9, 0, -91, 108}, {9, 3, 23, 108}, {9, 4, -976, 135}, {9, 5, 311, 54}, {9, 6, -19, 60}, {9, 7, 17, 6}, {9, 8, -1, 12},
+  {10, 0, 2383, 4100}, {10, 3, -341, 164}, {10, 4, 4496, 1025}, {10, 5, -301, 82}, {10, 6, 2133, 4100}, {10, 7, 45, 82},
+  {10, 8, 45, 164}, {10, 9, 18, 41},
+  {11, 0, 3, 205}, {11, 5, -6, 41}, {11, 6, -3, 205}, {11, 7, -3, 41}, {11, 8, 3, 41}, {11, 9, 6, 41},
+  {12, 0, -1777, 4100}, {12, 3, -341, 164}, {12, 4, 4496, 1025}, {12, 5, -289, 82}, {12, 6, 2193, 4100}, {12, 7, 51, 82},
+  {12, 8, 33, 164}, {12, 9, 12, 41}, {12, 11, 1, 1}};
+constexpr rk_entry fehlberg_b[] = {{5, 0, 34, 105}, {6, 0, 9, 35}, {7, 0, 9, 35}, {8, 0, 9, 280}, {9, 0, 9, 280},
+                                   {11, 0, 41, 840}, {12, 0, 41, 840}};
+
+enum rk_tableau_index { tableau_midpoint = 0, tableau_cash_karp = 1, tableau_dormand_prince = 2, tableau_fehlberg = 3 };
+
+__constant__ const rk_tableau rk_tableaux[4] = {
+  make_tableau(3, midpoint_a, midpoint_b),
+  make_tableau(6, cash_karp_a, cash_karp_b),
+  make_tableau(6, dormand_prince_a, dormand_prince_b),
+  make_tableau(13, fehlberg_a, fehlberg_b)};
+
 // RESAMPLED step: classical RK4 (or Euler) with the first-stage velocity k1
 // already sampled at x; stage points are sampled through the cell cache.
 __device__ __forceinline__ void resampled_step_cached(const field_view& f, corner_cache& k, const step_rule& r, float4& x,
@@ -363,6 +431,71 @@ __device__ __forceinline__ void resampled_step_cached(const field_view& f, corne
   compensated_add(x.x, lo.x, h6 * (k1.x + 2.0f * (k2.x + k3.x) + k4.x));
   compensated_add(x.y, lo.y, h6 * (k1.y + 2.0f * (k2.y + k3.y) + k4.y));
   compensated_add(x.z, lo.z, h6 * (k1.z + 2.0f * (k2.z + k3.z) + k4.z));
+}
+
+// RESAMPLED step of any scheme: the classic one above, an explicit tableau
+// (stage s sampled at x + h sum_j a_sj k_j, then x += h sum_i b_i k_i), or a
+// two-step Adams scheme whose history (the previous step's k1) is kept per
+// particle.  Position updates are compensated as in the classic step.
+__device__ __forceinline__ void general_step(const field_view& f, corner_cache& cache, const step_rule& r, float4& x, float3& lo,
+                                             const float3& k1, frozen_history& hist)
+{
+  if (r.scheme == scheme_classic) { resampled_step_cached(f, cache, r, x, lo, k1); return; }
+  float3 delta;
+  if (r.scheme == scheme_tableau)
+  {
+    const rk_tableau& T = rk_tableaux[r.tableau];
+    float3 k[13];
+    k[0] = k1;
+    for (int s = 1; s < T.stages; ++s)
+    {
+      float3 acc = make_float3(0.f, 0.f, 0.f);
+      for (int j = 0; j < s; ++j)
+      {
+        const float a = T.a[s][j];
+        if (a != 0.0f) acc = make_float3(fmaf(a, k[j].x, acc.x), fmaf(a, k[j].y, acc.y), fmaf(a, k[j].z, acc.z));
+      }
+      k[s] = sample_cached(f, cache, fmaf(r.h, acc.x, x.x), fmaf(r.h, acc.y, x.y), fmaf(r.h, acc.z, x.z));
+    }
+    float3 sum = make_float3(0.f, 0.f, 0.f);
+    for (int s = 0; s < T.stages; ++s)
+    {
+      const float b = T.b[s];
+      if (b != 0.0f) sum = make_float3(fmaf(b, k[s].x, sum.x), fmaf(b, k[s].y, sum.y), fmaf(b, k[s].z, sum.z));
+    }
+    delta = make_float3(r.h * sum.x, r.h * sum.y, r.h * sum.z);
+  }
+  else
+  {
+    // Adams-Bashforth 2: x + h (3/2 k_n - 1/2 k_{n-1}); a particle's first
+    // step is RK4.  Adams-Bashforth-Moulton 2: that prediction x*, then the
+    // trapezoid x + h/2 (k_n + f(x*)).
+    float4 predicted = x;
+    float3 predicted_lo = lo;
+    if (hist.started)
+    {
+      const float3 ab = make_float3(fmaf(1.5f, k1.x, -0.5f * hist.v.x), fmaf(1.5f, k1.y, -0.5f * hist.v.y),
+                                    fmaf(1.5f, k1.z, -0.5f * hist.v.z));
+      compensated_add(predicted.x, predicted_lo.x, r.h * ab.x);
+      compensated_add(predicted.y, predicted_lo.y, r.h * ab.y);
+      compensated_add(predicted.z, predicted_lo.z, r.h * ab.z);
+    }
+    else
+    {
+      step_rule classic = r;
+      classic.rk4 = 1;
+      resampled_step_cached(f, cache, classic, predicted, predicted_lo, k1);
+    }
+    hist.v = k1;
+    hist.started = 1;
+    if (r.scheme == scheme_adams_bashforth) { x = predicted; lo = predicted_lo; return; }
+    const float3 kp = sample_cached(f, cache, predicted.x, predicted.y, predicted.z);
+    const float hh = 0.5f * r.h;
+    delta = make_float3(hh * (k1.x + kp.x), hh * (k1.y + kp.y), hh * (k1.z + kp.z));
+  }
+  compensated_add(x.x, lo.x, delta.x);
+  compensated_add(x.y, lo.y, delta.y);
+  compensated_add(x.z, lo.z, delta.z);
 }
 
 // ---- Unsteady fields (pathlines) ----------------------------------------------

@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(256) flow_map_kernel(const __grid_constant__ f
       if (!inside) { finished = true; break; }
       if (is_zero(v)) { finished = true; break; }
       if (FROZEN) pos = frozen_step(a.rule, pos, v, hist);
-      else resampled_step_cached(a.f, cache, a.rule, pos, lo, v);
+      else general_step(a.f, cache, a.rule, pos, lo, v, hist);
       ++steps;
       if (it + 1 == a.iterations) { finished = true; break; }
     }

@@ -236,14 +236,23 @@ step_rule make_rule(int integrator, int stage_mode, float h)
 {
   PARS_REQUIRE(stage_mode == PARS_STAGES_FROZEN || stage_mode == PARS_STAGES_RESAMPLED, "unknown stage mode");
   PARS_REQUIRE(integrator >= PARS_EULER && integrator <= PARS_ADAMS_BASHFORTH_MOULTON_2, "unknown integrator");
-  if (stage_mode == PARS_STAGES_RESAMPLED && integrator != PARS_EULER && integrator != PARS_RUNGE_KUTTA_4)
-    throw error(PARS_ERR_UNSUPPORTED, "integrator " + std::to_string(integrator) +
-                " runs with frozen stages only (re-sampled stages: Euler and RK4)");
   step_rule r {};
   r.frozen = stage_mode == PARS_STAGES_FROZEN ? 1 : 0;
   r.rk4 = integrator == PARS_RUNGE_KUTTA_4 ? 1 : 0;
   r.h = h;
   r.method = frozen_weighted_sum;
+  // re-sampled stages ("true form") of each integrator
+  r.scheme = scheme_classic;
+  switch (integrator)
+  {
+  case PARS_MODIFIED_MIDPOINT:            r.scheme = scheme_tableau; r.tableau = tableau_midpoint; break;
+  case PARS_RUNGE_KUTTA_CASH_KARP_54:     r.scheme = scheme_tableau; r.tableau = tableau_cash_karp; break;
+  case PARS_RUNGE_KUTTA_DORMAND_PRINCE_5: r.scheme = scheme_tableau; r.tableau = tableau_dormand_prince; break;
+  case PARS_RUNGE_KUTTA_FEHLBERG_78:      r.scheme = scheme_tableau; r.tableau = tableau_fehlberg; break;
+  case PARS_ADAMS_BASHFORTH_2:            r.scheme = scheme_adams_bashforth; break;
+  case PARS_ADAMS_BASHFORTH_MOULTON_2:    r.scheme = scheme_adams_moulton; break;
+  default: break;
+  }
   // Frozen coefficients (the odeint 1.69 schemes of integrators.hpp:16-23 with
   // every stage seeing the step-start velocity): b_i * h, b_i = float(p) /
   // float(q) in FP32, as the generic RK scale-sum forms them.
@@ -1149,10 +1158,13 @@ int32_t pars_gpu_flow_map_generate(pars_gpu_context* ctx, int32_t field, int32_t
     // when the seed lattice covers the flow map every voxel is written.
     if (seeds[0] < entry->shape[0] || seeds[1] < entry->shape[1] || seeds[2] < entry->shape[2])
       PARS_CUDA(cudaMemsetAsync(entry->data.get(), 0xff, sizeof(float4) * voxels, ctx->stream));
-    if (rule.frozen || iterations <= 1)
+    if (rule.scheme != scheme_classic && f.slices > 1)
+      throw error(PARS_ERR_UNSUPPORTED, "unsteady flow maps integrate with RK4 or Euler");
+    if (rule.frozen || iterations <= 1 || rule.scheme != scheme_classic)
     {
       // The reference's scheme, bit for bit (and the iterations <= 1 case,
-      // where every voxel keeps its seed position).
+      // where every voxel keeps its seed position); re-sampled stages of the
+      // general schemes also run here (one seed per thread).
       ctx->counters.reserve(sizeof(unsigned long long) * 2);
       auto* counter = ctx->counters.as<unsigned long long>();
       PARS_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
@@ -1240,6 +1252,8 @@ int32_t pars_gpu_batch_advect(pars_gpu_context* ctx, pars_gpu_batch_job* jobs, i
       d.rule = make_rule(in.integrator, in.stage_mode, in.step_size);
       if (d.rule.frozen)
         throw error(PARS_ERR_UNSUPPORTED, "batched advection integrates with re-sampled stages (PARS_STAGES_RESAMPLED)");
+      if (d.rule.scheme != scheme_classic)
+        throw error(PARS_ERR_UNSUPPORTED, "batched advection integrates with RK4 or Euler");
       d.ux = d.uy = d.uz = 0;
       PARS_REQUIRE(in.max_steps >= 0, "max_steps must be >= 0");
       d.max_steps = in.max_steps;

@@ -345,7 +345,40 @@ void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std:
     jobs.push_back(j);
   }
   clock.mark("ftle.setup");
-  const auto steps = run_batch(c, jobs, -1);
+  // RK4 / Euler requests: the persistent batched engine; the other
+  // integrators' re-sampled schemes: the per-seed flow-map kernel, one launch each
+  std::vector<batch_job_device> classic;
+  std::vector<std::size_t> classic_of, general_of;
+  for (std::size_t k = 0; k < jobs.size(); ++k)
+  {
+    if (jobs[k].rule.scheme == scheme_classic) { classic.push_back(jobs[k]); classic_of.push_back(k); }
+    else general_of.push_back(k);
+  }
+  std::vector<unsigned long long> steps(jobs.size(), 0);
+  if (!classic.empty())
+  {
+    const auto s = run_batch(c, classic, -1);
+    for (std::size_t i = 0; i < classic_of.size(); ++i) steps[classic_of[i]] = s[i];
+  }
+  if (!general_of.empty())
+  {
+    device_buffer counters;
+    counters.reserve(sizeof(unsigned long long) * general_of.size());
+    PARS_CUDA(cudaMemsetAsync(counters.get(), 0, sizeof(unsigned long long) * general_of.size(), c.stream));
+    for (std::size_t i = 0; i < general_of.size(); ++i)
+    {
+      const batch_job_device& j = jobs[general_of[i]];
+      const request& r = *batch[general_of[i]];
+      const float offset[3] = {j.ox, j.oy, j.oz}, spacing[3] = {j.sx, j.sy, j.sz};
+      const int seeds[3] = {j.px, j.py, j.pz}, shape[3] = {j.ux, j.uy, j.uz};
+      launch_flow_map(c, j.field, j.rule, r.s.seed_generation_iterations, offset, spacing, seeds, shape,
+                      flows[general_of[i]].as<float4>(), counters.as<unsigned long long>() + i);
+    }
+    std::vector<unsigned long long> host(general_of.size());
+    PARS_CUDA(cudaMemcpyAsync(host.data(), counters.get(), sizeof(unsigned long long) * host.size(), cudaMemcpyDeviceToHost, c.stream));
+    PARS_CUDA(cudaStreamSynchronize(c.stream));
+    for (std::size_t i = 0; i < general_of.size(); ++i) steps[general_of[i]] = host[i];
+  }
   clock.mark("ftle.advect");
   for (std::size_t k = 0; k < batch.size(); ++k)
   {
@@ -496,7 +529,11 @@ std::size_t run_streamline_batch(pars_gpu_service& svc, pars_gpu_context& c, std
   PARS_CUDA(cudaMemcpyAsync(device_rules.get(), rules.data(), sizeof(step_rule) * rules.size(), cudaMemcpyHostToDevice, c.stream));
   clock.mark("streamlines.seed");
   pars_gpu_trace_summary summary {};
-  trace_rounds(c, blocks, device_blocks.as<const trace_block>(), total, block_count, block_max, rules[0], false, &summary,
+  // the launch's kernel follows the most general scheme among the requests'
+  // rules; each block then integrates with its own rule
+  step_rule launch_rule = rules[0];
+  for (const auto& r : rules) if (r.scheme != scheme_classic) launch_rule = r;
+  trace_rounds(c, blocks, device_blocks.as<const trace_block>(), total, block_count, block_max, launch_rule, false, &summary,
                device_rules.as<const step_rule>());
 
   clock.mark("streamlines.trace");
@@ -968,9 +1005,6 @@ int32_t pars_gpu_service_submit(pars_gpu_service* svc, const uint8_t* message, i
     {
       r->integrator = integrator_of(r->s.particle_tracing_integrator);
       if (r->integrator < 0) throw error(PARS_ERR_UNSUPPORTED, "unknown integrator '" + r->s.particle_tracing_integrator + "'");
-      // every integrator with the reference's frozen stages; re-sampled stages: Euler and RK4
-      if (r->stage_mode == PARS_STAGES_RESAMPLED && r->integrator != PARS_EULER && r->integrator != PARS_RUNGE_KUTTA_4)
-        throw error(PARS_ERR_UNSUPPORTED, "integrator '" + r->s.particle_tracing_integrator + "' runs in \"reference\" mode only");
       PARS_REQUIRE(r->s.particle_tracing_step_size != 0.0f, "particle_tracing_step_size must be non-zero");
     }
     r->color_mode = color_of(r->s.color_generation_mode);

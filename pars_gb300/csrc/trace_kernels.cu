@@ -17,6 +17,7 @@ namespace pars
 namespace
 {
 constexpr unsigned full_mask = 0xffffffffu;
+enum trace_mode { trace_frozen = 0, trace_classic = 1, trace_general = 2 };
 
 // The particle a lane traces.
 struct lane_particle
@@ -60,10 +61,11 @@ __device__ __forceinline__ void particle_start(const trace_launch& a, lane_parti
 // stored, and a particle that left its block through a face with a neighbour
 // is pushed onto the exit queue with one atomic — the queue is sorted by
 // (destination, source index) afterwards, so slots may be taken in any order).
-// FROZEN = true: the reference's scheme and FP32 operation order (bit-exact).
-// FROZEN = false: re-sampled stages, consistent cell weights, compensated
-// position accumulation.
-template <bool FROZEN>
+// MODE trace_frozen: the reference's scheme and FP32 operation order
+// (bit-exact).  MODE trace_classic: re-sampled stages of RK4 / Euler,
+// consistent cell weights, compensated position accumulation.  MODE
+// trace_general: the same for any re-sampled scheme (general_step).
+template <int MODE>
 __device__ __forceinline__ bool particle_iteration(const trace_launch& a, lane_particle& p, unsigned int& steps)
 {
   const float4 term = termination_vertex();
@@ -74,6 +76,7 @@ __device__ __forceinline__ bool particle_iteration(const trace_launch& a, lane_p
   {
     float3 v;
     bool inside;
+    constexpr bool FROZEN = MODE == trace_frozen;
     if (FROZEN) inside = sample_inside(p.f, p.last, v);
     else        inside = sample_start(p.f, p.cache, p.last, v);
     if (!inside)
@@ -102,7 +105,8 @@ __device__ __forceinline__ bool particle_iteration(const trace_launch& a, lane_p
     else
     {
       float4 next;
-      if (FROZEN) next = frozen_step(*p.frozen_rule, p.last, v, p.hist);
+      if constexpr (MODE == trace_frozen) next = frozen_step(*p.frozen_rule, p.last, v, p.hist);
+      else if constexpr (MODE == trace_general) { next = p.last; general_step(p.f, p.cache, p.rule, next, p.lo, v, p.hist); }
       else { next = p.last; resampled_step_cached(p.f, p.cache, p.rule, next, p.lo, v); }
       p.out[p.it] = next;
       ++p.written;
@@ -128,7 +132,7 @@ __device__ __forceinline__ void add_steps(const trace_launch& a, unsigned int st
 
 // One particle per thread: for launches with no more particles than resident
 // lanes, where refilling cannot help and warp votes would only add latency.
-template <bool FROZEN>
+template <int MODE>
 __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ trace_launch a)
 {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -137,7 +141,7 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ trac
   {
     lane_particle p;
     particle_start(a, p, i);
-    while (!particle_iteration<FROZEN>(a, p, steps)) {}
+    while (!particle_iteration<MODE>(a, p, steps)) {}
   }
   add_steps(a, steps);
 }
@@ -148,7 +152,7 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ trac
 // longer curves.  Every particle writes only its own slot range, its counts
 // and its exit-queue entry, so the result does not depend on which lane traced
 // it.
-template <bool FROZEN>
+template <int MODE>
 __global__ void __launch_bounds__(128) trace_persistent_kernel(const __grid_constant__ trace_launch a, int pool_size)
 {
   const int lane = threadIdx.x & 31;
@@ -182,7 +186,7 @@ __global__ void __launch_bounds__(128) trace_persistent_kernel(const __grid_cons
       }
     }
     if (need == full_mask) break;   // every lane idle, and the pools are exhausted
-    if (alive && particle_iteration<FROZEN>(a, p, steps)) alive = false;
+    if (alive && particle_iteration<MODE>(a, p, steps)) alive = false;
   }
   add_steps(a, steps);
 }
@@ -279,9 +283,11 @@ unsigned int grid_for(long long work, int threads)
 void launch_trace(pars_gpu_context& ctx, const trace_launch& a)
 {
   if (a.count <= 0) return;
-  const bool frozen = a.rule.frozen != 0;
-  const void* persistent = frozen ? (const void*)trace_persistent_kernel<true> : (const void*)trace_persistent_kernel<false>;
-  int& per_sm = ctx.trace_ctas_per_sm[frozen ? 0 : 1];
+  const int mode = a.rule.frozen ? trace_frozen : (a.rule.scheme == scheme_classic ? trace_classic : trace_general);
+  const void* persistent = mode == trace_frozen ? (const void*)trace_persistent_kernel<trace_frozen>
+                         : mode == trace_classic ? (const void*)trace_persistent_kernel<trace_classic>
+                                                 : (const void*)trace_persistent_kernel<trace_general>;
+  int& per_sm = ctx.trace_ctas_per_sm[mode];
   if (ctx.sm_count <= 0) PARS_CUDA(cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, ctx.device));
   if (per_sm < 0) PARS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent, 128, 0));
   const int sms = ctx.sm_count;
@@ -293,8 +299,9 @@ void launch_trace(pars_gpu_context& ctx, const trace_launch& a)
     // small counts so that the work spreads over all SMs
     const int threads = a.count <= 128LL * sms ? 32 : 128;
     const unsigned grid = (unsigned)((a.count + threads - 1) / threads);
-    if (frozen) trace_kernel<true><<<grid, threads, 0, ctx.stream>>>(a);
-    else        trace_kernel<false><<<grid, threads, 0, ctx.stream>>>(a);
+    if (mode == trace_frozen)       trace_kernel<trace_frozen><<<grid, threads, 0, ctx.stream>>>(a);
+    else if (mode == trace_classic) trace_kernel<trace_classic><<<grid, threads, 0, ctx.stream>>>(a);
+    else                            trace_kernel<trace_general><<<grid, threads, 0, ctx.stream>>>(a);
     return;
   }
   // pools of 256 particles when every resident warp gets several, else 32

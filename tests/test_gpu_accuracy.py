@@ -113,3 +113,41 @@ def test_ftle_of_linear_flow_is_analytic(ctx):
     assert np.abs(core - expected).max() <= 1e-4 * abs(expected)
     ctx.release_field(fm)
     ctx.release_field(h)
+
+
+@pytest.mark.parametrize("integrator", [0, 1, 3, 4, 5, 6, 7])
+def test_resampled_schemes_of_every_integrator_within_1e3_cells(ctx, port, integrator):
+    """Re-sampled stages ("true form") of the other integrators: streamlines
+    and flow maps against the FP64 oracle of the same scheme (1e-3 cells for
+    curves with the oracle's step count, as for RK4)."""
+    from pars_gb300 import native, workloads as W
+    f = W.abc_field(40)
+    seeds = port.seed_generate(f.offset, f.size, (f.spacing * np.float32(3)).astype(np.float32), 402)
+    h = ctx.upload_field(f)
+    s = ctx.trace(h, seeds, integrator, native.STAGES_RESAMPLED, 0.01)
+    vertices = np.concatenate([b["vertices"] for b in ctx.curves(s["batches"])])
+    curves = split_curves(vertices)
+    assert len(curves) == len(seeds)
+    end64, steps64, _ = port.advect_fp64(f, seeds["position"][:, :3].astype(np.float64), 400, integrator=integrator,
+                                         mode=1, step=0.01)
+    cell = float(f.spacing[0])
+    steps32 = np.array([len(c) - 1 for c in curves])
+    same = steps32 == steps64
+    assert same.mean() > 0.98
+    end32 = np.array([c[-1, :3] for c in curves], np.float64)
+    err = np.linalg.norm(end32[same] - end64[same], axis=1) / cell
+    assert err.max() <= 1e-3, f"max end-point error {err.max()} cells"
+    # flow map (per-seed kernel) against the same oracle
+    fm, _ = ctx.flow_map_generate(h, 201, 1.0, integrator, native.STAGES_RESAMPLED, 0.01)
+    flow = ctx.download_field(fm).reshape(-1, 3).astype(np.float64)
+    g = np.stack(np.meshgrid(*[np.arange(40, dtype=np.float32) * f.spacing[0]] * 3, indexing="ij"), -1).reshape(-1, 3)
+    pick = np.arange(0, len(g), 97)
+    e64, s64, _ = port.advect_fp64(f, g[pick].astype(np.float64), 200, integrator=integrator, mode=1, step=0.01)
+    inside = s64 == 200
+    assert inside.sum() >= 100
+    ferr = np.linalg.norm(flow[pick][inside] - e64[inside], axis=1) / cell
+    # (the flow map has no per-seed step count: a seed whose path grazes the
+    # boundary may stop on one side only)
+    assert (ferr <= 1e-3).mean() >= 0.99, np.quantile(ferr, 0.99)
+    ctx.release_field(fm)
+    ctx.release_field(h)

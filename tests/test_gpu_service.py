@@ -213,3 +213,38 @@ def test_profile_reports_kernels_and_phases(service):
     requests, batches = service.profile_get("batches.streamlines")   # (requests held, batches)
     assert requests == 6.0 and 1 <= batches <= 6
     service.profile_enable(False)
+
+
+def test_requests_with_the_other_integrators_equal_the_context_path(service, ctx):
+    """A Dormand-Prince streamline request and an Adams-Bashforth-Moulton FTLE
+    request (re-sampled stages) give what the context path gives, bit for bit,
+    also when they share their batches with RK4 requests."""
+    from pars_gb300 import native, workloads as W
+    from pars_gb300.requests import encode_settings
+    f = W.abc_field(28)
+    stream = {"mode": "streamlines", "dataset_filepath": "abc28", "seed_generation_stride": [4, 4, 4],
+              "seed_generation_iterations": 152, "particle_tracing_integrator": "runge_kutta_dormand_prince_5",
+              "particle_tracing_step_size": 0.01, "color_generation_mode": "rgb"}
+    ftle = {"mode": "ftle", "dataset_filepath": "abc28", "seed_generation_stride": [1, 1, 1],
+            "seed_generation_iterations": 81, "particle_tracing_integrator": "adams_bashforth_moulton_2",
+            "particle_tracing_step_size": 0.01}
+    mix = [r for r in _requests()][:3] + [stream, ftle] + [r for r in _requests()][-2:]
+    tickets = [service.submit(encode_settings(r)) for r in mix]
+    for t in tickets:
+        assert service.wait(t) == 2
+    got_curves = service.streamlines(tickets[3])
+    got_ftle = service.ftle(tickets[4])
+    for t in tickets:
+        service.release(t)
+    h = ctx.upload_field(f)
+    seeds = ctx.seed_generate(f.offset, f.size, (f.spacing * np.float32(4)).astype(np.float32), 152)
+    s = ctx.trace(h, seeds, native.INTEGRATORS["runge_kutta_dormand_prince_5"], native.STAGES_RESAMPLED, 0.01)
+    ctx.curves_index()
+    ctx.curves_color("rgb")
+    expected = [(b["vertices"], b["colors"], b["indices"]) for b in ctx.curves(s["batches"], True, True, True)]
+    assert _same(got_curves, expected, "streamlines")
+    fm, _ = ctx.flow_map_generate(h, 81, 1.0, native.INTEGRATORS["adams_bashforth_moulton_2"], native.STAGES_RESAMPLED, 0.01)
+    expected_ftle = ctx.ftle_generate(fm, np.float32(0.01) * 81, 0, shape=tuple(f.dims))
+    assert np.array_equal(got_ftle, expected_ftle, equal_nan=True)
+    ctx.release_field(fm)
+    ctx.release_field(h)

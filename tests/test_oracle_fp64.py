@@ -55,3 +55,28 @@ def test_ftle_fp64_of_linear_flow_map(port):
     ftle = port.ftle_fp64(flow, np.full(3, h, np.float32), T)
     expected = np.log(np.linalg.svd(M, compute_uv=False).max()) / T
     assert np.abs(ftle[2:-2, 2:-2, 2:-2] - expected).max() < 1e-5
+
+
+def test_every_integrator_has_its_order_on_an_exact_linear_field(port):
+    """The FP64 oracle's re-sampled schemes (the true forms of integrators.hpp:
+    16-23) on v = A (x - c) with dyadic A, grid and centre, which trilinear
+    interpolation reproduces exactly: halving h divides the error by 2^p,
+    p = 1 (Euler), 2 (modified midpoint, Adams-Bashforth 2, Adams-Bashforth-
+    Moulton 2), 4 (RK4), 5 (Cash-Karp, Dormand-Prince), >= 6.5 for
+    Fehlberg 7(8) before FP64 rounding takes over."""
+    from pars_gb300 import workloads as W
+    A = np.array([[0.25, 0.5, 0.0], [-0.5, 0.25, 0.125], [0.0, -0.125, -0.25]])
+    n, sp = 33, 0.25
+    f = W.linear_field(n, A, spacing=sp)
+    c = sp * (n - 1) / 2
+    start = np.array([[c + 0.5, c - 0.75, c + 0.25]])
+    T = 2.0
+    exact = scipy.linalg.expm(A * T) @ (start[0] - c) + c
+    orders = [1, 2, 4, 5, 5, 6.5, 2, 2]
+    for k, p in enumerate(orders):
+        hs = (0.5, 0.25) if k == 5 else (0.25, 0.125)
+        errs = []
+        for h in hs:
+            end, _, _ = port.advect_fp64(f, start, int(round(T / h)), integrator=k, mode=1, step=h)
+            errs.append(np.linalg.norm(end[0] - exact))
+        assert np.log2(errs[0] / errs[1]) >= p - 0.3, (k, errs)
