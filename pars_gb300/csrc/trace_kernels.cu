@@ -24,8 +24,9 @@ struct lane_particle
 {
   long long    i = 0;
   int          it = 0, N = 0, written = 0, kept = 0, block = 0;
-  float4       last = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4       last = make_float4(0.f, 0.f, 0.f, 0.f);   // the last vertex written
   float3       lo = make_float3(0.f, 0.f, 0.f);
+  local_position q {0, 0, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // re-sampled RK4 / Euler: cell + offset
   corner_cache cache;
   field_view   f {};
   step_rule    rule {};                      // re-sampled stages: the rule's h and scheme
@@ -35,6 +36,7 @@ struct lane_particle
 };
 
 // Loads particle i and writes its seed vertex (slot 0).
+template <int MODE>
 __device__ __forceinline__ void particle_start(const trace_launch& a, lane_particle& p, long long i)
 {
   p.i = i;
@@ -52,6 +54,7 @@ __device__ __forceinline__ void particle_start(const trace_launch& a, lane_parti
   p.written = 1;
   p.kept = is_invalid_vertex(p.last) ? 0 : 1;
   p.lo = make_float3(0.f, 0.f, 0.f);
+  if constexpr (MODE == trace_classic) p.q = to_local(p.f, p.last);
   p.cache = corner_cache();
   p.it = 1;
 }
@@ -62,9 +65,13 @@ __device__ __forceinline__ void particle_start(const trace_launch& a, lane_parti
 // is pushed onto the exit queue with one atomic — the queue is sorted by
 // (destination, source index) afterwards, so slots may be taken in any order).
 // MODE trace_frozen: the reference's scheme and FP32 operation order
-// (bit-exact).  MODE trace_classic: re-sampled stages of RK4 / Euler,
-// consistent cell weights, compensated position accumulation.  MODE
-// trace_general: the same for any re-sampled scheme (general_step).
+// (bit-exact).  MODE trace_classic: re-sampled stages of RK4 / Euler carried
+// in local cell coordinates (cell + offset + compensation, as the batched
+// engine does; the step-start test is the cell index, which differs from
+// contains() only within an ulp of the block's last face), each vertex
+// written as offset + (cell + u) h.  MODE trace_general: any re-sampled scheme
+// (general_step) on absolute positions with consistent cell weights and
+// compensated accumulation.
 template <int MODE>
 __device__ __forceinline__ bool particle_iteration(const trace_launch& a, lane_particle& p, unsigned int& steps)
 {
@@ -76,9 +83,13 @@ __device__ __forceinline__ bool particle_iteration(const trace_launch& a, lane_p
   {
     float3 v;
     bool inside;
-    constexpr bool FROZEN = MODE == trace_frozen;
-    if (FROZEN) inside = sample_inside(p.f, p.last, v);
-    else        inside = sample_start(p.f, p.cache, p.last, v);
+    if constexpr (MODE == trace_frozen) inside = sample_inside(p.f, p.last, v);
+    else if constexpr (MODE == trace_classic)
+    {
+      inside = local_inside(p.f, p.q);
+      if (inside) v = sample_local(p.f, p.cache, p.q.ix, p.q.iy, p.q.iz, p.q.ux, p.q.uy, p.q.uz);
+    }
+    else inside = sample_start(p.f, p.cache, p.last, v);
     if (!inside)
     {
       p.out[p.it] = term; ++p.written; ++p.kept; finish = true;
@@ -101,13 +112,17 @@ __device__ __forceinline__ bool particle_iteration(const trace_launch& a, lane_p
         }
       }
     }
-    else if (is_zero(v)) { p.out[p.it] = term; ++p.written; ++p.kept; finish = true; }
+    else if (MODE == trace_classic ? is_zero_local(p.f, v) : is_zero(v)) { p.out[p.it] = term; ++p.written; ++p.kept; finish = true; }
     else
     {
       float4 next;
       if constexpr (MODE == trace_frozen) next = frozen_step(*p.frozen_rule, p.last, v, p.hist);
       else if constexpr (MODE == trace_general) { next = p.last; general_step(p.f, p.cache, p.rule, next, p.lo, v, p.hist); }
-      else { next = p.last; resampled_step_cached(p.f, p.cache, p.rule, next, p.lo, v); }
+      else
+      {
+        local_step(p.f, p.cache, p.rule.rk4, p.rule.h, p.q, v);
+        next = to_absolute(p.f, p.q, p.last.w);
+      }
       p.out[p.it] = next;
       ++p.written;
       p.kept += is_invalid_vertex(next) ? 0 : 1;
@@ -140,7 +155,7 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ trac
   if (i < a.count)
   {
     lane_particle p;
-    particle_start(a, p, i);
+    particle_start<MODE>(a, p, i);
     while (!particle_iteration<MODE>(a, p, steps)) {}
   }
   add_steps(a, steps);
@@ -172,7 +187,7 @@ __global__ void __launch_bounds__(128) trace_persistent_kernel(const __grid_cons
         if (pool_next < pool_end)
         {
           const long long s = pool_next + __popc(need & lanes_below);
-          if (!alive && s < pool_end) { particle_start(a, p, s); alive = true; }
+          if (!alive && s < pool_end) { particle_start<MODE>(a, p, s); alive = true; }
           pool_next = min(pool_end, pool_next + (long long)__popc(need));
           need = __ballot_sync(full_mask, !alive);
           continue;
