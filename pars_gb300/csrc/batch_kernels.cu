@@ -13,10 +13,10 @@
 // (particle_advector.cpp:74-139): before every step it stops when it has
 // taken max_steps steps, left the grid or meets a zero velocity
 // (|v_i| <= 1e-5); its last position (and optionally its step count) is
-// written to the job's output.  Unsteady jobs test leaving the grid as the
-// reference's contains() does (floor of the IEEE quotient, start_cell);
-// steady jobs, carried in local cell coordinates, test their cell index,
-// which differs from that only within an ulp of the grid's last face.
+// written to the job's output.  Particles are carried in local cell
+// coordinates (steady and unsteady jobs alike) and test their cell index,
+// which differs from the reference's contains() (floor of the IEEE quotient)
+// only within an ulp of the grid's last face.
 #include "context.hpp"
 
 namespace pars
@@ -62,9 +62,8 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
   bool alive = false;
   long long seed = 0;
   int steps = 0;
-  float4 pos = make_float4(0.f, 0.f, 0.f, 0.f);   // unsteady: absolute position
-  float3 lo = make_float3(0.f, 0.f, 0.f);         // unsteady: its compensation term
-  local_position local {0, 0, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // steady: cell + offset
+  float4 pos = make_float4(0.f, 0.f, 0.f, 0.f);   // seed / end position
+  local_position local {0, 0, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // cell + offset
   lane_cache<UNSTEADY> cache;
   // current job's parameters (warp-uniform)
   field_view f {};
@@ -95,8 +94,7 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
             pos = make_float4(__fadd_rn(J.ox, __fmul_rn(J.sx, float(ix))), __fadd_rn(J.oy, __fmul_rn(J.sy, float(iy))),
                               __fadd_rn(J.oz, __fmul_rn(J.sz, float(iz))), 0.0f);
           }
-          lo = make_float3(0.f, 0.f, 0.f);
-          if constexpr (!UNSTEADY) local = to_local(f, pos);
+          local = to_local(f, pos);
           steps = 0;
           alive = true;
         }
@@ -144,24 +142,17 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
       bool retire = steps >= max_steps;
       if constexpr (UNSTEADY)
       {
-        axis_cell cx, cy, cz;
+        // local coordinates as for steady jobs, with the time of this step
+        // (start + n h, from n: no accumulated rounding)
+        if (!retire) retire = !local_inside(f, local);
         if (!retire)
         {
-          const bool in_x = start_cell(pos.x, f.ox, f.hx, f.inv_hx, f.nx, cx);
-          const bool in_y = start_cell(pos.y, f.oy, f.hy, f.inv_hy, f.ny, cy);
-          const bool in_z = start_cell(pos.z, f.oz, f.hz, f.inv_hz, f.nz, cz);
-          retire = !(in_x && in_y && in_z);
-        }
-        if (!retire)
-        {
-          step_rule r;
-          r.frozen = 0; r.rk4 = rk4; r.h = h; r.count = 0;
-          // time of this step: start + n h, from n (no accumulated rounding)
           const slice_time t = step_time(clock, steps);
-          const float3 k1 = sample_unsteady_cached(f, ta, cache.k, pos.x, pos.y, pos.z, t);
-          if (is_zero(k1)) retire = true;
-          else { unsteady_step(f, ta, clock, cache.k, r, pos, lo, k1, t); ++steps; ++job_steps; }
+          const float3 k1 = sample_local_unsteady(f, ta, cache.k, local.ix, local.iy, local.iz, local.ux, local.uy, local.uz, t);
+          if (is_zero_local(f, k1)) retire = true;
+          else { local_unsteady_step(f, ta, clock, cache.k, rk4, h, local, k1, t); ++steps; ++job_steps; }
         }
+        if (retire) pos = to_absolute(f, local, 0.0f);
       }
       else
       {

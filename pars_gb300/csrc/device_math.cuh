@@ -588,56 +588,6 @@ struct corner_cache2
   corner_cache c0, c1;
 };
 
-__device__ __forceinline__ float3 sample_unsteady_cached(const field_view& fv, const time_axis& ta, corner_cache2& k,
-                                                         float px, float py, float pz, const slice_time& t)
-{
-  axis_cell cx = cell_consistent(px, fv.ox, fv.hx, fv.inv_hx), cy = cell_consistent(py, fv.oy, fv.hy, fv.inv_hy),
-            cz = cell_consistent(pz, fv.oz, fv.hz, fv.inv_hz);
-  clamp_cell(cx, fv.nx); clamp_cell(cy, fv.ny); clamp_cell(cz, fv.nz);
-  int slice;
-  float wt;
-  slice_of(ta, t, slice, wt);
-  const int ix = int(cx.s), iy = int(cy.s), iz = int(cz.s);
-  if (slice != k.slice || ix != k.c0.ix || iy != k.c0.iy || iz != k.c0.iz)
-  {
-    field_view s0 = fv, s1 = fv;
-    s0.data = fv.data + (long long)slice * ta.slice_stride;
-    s1.data = fv.data + (long long)(ta.nt > 1 ? slice + 1 : slice) * ta.slice_stride;
-    corner_load(s0, k.c0, ix, iy, iz);
-    corner_load(s1, k.c1, ix, iy, iz);
-    k.slice = slice;
-  }
-  const float3 v0 = corner_eval(k.c0, cx.w, cy.w, cz.w);
-  if (wt == 0.0f) return v0;
-  const float3 v1 = corner_eval(k.c1, cx.w, cy.w, cz.w);
-  return make_float3(fmaf(wt, v1.x - v0.x, v0.x), fmaf(wt, v1.y - v0.y, v0.y), fmaf(wt, v1.z - v0.z, v0.z));
-}
-
-// One pathline step from (x, t): classical RK4 in space-time with re-sampled
-// stages at t, t + h/2, t + h/2, t + h, or the frozen rule (velocity at (x, t)).
-__device__ __forceinline__ void unsteady_step(const field_view& f, const time_axis& ta, const slice_clock& clock,
-                                              corner_cache2& k, const step_rule& r, float4& x, float3& lo,
-                                              const float3& k1, const slice_time& t)
-{
-  if (r.frozen || !r.rk4)
-  {
-    const float scale = r.h;
-    compensated_add(x.x, lo.x, scale * k1.x);
-    compensated_add(x.y, lo.y, scale * k1.y);
-    compensated_add(x.z, lo.z, scale * k1.z);
-    return;
-  }
-  const float hh = 0.5f * r.h;
-  const slice_time th = advance_time(t, clock, 0.5f), t1 = advance_time(t, clock, 1.0f);
-  const float3 k2 = sample_unsteady_cached(f, ta, k, fmaf(hh, k1.x, x.x), fmaf(hh, k1.y, x.y), fmaf(hh, k1.z, x.z), th);
-  const float3 k3 = sample_unsteady_cached(f, ta, k, fmaf(hh, k2.x, x.x), fmaf(hh, k2.y, x.y), fmaf(hh, k2.z, x.z), th);
-  const float3 k4 = sample_unsteady_cached(f, ta, k, fmaf(r.h, k3.x, x.x), fmaf(r.h, k3.y, x.y), fmaf(r.h, k3.z, x.z), t1);
-  const float h6 = r.h * (1.0f / 6.0f);
-  compensated_add(x.x, lo.x, h6 * (k1.x + 2.0f * (k2.x + k3.x) + k4.x));
-  compensated_add(x.y, lo.y, h6 * (k1.y + 2.0f * (k2.y + k3.y) + k4.y));
-  compensated_add(x.z, lo.z, h6 * (k1.z + 2.0f * (k2.z + k3.z) + k4.z));
-}
-
 // ---- Local cell coordinates (batched engine) -----------------------------------
 // A particle is carried as its cell (ix, iy, iz) and its offset u in [0, 1)^3
 // within that cell, in units of the cell; position = offset + (i + u) * h.
@@ -751,6 +701,69 @@ __device__ __forceinline__ void local_step(const field_view& f, corner_cache& k,
   const float3 k2 = sample_local(f, k, q.ix, q.iy, q.iz, fmaf(hh, k1.x, q.ux), fmaf(hh, k1.y, q.uy), fmaf(hh, k1.z, q.uz));
   const float3 k3 = sample_local(f, k, q.ix, q.iy, q.iz, fmaf(hh, k2.x, q.ux), fmaf(hh, k2.y, q.uy), fmaf(hh, k2.z, q.uz));
   const float3 k4 = sample_local(f, k, q.ix, q.iy, q.iz, fmaf(h, k3.x, q.ux), fmaf(h, k3.y, q.uy), fmaf(h, k3.z, q.uz));
+  const float h6 = h * (1.0f / 6.0f);
+  compensated_add(q.ux, q.lx, h6 * (k1.x + 2.0f * (k2.x + k3.x) + k4.x));
+  compensated_add(q.uy, q.ly, h6 * (k1.y + 2.0f * (k2.y + k3.y) + k4.y));
+  compensated_add(q.uz, q.lz, h6 * (k1.z + 2.0f * (k2.z + k3.z) + k4.z));
+  renormalize(q);
+}
+
+// Unsteady sample in local coordinates: the two slices around time t, blended
+// linearly in time; velocity in cells per unit time.
+__device__ __forceinline__ float3 sample_local_unsteady(const field_view& f, const time_axis& ta, corner_cache2& k, int cx, int cy,
+                                                        int cz, float ux, float uy, float uz, const slice_time& t)
+{
+  int ix = cx, iy = cy, iz = cz;
+  float wx = ux, wy = uy, wz = uz;
+  if (!in_unit_cube(ux, uy, uz))
+  {
+    const float fx = floorf(ux), fy = floorf(uy), fz = floorf(uz);
+    ix += int(fx); iy += int(fy); iz += int(fz);
+    wx -= fx; wy -= fy; wz -= fz;
+    if (ix < 0) { ix = 0; wx = 0.0f; } else if (ix > f.nx - 2) { ix = f.nx - 2; wx = 1.0f; }
+    if (iy < 0) { iy = 0; wy = 0.0f; } else if (iy > f.ny - 2) { iy = f.ny - 2; wy = 1.0f; }
+    if (iz < 0) { iz = 0; wz = 0.0f; } else if (iz > f.nz - 2) { iz = f.nz - 2; wz = 1.0f; }
+  }
+  int slice;
+  float wt;
+  slice_of(ta, t, slice, wt);
+  if (slice != k.slice || ix != k.c0.ix || iy != k.c0.iy || iz != k.c0.iz)
+  {
+    field_view s0 = f, s1 = f;
+    s0.data = f.data + (long long)slice * ta.slice_stride;
+    s1.data = f.data + (long long)(ta.nt > 1 ? slice + 1 : slice) * ta.slice_stride;
+    corner_load(s0, k.c0, ix, iy, iz);
+    corner_load(s1, k.c1, ix, iy, iz);
+    k.slice = slice;
+  }
+  float3 v = corner_eval(k.c0, wx, wy, wz);
+  if (wt != 0.0f)
+  {
+    const float3 v1 = corner_eval(k.c1, wx, wy, wz);
+    v = make_float3(fmaf(wt, v1.x - v.x, v.x), fmaf(wt, v1.y - v.y, v.y), fmaf(wt, v1.z - v.z, v.z));
+  }
+  return make_float3(f.inv_hx * v.x, f.inv_hy * v.y, f.inv_hz * v.z);
+}
+
+// One pathline step in local coordinates: classical RK4 in space-time (stages
+// at t, t + h/2, t + h/2, t + h) or Euler, k1 sampled at (q, t).
+__device__ __forceinline__ void local_unsteady_step(const field_view& f, const time_axis& ta, const slice_clock& clock,
+                                                    corner_cache2& k, int rk4, float h, local_position& q, const float3& k1,
+                                                    const slice_time& t)
+{
+  if (!rk4)
+  {
+    compensated_add(q.ux, q.lx, h * k1.x);
+    compensated_add(q.uy, q.ly, h * k1.y);
+    compensated_add(q.uz, q.lz, h * k1.z);
+    renormalize(q);
+    return;
+  }
+  const float hh = 0.5f * h;
+  const slice_time th = advance_time(t, clock, 0.5f), t1 = advance_time(t, clock, 1.0f);
+  const float3 k2 = sample_local_unsteady(f, ta, k, q.ix, q.iy, q.iz, fmaf(hh, k1.x, q.ux), fmaf(hh, k1.y, q.uy), fmaf(hh, k1.z, q.uz), th);
+  const float3 k3 = sample_local_unsteady(f, ta, k, q.ix, q.iy, q.iz, fmaf(hh, k2.x, q.ux), fmaf(hh, k2.y, q.uy), fmaf(hh, k2.z, q.uz), th);
+  const float3 k4 = sample_local_unsteady(f, ta, k, q.ix, q.iy, q.iz, fmaf(h, k3.x, q.ux), fmaf(h, k3.y, q.uy), fmaf(h, k3.z, q.uz), t1);
   const float h6 = h * (1.0f / 6.0f);
   compensated_add(q.ux, q.lx, h6 * (k1.x + 2.0f * (k2.x + k3.x) + k4.x));
   compensated_add(q.uy, q.ly, h6 * (k1.y + 2.0f * (k2.y + k3.y) + k4.y));
