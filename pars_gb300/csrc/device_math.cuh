@@ -197,6 +197,31 @@ __device__ __forceinline__ float corner_eval1(float c000, float c001, float c010
   return lerp_fast(lerp_fast(c00, c01, wy), lerp_fast(c10, c11, wy), wx);
 }
 
+// The reference's blend (lerp_exact along z, then y, then x) of a cached cell:
+// the same arithmetic as blend8, so the frozen path stays bit-exact.
+__device__ __forceinline__ float3 blend8_cached(const corner_cache& k, float wx, float wy, float wz)
+{
+  const float4 c000 = make_float4(k.c000.x, k.c000.y, k.c000.z, 0.f), c001 = make_float4(k.c001.x, k.c001.y, k.c001.z, 0.f);
+  const float4 c010 = make_float4(k.c010.x, k.c010.y, k.c010.z, 0.f), c011 = make_float4(k.c011.x, k.c011.y, k.c011.z, 0.f);
+  const float4 c100 = make_float4(k.c100.x, k.c100.y, k.c100.z, 0.f), c101 = make_float4(k.c101.x, k.c101.y, k.c101.z, 0.f);
+  const float4 c110 = make_float4(k.c110.x, k.c110.y, k.c110.z, 0.f), c111 = make_float4(k.c111.x, k.c111.y, k.c111.z, 0.f);
+  return blend8(c000, c001, c010, c011, c100, c101, c110, c111, wx, wy, wz);
+}
+
+// contains() followed by interpolate() at p (the reference's cell search and
+// blend), the cell's corners kept in the lane's cache between steps.
+__device__ __forceinline__ bool sample_inside_cached(const field_view& f, corner_cache& k, const float4& p, float3& v)
+{
+  const axis_cell cx = cell_of(p.x, f.ox, f.hx);
+  const axis_cell cy = cell_of(p.y, f.oy, f.hy);
+  const axis_cell cz = cell_of(p.z, f.oz, f.hz);
+  if (!(cell_inside(cx.s, f.nx) && cell_inside(cy.s, f.ny) && cell_inside(cz.s, f.nz))) return false;
+  const int ix = int(cx.s), iy = int(cy.s), iz = int(cz.s);
+  if (ix != k.ix || iy != k.iy || iz != k.iz) corner_load(f, k, ix, iy, iz);
+  v = blend8_cached(k, cx.w, cy.w, cz.w);
+  return true;
+}
+
 __device__ __forceinline__ float3 corner_eval(const corner_cache& k, float wx, float wy, float wz)
 {
   return make_float3(corner_eval1(k.c000.x, k.c001.x, k.c010.x, k.c011.x, k.c100.x, k.c101.x, k.c110.x, k.c111.x, wx, wy, wz),

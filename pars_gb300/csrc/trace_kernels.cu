@@ -83,7 +83,7 @@ __device__ __forceinline__ bool particle_iteration(const trace_launch& a, lane_p
   {
     float3 v;
     bool inside;
-    if constexpr (MODE == trace_frozen) inside = sample_inside(p.f, p.last, v);
+    if constexpr (MODE == trace_frozen) inside = sample_inside_cached(p.f, p.cache, p.last, v);
     else if constexpr (MODE == trace_classic)
     {
       inside = local_inside(p.f, p.q);
