@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(256) flow_map_kernel(const __grid_constant__ f
     {
       float3 v;
       bool inside;
-      if (FROZEN) inside = sample_inside(a.f, pos, v);
+      if (FROZEN) inside = sample_inside_cached(a.f, cache, pos, v);
       else        inside = sample_start(a.f, cache, pos, v);
       if (!inside) { finished = true; break; }
       if (is_zero(v)) { finished = true; break; }
