@@ -10,6 +10,8 @@
 //   pa::partitioner         pa/include/pa/stages/partitioner.hpp:12-53
 //   pa::flow_map_generator  pa/include/pa/stages/flow_map_generator.hpp:10-28
 //   pa::ftle_map_generator  pa/include/pa/stages/ftle_map_generator.hpp:11-40
+//   pa::data_io             pa/include/pa/stages/data_io.hpp (on "pars raw" files)
+//   pars::ray_tracer        pars/include/pars/stages/ray_tracer.hpp:24-44
 // The value types are layout-compatible with the reference's (pa::particle is
 // 48 bytes with the same field offsets; vector4 is 16 bytes), so a caller
 // holding the reference's std::vector<pa::particle> can pass its data()
@@ -329,6 +331,123 @@ private:
   mode    mode_;
   int32_t flow_map_ = -1;
   scalar  time_ = 1;
+};
+
+// pa::data_io on "pars raw" files (pars_gpu.h): the rank's ghosted block of a
+// file's vector field (uploaded) or scalar field, and FTLE write-back.
+class data_io
+{
+public:
+  data_io(device& dev, integer ranks = 1, integer rank = 0) : dev_(dev), ranks_(ranks), rank_(rank) {}
+  void set_file(const std::string& path) { path_ = path; }
+  ivector3 load_dimensions() const
+  {
+    int32_t components = 0;
+    int64_t shape[3];
+    float spacing[3];
+    check(dev_.get(), pars_gpu_raw_info(path_.c_str(), &components, shape, spacing), "pars_gpu_raw_info");
+    return ivector3 {{integer(shape[0]), integer(shape[1]), integer(shape[2])}};
+  }
+  // The block as a resident field handle (data_io.cpp:50-58, 90-114).
+  int32_t load_local_vector_field()
+  {
+    int32_t handle = -1;
+    check(dev_.get(), pars_gpu_field_load(dev_.get(), path_.c_str(), ranks_, rank_, &handle, nullptr), "pars_gpu_field_load");
+    return handle;
+  }
+  // A scalar dataset's block (data_io.cpp:41-49, 76-89); `file` names its own file.
+  scalar_field load_local_scalar_field(const std::string& file) const
+  {
+    scalar_field out;
+    check(dev_.get(), pars_gpu_scalar_load(file.c_str(), ranks_, rank_, nullptr, out.shape.data(), out.offset.data,
+                                           out.spacing.data, out.size.data), "pars_gpu_scalar_load");
+    out.data.resize((std::size_t)out.shape[0] * out.shape[1] * out.shape[2]);
+    check(dev_.get(), pars_gpu_scalar_load(file.c_str(), ranks_, rank_, out.data.data(), out.shape.data(), out.offset.data,
+                                           out.spacing.data, out.size.data), "pars_gpu_scalar_load");
+    return out;
+  }
+  // save_ftle_field (data_io.cpp:117-140): this rank's block at its voxel offset.
+  void save_ftle_field(const std::string& file, const scalar_field& ftle, const std::array<integer, 3>& domain,
+                       const std::array<integer, 3>& voxel_offset) const
+  {
+    check(dev_.get(), pars_gpu_ftle_save(file.c_str(), domain.data(), voxel_offset.data(), ftle.shape.data(), ftle.data.data(),
+                                         ftle.spacing.data), "pars_gpu_ftle_save");
+  }
+  // save_integral_curves (data_io.cpp:142-196) of the device's current curves.
+  void save_integral_curves(const std::string& file) const
+  {
+    check(dev_.get(), pars_gpu_curves_export_vtk(dev_.get(), file.c_str()), "pars_gpu_curves_export_vtk");
+  }
+
+private:
+  device&     dev_;
+  integer     ranks_, rank_;
+  std::string path_;
+};
+
+// pars::ray_tracer (ray_tracer.hpp:24-44) on the device; serialize() returns
+// the `image` reply (image.proto) as bytes.
+class ray_tracer
+{
+public:
+  explicit ray_tracer(device& dev) : dev_(dev) {}
+  void set_volume(const scalar_field& volume)
+  {
+    check(dev_.get(), pars_gpu_ray_tracer_set_volume(dev_.get(), volume.data.data(), volume.shape.data(), volume.offset.data,
+                                                     volume.spacing.data), "pars_gpu_ray_tracer_set_volume");
+  }
+  // The device's current curves (traced, indexed, coloured).
+  void set_integral_curves(float radius)
+  {
+    check(dev_.get(), pars_gpu_ray_tracer_set_integral_curves(dev_.get(), radius), "pars_gpu_ray_tracer_set_integral_curves");
+  }
+  void set_integral_curves(const std::vector<integral_curves>& curves, float radius)
+  {
+    std::vector<int64_t> vertex_counts, index_counts;
+    std::vector<const float*> vertices, colors;
+    std::vector<const int32_t*> indices;
+    for (const auto& c : curves)
+    {
+      vertex_counts.push_back((int64_t)c.vertices.size());
+      index_counts.push_back((int64_t)c.indices.size());
+      vertices.push_back(c.vertices.empty() ? nullptr : c.vertices[0].data);
+      colors.push_back(c.colors.size() == c.vertices.size() && !c.colors.empty() ? c.colors[0].data : nullptr);
+      indices.push_back(c.indices.empty() ? nullptr : c.indices.data());
+    }
+    check(dev_.get(), pars_gpu_ray_tracer_set_integral_curves_host(dev_.get(), (int64_t)curves.size(), vertex_counts.data(),
+                                                                   vertices.data(), colors.data(), index_counts.data(),
+                                                                   indices.data(), radius),
+          "pars_gpu_ray_tracer_set_integral_curves_host");
+  }
+  void set_camera(const vector3& position, const vector3& forward, const vector3& up)
+  {
+    check(dev_.get(), pars_gpu_ray_tracer_set_camera(dev_.get(), position.data, forward.data, up.data), "pars_gpu_ray_tracer_set_camera");
+  }
+  void set_image_size(integer width, integer height)
+  {
+    check(dev_.get(), pars_gpu_ray_tracer_set_image_size(dev_.get(), width, height), "pars_gpu_ray_tracer_set_image_size");
+  }
+  void trace(std::size_t iterations = 1)
+  {
+    check(dev_.get(), pars_gpu_ray_tracer_trace(dev_.get(), (int32_t)iterations), "pars_gpu_ray_tracer_trace");
+  }
+  std::string serialize()
+  {
+    int32_t size[2] = {0, 0};
+    check(dev_.get(), pars_gpu_ray_tracer_serialize(dev_.get(), nullptr, size), "pars_gpu_ray_tracer_serialize");
+    std::vector<uint8_t> rgba((std::size_t)size[0] * size[1] * 4);
+    check(dev_.get(), pars_gpu_ray_tracer_serialize(dev_.get(), rgba.data(), size), "pars_gpu_ray_tracer_serialize");
+    int64_t length = 0;
+    if (pars_gpu_image_encode(size, rgba.data(), (int64_t)rgba.size(), nullptr, 0, &length) != PARS_OK)
+      throw std::runtime_error("pars_gpu_image_encode failed");
+    std::string message((std::size_t)length, '\0');
+    if (pars_gpu_image_encode(size, rgba.data(), (int64_t)rgba.size(), reinterpret_cast<uint8_t*>(&message[0]), length, &length) != PARS_OK)
+      throw std::runtime_error("pars_gpu_image_encode failed");
+    return message;
+  }
+
+private:
+  device& dev_;
 };
 }
 

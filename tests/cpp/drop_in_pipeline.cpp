@@ -1,7 +1,8 @@
 // The stage sequence of pars::pipeline::execute (pars/source/pipeline.cpp:
-// 107-260) and execute_ftle (:345-409), written against the C++ drop-in
-// (include/pa_gpu.hpp).  Reads a raw field, writes the curves and the FTLE
-// field as raw files for tests/test_gpu_drop_in.py to compare with the oracle.
+// 107-337) and execute_ftle (:345-409), written against the C++ drop-in
+// (include/pa_gpu.hpp).  Reads a raw field, writes the curves, the `image`
+// reply of the ray tracer and the FTLE field as raw files for
+// tests/test_gpu_drop_in.py to compare with the oracle.
 //
 // usage: drop_in_pipeline field.bin nx ny nz spacing stride iterations step out_dir
 #include <cstdio>
@@ -69,6 +70,16 @@ int main(int argc, char** argv)
       pa_gpu::index_generator::generate(device, &again);
       if (again.indices != curves[b].indices) { std::fprintf(stderr, "index_generator mismatch\n"); return 1; }
     }
+
+    // 6.0-6.6 ray_tracer: camera, image size, the curves, trace, serialize
+    pa_gpu::ray_tracer tracer6(device);
+    tracer6.set_camera(pa_gpu::vector3 {{3.0f, 3.2f, 13.0f}}, pa_gpu::vector3 {{0.0f, 0.0f, -1.0f}}, pa_gpu::vector3 {{0.0f, 1.0f, 0.0f}});
+    tracer6.set_image_size(64, 48);
+    tracer6.set_integral_curves(curves, 0.05f);
+    tracer6.trace(2);
+    const std::string image = tracer6.serialize();
+    std::ofstream im(out + "/image.bin", std::ios::binary);
+    im.write(image.data(), (std::streamsize)image.size());
 
     // execute_ftle: 2.1 flow_map_generator, 3.0-3.1 ftle_map_generator
     pa_gpu::flow_map_generator flow(device);

@@ -67,3 +67,16 @@ def test_invalid_arguments_are_rejected_without_a_gpu():
         lib.pars_gpu_destroy(handle)
         pytest.skip("a CUDA device is present")
     assert status in (-1, -2)
+
+
+def test_cpp_drop_in_header_compiles_and_links(tmp_path):
+    """include/pa_gpu.hpp (the C++ stage classes, ray tracer and data_io
+    included) compiles with the pipeline driver and links against the library
+    (running it needs a GPU: tests/test_gpu_drop_in.py)."""
+    from pars_gb300 import native
+    lib_dir = os.path.dirname(native.LIBRARY_PATH)
+    exe = str(tmp_path / "drop_in_pipeline")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "drop_in_pipeline.cpp"), "-L" + lib_dir, "-lpars_gpu",
+                    "-Wl,-rpath," + lib_dir, "-o", exe], check=True)
+    assert os.path.exists(exe)

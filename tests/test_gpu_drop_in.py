@@ -1,7 +1,9 @@
 """The C++ drop-in (include/pa_gpu.hpp) driven the way pars::pipeline drives
 the reference stages (tests/cpp/drop_in_pipeline.cpp), compiled with g++ and
 checked against the oracle: bit-exact curves and indices, hsv colours within
-2e-6, FTLE within 1e-4 of the FP64 evaluation of the same flow map."""
+2e-6, the ray tracer's `image` reply byte-identical to the CPU restatement's
+render of the same curves, FTLE within 1e-4 of the FP64 evaluation of the
+same flow map."""
 import os
 import subprocess
 import tempfile
@@ -40,6 +42,17 @@ def test_cpp_drop_in_pipeline_matches_oracle(port):
             assert np.array_equal(v, e["vertices"])
             assert np.array_equal(i, e["indices"])
             assert_colors_equal(c, e["colors"], 2e-6)
+        from test_render_cpu import decode_image
+        size, data = decode_image(open(os.path.join(tmp, "image.bin"), "rb").read())
+        assert size == [64, 48]
+        batches = []
+        for b in range(len(expected.batches)):
+            v = np.fromfile(os.path.join(tmp, f"vertices_{b}.bin"), np.float32).reshape(-1, 4)
+            c = np.fromfile(os.path.join(tmp, f"colors_{b}.bin"), np.float32).reshape(-1, 4)
+            i = np.fromfile(os.path.join(tmp, f"indices_{b}.bin"), np.int32)
+            batches.append((v, c, i))
+        image, _ = port.render(batches, 0.05, ((3.0, 3.2, 13.0), (0.0, 0.0, -1.0), (0.0, 1.0, 0.0)), (64, 48), frames=2)
+        assert data == image.tobytes()
         flow, _ = port.flow_map(f, iterations, 1.0, 2, step)
         ftle = np.fromfile(os.path.join(tmp, "ftle.bin"), np.float32).reshape(tuple(f.dims))
         ref = port.ftle_fp64(flow, f.spacing, step * (iterations - 1))
