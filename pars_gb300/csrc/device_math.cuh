@@ -147,14 +147,6 @@ __device__ __forceinline__ axis_cell cell_consistent(float p, float o, float h, 
   return axis_cell{s, r * inv_h};
 }
 
-// Outside the grid the cell index is clamped to [0, n-2] and the weight to 0
-// or 1 (constant extension of the boundary values).
-__device__ __forceinline__ void clamp_cell(axis_cell& c, int n)
-{
-  if (!(c.s >= 0.0f)) { c.s = 0.0f; c.w = 0.0f; }
-  else if (c.s > float(n - 2)) { c.s = float(n - 2); c.w = 1.0f; }
-}
-
 // Lerp with one FMA (re-sampled path; not bit-exact with the reference).
 __device__ __forceinline__ float lerp_fast(float a, float b, float w) { return fmaf(w, b - a, a); }
 
@@ -227,54 +219,6 @@ __device__ __forceinline__ float3 corner_eval(const corner_cache& k, float wx, f
   return make_float3(corner_eval1(k.c000.x, k.c001.x, k.c010.x, k.c011.x, k.c100.x, k.c101.x, k.c110.x, k.c111.x, wx, wy, wz),
                      corner_eval1(k.c000.y, k.c001.y, k.c010.y, k.c011.y, k.c100.y, k.c101.y, k.c110.y, k.c111.y, wx, wy, wz),
                      corner_eval1(k.c000.z, k.c001.z, k.c010.z, k.c011.z, k.c100.z, k.c101.z, k.c110.z, k.c111.z, wx, wy, wz));
-}
-
-// The velocity at the consistent cells (cx, cy, cz) — clamped to the grid:
-// constant extension of the boundary values — through the lane's cached cell.
-__device__ __forceinline__ float3 sample_cached_cells(const field_view& fv, corner_cache& k, axis_cell cx, axis_cell cy, axis_cell cz)
-{
-  clamp_cell(cx, fv.nx); clamp_cell(cy, fv.ny); clamp_cell(cz, fv.nz);
-  const int ix = int(cx.s), iy = int(cy.s), iz = int(cz.s);
-  if (ix != k.ix || iy != k.iy || iz != k.iz) corner_load(fv, k, ix, iy, iz);
-  return corner_eval(k, cx.w, cy.w, cz.w);
-}
-
-__device__ __forceinline__ float3 sample_cached(const field_view& fv, corner_cache& k, float px, float py, float pz)
-{
-  return sample_cached_cells(fv, k, cell_consistent(px, fv.ox, fv.hx, fv.inv_hx), cell_consistent(py, fv.oy, fv.hy, fv.inv_hy),
-                             cell_consistent(pz, fv.oz, fv.hz, fv.inv_hz));
-}
-
-// Cell of one axis for the step-start test: the consistent pair (s, w), and
-// whether the reference's floor(rn(d / h)) (contains(), vector_field.cpp:16-17)
-// puts the point inside.  rn(d / h) can differ from s only when d / h lies
-// within half an ulp of s + 1 (at most (s + 1) 2^-24), i.e. when w is that
-// close to 1, or when d is a tiny negative number (a point just below the
-// grid's origin, where no representable remainder lies in [0, h) and w comes
-// out negative); the IEEE division is evaluated only when w < 0 or w is within
-// max(2^-20, (s + 1) 2^-22) of 1, which covers those cases with room for the
-// rounding of w itself.
-__device__ __forceinline__ bool start_cell(float p, float o, float h, float inv_h, int n, axis_cell& c)
-{
-  c = cell_consistent(p, o, h, inv_h);
-  float s_ref = c.s;
-  if (c.w < 0.0f || c.w >= 1.0f - fmaxf(0x1p-20f, (c.s + 1.0f) * 0x1p-22f)) s_ref = floorf(__fdiv_rn(__fsub_rn(p, o), h));
-  return cell_inside(s_ref, n);
-}
-
-// The reference's contains() at p (floor of the IEEE quotient per axis inside
-// [0, n-2], vector_field.cpp:16-17) and, when p is inside, the velocity there
-// through the cell cache — the IEEE divisions are evaluated only within
-// rounding distance of a cell face.
-__device__ __forceinline__ bool sample_start(const field_view& f, corner_cache& k, const float4& p, float3& v)
-{
-  axis_cell cx, cy, cz;
-  const bool in_x = start_cell(p.x, f.ox, f.hx, f.inv_hx, f.nx, cx);
-  const bool in_y = start_cell(p.y, f.oy, f.hy, f.inv_hy, f.ny, cy);
-  const bool in_z = start_cell(p.z, f.oz, f.hz, f.inv_hz, f.nz, cz);
-  if (!(in_x && in_y && in_z)) return false;
-  v = sample_cached_cells(f, k, cx, cy, cz);
-  return true;
 }
 
 // Eigen isZero() with its default precision (NumTraits<float>::dummy_precision).
@@ -435,93 +379,6 @@ __constant__ const rk_tableau rk_tableaux[4] = {
   make_tableau(6, cash_karp_a, cash_karp_b),
   make_tableau(6, dormand_prince_a, dormand_prince_b),
   make_tableau(13, fehlberg_a, fehlberg_b)};
-
-// RESAMPLED step: classical RK4 (or Euler) with the first-stage velocity k1
-// already sampled at x; stage points are sampled through the cell cache.
-__device__ __forceinline__ void resampled_step_cached(const field_view& f, corner_cache& k, const step_rule& r, float4& x,
-                                                      float3& lo, const float3& k1)
-{
-  if (!r.rk4)
-  {
-    compensated_add(x.x, lo.x, r.h * k1.x);
-    compensated_add(x.y, lo.y, r.h * k1.y);
-    compensated_add(x.z, lo.z, r.h * k1.z);
-    return;
-  }
-  const float hh = 0.5f * r.h;
-  const float3 k2 = sample_cached(f, k, fmaf(hh, k1.x, x.x), fmaf(hh, k1.y, x.y), fmaf(hh, k1.z, x.z));
-  const float3 k3 = sample_cached(f, k, fmaf(hh, k2.x, x.x), fmaf(hh, k2.y, x.y), fmaf(hh, k2.z, x.z));
-  const float3 k4 = sample_cached(f, k, fmaf(r.h, k3.x, x.x), fmaf(r.h, k3.y, x.y), fmaf(r.h, k3.z, x.z));
-  const float h6 = r.h * (1.0f / 6.0f);
-  compensated_add(x.x, lo.x, h6 * (k1.x + 2.0f * (k2.x + k3.x) + k4.x));
-  compensated_add(x.y, lo.y, h6 * (k1.y + 2.0f * (k2.y + k3.y) + k4.y));
-  compensated_add(x.z, lo.z, h6 * (k1.z + 2.0f * (k2.z + k3.z) + k4.z));
-}
-
-// RESAMPLED step of any scheme: the classic one above, an explicit tableau
-// (stage s sampled at x + h sum_j a_sj k_j, then x += h sum_i b_i k_i), or a
-// two-step Adams scheme whose history (the previous step's k1) is kept per
-// particle.  Position updates are compensated as in the classic step.
-__device__ __forceinline__ void general_step(const field_view& f, corner_cache& cache, const step_rule& r, float4& x, float3& lo,
-                                             const float3& k1, frozen_history& hist)
-{
-  if (r.scheme == scheme_classic) { resampled_step_cached(f, cache, r, x, lo, k1); return; }
-  float3 delta;
-  if (r.scheme == scheme_tableau)
-  {
-    const rk_tableau& T = rk_tableaux[r.tableau];
-    float3 k[13];
-    k[0] = k1;
-    for (int s = 1; s < T.stages; ++s)
-    {
-      float3 acc = make_float3(0.f, 0.f, 0.f);
-      for (int j = 0; j < s; ++j)
-      {
-        const float a = T.a[s][j];
-        if (a != 0.0f) acc = make_float3(fmaf(a, k[j].x, acc.x), fmaf(a, k[j].y, acc.y), fmaf(a, k[j].z, acc.z));
-      }
-      k[s] = sample_cached(f, cache, fmaf(r.h, acc.x, x.x), fmaf(r.h, acc.y, x.y), fmaf(r.h, acc.z, x.z));
-    }
-    float3 sum = make_float3(0.f, 0.f, 0.f);
-    for (int s = 0; s < T.stages; ++s)
-    {
-      const float b = T.b[s];
-      if (b != 0.0f) sum = make_float3(fmaf(b, k[s].x, sum.x), fmaf(b, k[s].y, sum.y), fmaf(b, k[s].z, sum.z));
-    }
-    delta = make_float3(r.h * sum.x, r.h * sum.y, r.h * sum.z);
-  }
-  else
-  {
-    // Adams-Bashforth 2: x + h (3/2 k_n - 1/2 k_{n-1}); a particle's first
-    // step is RK4.  Adams-Bashforth-Moulton 2: that prediction x*, then the
-    // trapezoid x + h/2 (k_n + f(x*)).
-    float4 predicted = x;
-    float3 predicted_lo = lo;
-    if (hist.started)
-    {
-      const float3 ab = make_float3(fmaf(1.5f, k1.x, -0.5f * hist.v.x), fmaf(1.5f, k1.y, -0.5f * hist.v.y),
-                                    fmaf(1.5f, k1.z, -0.5f * hist.v.z));
-      compensated_add(predicted.x, predicted_lo.x, r.h * ab.x);
-      compensated_add(predicted.y, predicted_lo.y, r.h * ab.y);
-      compensated_add(predicted.z, predicted_lo.z, r.h * ab.z);
-    }
-    else
-    {
-      step_rule classic = r;
-      classic.rk4 = 1;
-      resampled_step_cached(f, cache, classic, predicted, predicted_lo, k1);
-    }
-    hist.v = k1;
-    hist.started = 1;
-    if (r.scheme == scheme_adams_bashforth) { x = predicted; lo = predicted_lo; return; }
-    const float3 kp = sample_cached(f, cache, predicted.x, predicted.y, predicted.z);
-    const float hh = 0.5f * r.h;
-    delta = make_float3(hh * (k1.x + kp.x), hh * (k1.y + kp.y), hh * (k1.z + kp.z));
-  }
-  compensated_add(x.x, lo.x, delta.x);
-  compensated_add(x.y, lo.y, delta.y);
-  compensated_add(x.z, lo.z, delta.z);
-}
 
 // ---- Unsteady fields (pathlines) ----------------------------------------------
 // An unsteady field is a sequence of `nt` slices of one grid, slice k holding
@@ -793,6 +650,71 @@ __device__ __forceinline__ void local_unsteady_step(const field_view& f, const t
   compensated_add(q.ux, q.lx, h6 * (k1.x + 2.0f * (k2.x + k3.x) + k4.x));
   compensated_add(q.uy, q.ly, h6 * (k1.y + 2.0f * (k2.y + k3.y) + k4.y));
   compensated_add(q.uz, q.lz, h6 * (k1.z + 2.0f * (k2.z + k3.z) + k4.z));
+  renormalize(q);
+}
+
+// RESAMPLED step of any scheme in local coordinates (k1 sampled at q, in cells
+// per unit time): the classic step above, an explicit tableau (stage s at
+// u + h sum_j a_sj k_j), or a two-step Adams scheme whose history (the
+// previous step's k1) is kept per particle; offsets accumulate compensated.
+__device__ __forceinline__ void general_step_local(const field_view& f, corner_cache& cache, const step_rule& r, local_position& q,
+                                                   const float3& k1, frozen_history& hist)
+{
+  if (r.scheme == scheme_classic) { local_step(f, cache, r.rk4, r.h, q, k1); return; }
+  float3 delta;
+  if (r.scheme == scheme_tableau)
+  {
+    const rk_tableau& T = rk_tableaux[r.tableau];
+    float3 k[13];
+    k[0] = k1;
+    for (int s = 1; s < T.stages; ++s)
+    {
+      float3 acc = make_float3(0.f, 0.f, 0.f);
+      for (int j = 0; j < s; ++j)
+      {
+        const float a = T.a[s][j];
+        if (a != 0.0f) acc = make_float3(fmaf(a, k[j].x, acc.x), fmaf(a, k[j].y, acc.y), fmaf(a, k[j].z, acc.z));
+      }
+      k[s] = sample_local(f, cache, q.ix, q.iy, q.iz, fmaf(r.h, acc.x, q.ux), fmaf(r.h, acc.y, q.uy), fmaf(r.h, acc.z, q.uz));
+    }
+    float3 sum = make_float3(0.f, 0.f, 0.f);
+    for (int s = 0; s < T.stages; ++s)
+    {
+      const float b = T.b[s];
+      if (b != 0.0f) sum = make_float3(fmaf(b, k[s].x, sum.x), fmaf(b, k[s].y, sum.y), fmaf(b, k[s].z, sum.z));
+    }
+    delta = make_float3(r.h * sum.x, r.h * sum.y, r.h * sum.z);
+  }
+  else
+  {
+    // Adams-Bashforth 2: u + h (3/2 k_n - 1/2 k_{n-1}); a particle's first
+    // step is RK4.  Adams-Bashforth-Moulton 2: that prediction u*, then the
+    // trapezoid u + h/2 (k_n + f(u*)).
+    local_position predicted = q;
+    if (hist.started)
+    {
+      compensated_add(predicted.ux, predicted.lx, r.h * fmaf(1.5f, k1.x, -0.5f * hist.v.x));
+      compensated_add(predicted.uy, predicted.ly, r.h * fmaf(1.5f, k1.y, -0.5f * hist.v.y));
+      compensated_add(predicted.uz, predicted.lz, r.h * fmaf(1.5f, k1.z, -0.5f * hist.v.z));
+      renormalize(predicted);
+    }
+    else
+      local_step(f, cache, 1, r.h, predicted, k1);
+    hist.v = k1;
+    hist.started = 1;
+    if (r.scheme == scheme_adams_bashforth) { q = predicted; return; }
+    // f(u*) relative to the particle's own cell, which is inside the grid:
+    // the predictor's cell may not be, and sample_local clamps only offsets
+    // that leave the given cell (the cell differences are small integers, so
+    // the shifted offsets are exact).
+    const float3 kp = sample_local(f, cache, q.ix, q.iy, q.iz, predicted.ux + float(predicted.ix - q.ix),
+                                   predicted.uy + float(predicted.iy - q.iy), predicted.uz + float(predicted.iz - q.iz));
+    const float hh = 0.5f * r.h;
+    delta = make_float3(hh * (k1.x + kp.x), hh * (k1.y + kp.y), hh * (k1.z + kp.z));
+  }
+  compensated_add(q.ux, q.lx, delta.x);
+  compensated_add(q.uy, q.ly, delta.y);
+  compensated_add(q.uz, q.lz, delta.z);
   renormalize(q);
 }
 

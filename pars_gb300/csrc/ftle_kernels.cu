@@ -48,26 +48,35 @@ __global__ void __launch_bounds__(256) flow_map_kernel(const __grid_constant__ f
     const int ix = int(i / ((long long)a.pz * a.py));
     float4 pos = make_float4(__fadd_rn(a.ox, __fmul_rn(a.sx, float(ix))), __fadd_rn(a.oy, __fmul_rn(a.sy, float(iy))),
                              __fadd_rn(a.oz, __fmul_rn(a.sz, float(iz))), 0.0f);
-    bool finished = false;
-    float3 lo = make_float3(0.0f, 0.0f, 0.0f);
     corner_cache cache;
     frozen_history hist;
-    for (int it = 1; it < a.iterations; ++it)
+    if constexpr (FROZEN)
     {
-      float3 v;
-      bool inside;
-      if (FROZEN) inside = sample_inside_cached(a.f, cache, pos, v);
-      else        inside = sample_start(a.f, cache, pos, v);
-      if (!inside) { finished = true; break; }
-      if (is_zero(v)) { finished = true; break; }
-      if (FROZEN) pos = frozen_step(a.rule, pos, v, hist);
-      else general_step(a.f, cache, a.rule, pos, lo, v, hist);
-      ++steps;
-      if (it + 1 == a.iterations) { finished = true; break; }
+      for (int it = 1; it < a.iterations; ++it)
+      {
+        float3 v;
+        if (!sample_inside_cached(a.f, cache, pos, v) || is_zero(v)) break;
+        pos = frozen_step(a.rule, pos, v, hist);
+        ++steps;
+      }
+    }
+    else
+    {
+      // Re-sampled schemes in local cell coordinates (cell + offset +
+      // compensation); the position leaves them once, at the end.
+      local_position q = to_local(a.f, pos);
+      for (int it = 1; it < a.iterations; ++it)
+      {
+        if (!local_inside(a.f, q)) break;
+        const float3 v = sample_local(a.f, cache, q.ix, q.iy, q.iz, q.ux, q.uy, q.uz);
+        if (is_zero_local(a.f, v)) break;
+        general_step_local(a.f, cache, a.rule, q, v, hist);
+        ++steps;
+      }
+      if (steps) pos = to_absolute(a.f, q, 0.0f);
     }
     // With iterations <= 1 the reference never assigns the voxel; it keeps the
     // seed position here.
-    (void)finished;
     if (ix < a.fx && iy < a.fy && iz < a.fz)
       a.flow[((long long)ix * a.fy + iy) * a.fz + iz] = pos;
   }

@@ -25,7 +25,6 @@ struct lane_particle
   long long    i = 0;
   int          it = 0, N = 0, written = 0, kept = 0, block = 0;
   float4       last = make_float4(0.f, 0.f, 0.f, 0.f);   // the last vertex written
-  float3       lo = make_float3(0.f, 0.f, 0.f);
   local_position q {0, 0, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};   // re-sampled RK4 / Euler: cell + offset
   corner_cache cache;
   field_view   f {};
@@ -53,8 +52,7 @@ __device__ __forceinline__ void particle_start(const trace_launch& a, lane_parti
   p.out[0] = p.last;
   p.written = 1;
   p.kept = is_invalid_vertex(p.last) ? 0 : 1;
-  p.lo = make_float3(0.f, 0.f, 0.f);
-  if constexpr (MODE == trace_classic) p.q = to_local(p.f, p.last);
+  if constexpr (MODE != trace_frozen) p.q = to_local(p.f, p.last);
   p.cache = corner_cache();
   p.it = 1;
 }
@@ -69,9 +67,8 @@ __device__ __forceinline__ void particle_start(const trace_launch& a, lane_parti
 // in local cell coordinates (cell + offset + compensation, as the batched
 // engine does; the step-start test is the cell index, which differs from
 // contains() only within an ulp of the block's last face), each vertex
-// written as offset + (cell + u) h.  MODE trace_general: any re-sampled scheme
-// (general_step) on absolute positions with consistent cell weights and
-// compensated accumulation.
+// written as offset + (cell + u) h.  MODE trace_general: the same for any
+// re-sampled scheme (general_step_local).
 template <int MODE>
 __device__ __forceinline__ bool particle_iteration(const trace_launch& a, lane_particle& p, unsigned int& steps)
 {
@@ -84,12 +81,11 @@ __device__ __forceinline__ bool particle_iteration(const trace_launch& a, lane_p
     float3 v;
     bool inside;
     if constexpr (MODE == trace_frozen) inside = sample_inside_cached(p.f, p.cache, p.last, v);
-    else if constexpr (MODE == trace_classic)
+    else
     {
       inside = local_inside(p.f, p.q);
       if (inside) v = sample_local(p.f, p.cache, p.q.ix, p.q.iy, p.q.iz, p.q.ux, p.q.uy, p.q.uz);
     }
-    else inside = sample_start(p.f, p.cache, p.last, v);
     if (!inside)
     {
       p.out[p.it] = term; ++p.written; ++p.kept; finish = true;
@@ -112,15 +108,15 @@ __device__ __forceinline__ bool particle_iteration(const trace_launch& a, lane_p
         }
       }
     }
-    else if (MODE == trace_classic ? is_zero_local(p.f, v) : is_zero(v)) { p.out[p.it] = term; ++p.written; ++p.kept; finish = true; }
+    else if (MODE == trace_frozen ? is_zero(v) : is_zero_local(p.f, v)) { p.out[p.it] = term; ++p.written; ++p.kept; finish = true; }
     else
     {
       float4 next;
       if constexpr (MODE == trace_frozen) next = frozen_step(*p.frozen_rule, p.last, v, p.hist);
-      else if constexpr (MODE == trace_general) { next = p.last; general_step(p.f, p.cache, p.rule, next, p.lo, v, p.hist); }
       else
       {
-        local_step(p.f, p.cache, p.rule.rk4, p.rule.h, p.q, v);
+        if constexpr (MODE == trace_general) general_step_local(p.f, p.cache, p.rule, p.q, v, p.hist);
+        else local_step(p.f, p.cache, p.rule.rk4, p.rule.h, p.q, v);
         next = to_absolute(p.f, p.q, p.last.w);
       }
       p.out[p.it] = next;
