@@ -179,7 +179,7 @@ class Port(_Lib):
         L.orc_advect_fp64.restype = None
         L.orc_advect_fp64.argtypes = [_P] * 5 + [_P, _LL, _I, _I, _D, _LL, _P, _P, _P, _D, ctypes.c_ulonglong]
         L.orc_ftle_fp64.restype = None
-        L.orc_ftle_fp64.argtypes = [_P, _P, _P, _D, _P]
+        L.orc_ftle_fp64.argtypes = [_P, _P, _P, _D, _I, _P]
         L.orc_largest_eigenvalue.restype = None
         L.orc_largest_eigenvalue.argtypes = [_P, _LL, _P]
         L.orc_largest_eigenvalue_closed_form.restype = None
@@ -281,12 +281,13 @@ class Port(_Lib):
             same &= s == steps
         return clean, steps, spread, same
 
-    def ftle_fp64(self, flow, spacing, time):
+    def ftle_fp64(self, flow, spacing, time, mode=0):
+        """mode 0: FTLE; mode 1: fractional anisotropy of C's eigenvalues."""
         flow = np.ascontiguousarray(flow, np.float32)
         dims = np.array(flow.shape[:3], np.int32)
         sp = np.ascontiguousarray(spacing, np.float32)
         out = np.zeros(flow.shape[:3], np.float64)
-        self.lib.orc_ftle_fp64(_ptr(flow), _ptr(dims), _ptr(sp), time, _ptr(out))
+        self.lib.orc_ftle_fp64(_ptr(flow), _ptr(dims), _ptr(sp), time, mode, _ptr(out))
         return out
 
     def largest_eigenvalue(self, matrices, closed_form=False):

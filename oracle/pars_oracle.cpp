@@ -696,11 +696,11 @@ void rk4_fp64(const field& f, double h, const double* x, const double* k1, doubl
   for (int c = 0; c < 3; ++c) out[c] = x[c] + h / 6.0 * (k1[c] + 2.0 * k2[c] + 2.0 * k3[c] + k4[c]);
 }
 
-// Largest eigenvalue of a symmetric 3x3 matrix by cyclic Jacobi rotations
-// (each rotation zeroes one off-diagonal entry; sweeps repeat until the
+// Eigenvalues of a symmetric 3x3 matrix by cyclic Jacobi rotations (each
+// rotation zeroes one off-diagonal entry; sweeps repeat until the
 // off-diagonal part vanishes), accurate to a few ulps of the matrix norm even
-// for repeated eigenvalues.  The FTLE oracle uses this one.
-double largest_eigenvalue_jacobi(const double in[3][3])
+// for repeated eigenvalues.  The FTLE oracle uses these.
+void eigenvalues_jacobi(const double in[3][3], double lambda[3])
 {
   double a[3][3];
   for (int r = 0; r < 3; ++r) for (int c = 0; c < 3; ++c) a[r][c] = 0.5 * (in[r][c] + in[c][r]);
@@ -731,7 +731,14 @@ double largest_eigenvalue_jacobi(const double in[3][3])
         a[p][q] = a[q][p] = 0.0;
       }
   }
-  return std::max(a[0][0], std::max(a[1][1], a[2][2]));
+  for (int i = 0; i < 3; ++i) lambda[i] = a[i][i];
+}
+
+double largest_eigenvalue_jacobi(const double in[3][3])
+{
+  double l[3];
+  eigenvalues_jacobi(in, l);
+  return std::max(l[0], std::max(l[1], l[2]));
 }
 
 // Largest eigenvalue of a symmetric 3x3 matrix (trigonometric closed form,
@@ -1132,9 +1139,12 @@ void orc_advect_unsteady_fp64(const float* xyz, const int dims[3], int slices, c
 
 // ---- FTLE, FP64 intended mathematics -------------------------------------------
 // J_ij = d phi_i / d x_j by central differences with denominator 2h_j, one-sided
-// at the grid borders (0 along an axis of extent 1); C = J^T J; FTLE =
-// log(sqrt(lambda_max(C))) / |T|.  flow: [X][Y][Z][3] (FP32), out FP64.
-void orc_ftle_fp64(const float* flow, const int dims[3], const float spacing[3], double time, double* out)
+// at the grid borders (0 along an axis of extent 1); C = J^T J with eigenvalues
+// l0, l1, l2.  mode 0 (regular): log(sqrt(max l)) / |T|.  mode 1 (fractional
+// anisotropy, ftle_map_generator.cpp:51-54): sqrt(0.5) sqrt((l0 - l1)^2 +
+// (l1 - l2)^2 + (l2 - l0)^2) / sqrt(l0^2 + l1^2 + l2^2).  flow: [X][Y][Z][3]
+// (FP32), out FP64.
+void orc_ftle_fp64(const float* flow, const int dims[3], const float spacing[3], double time, int mode, double* out)
 {
   const long long X = dims[0], Y = dims[1], Z = dims[2];
   #pragma omp parallel for schedule(static)
@@ -1161,8 +1171,15 @@ void orc_ftle_fp64(const float* flow, const int dims[3], const float spacing[3],
         for (int r = 0; r < 3; ++r)
           for (int c = 0; c < 3; ++c)
             C[r][c] = J[0][r] * J[0][c] + J[1][r] * J[1][c] + J[2][r] * J[2][c];
-        const double lambda = largest_eigenvalue_jacobi(C);
-        out[(x * Y + y) * Z + z] = std::log(std::sqrt(lambda)) / std::fabs(time);
+        double l[3];
+        eigenvalues_jacobi(C, l);
+        double value;
+        if (mode == 0) value = std::log(std::sqrt(std::max(l[0], std::max(l[1], l[2])))) / std::fabs(time);
+        else
+          value = std::sqrt(0.5) *
+                  std::sqrt((l[0] - l[1]) * (l[0] - l[1]) + (l[1] - l[2]) * (l[1] - l[2]) + (l[2] - l[0]) * (l[2] - l[0])) /
+                  std::sqrt(l[0] * l[0] + l[1] * l[1] + l[2] * l[2]);
+        out[(x * Y + y) * Z + z] = value;
       }
 }
 

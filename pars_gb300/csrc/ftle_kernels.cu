@@ -169,20 +169,29 @@ __global__ void __launch_bounds__(256) ftle_kernel(const ftle_args a)
     #pragma unroll
     for (int c = r; c < 3; ++c)
       C[r][c] = fmaf(J[2][r], J[2][c], fmaf(J[1][r], J[1][c], J[0][r] * J[0][c]));
-  float l0 = C[0][0], l1 = C[1][1], l2 = C[2][2];
-  jacobi_eigenvalues(l0, l1, l2, C[0][1], C[0][2], C[1][2]);
   float value;
   if constexpr (MODE == PARS_FTLE_REGULAR)
   {
     // log(sqrt(lambda_max)) / |T|
+    float l0 = C[0][0], l1 = C[1][1], l2 = C[2][2];
+    jacobi_eigenvalues(l0, l1, l2, C[0][1], C[0][2], C[1][2]);
     const float lambda = fmaxf(l0, fmaxf(l1, l2));
     value = 0.5f * logf(lambda) * a.inverse_time;
   }
   else
   {
-    // fractional anisotropy of the eigenvalues (ftle_map_generator.cpp:51-54)
-    const float d01 = l0 - l1, d12 = l1 - l2, d20 = l2 - l0;
-    value = 0.70710678f * sqrtf(d01 * d01 + d12 * d12 + d20 * d20) / sqrtf(l0 * l0 + l1 * l1 + l2 * l2);
+    // Fractional anisotropy of the eigenvalues (ftle_map_generator.cpp:51-54),
+    // sqrt(1/2) sqrt(sum_{i<j} (l_i - l_j)^2) / sqrt(sum_i l_i^2), from the
+    // invariants: sum_{i<j} (l_i - l_j)^2 = 3 |C - (tr C / 3) I|_F^2 and
+    // sum_i l_i^2 = |C|_F^2, so FA = sqrt(3/2) |dev C|_F / |C|_F — no
+    // eigen-solve, and the deviator's diagonal is formed before squaring, so
+    // nearly isotropic tensors keep their small anisotropy.
+    const float m = (C[0][0] + C[1][1] + C[2][2]) * (1.0f / 3.0f);
+    const float d0 = C[0][0] - m, d1 = C[1][1] - m, d2 = C[2][2] - m;
+    const float off = fmaf(C[0][1], C[0][1], fmaf(C[0][2], C[0][2], C[1][2] * C[1][2]));
+    const float dev = fmaf(2.0f, off, fmaf(d0, d0, fmaf(d1, d1, d2 * d2)));
+    const float all = fmaf(2.0f, off, fmaf(C[0][0], C[0][0], fmaf(C[1][1], C[1][1], C[2][2] * C[2][2])));
+    value = 1.22474487f * __fsqrt_rn(__fdiv_rn(dev, all));
   }
   a.out[i] = value;
 }

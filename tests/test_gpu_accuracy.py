@@ -97,6 +97,32 @@ def test_ftle_matches_fp64_on_the_same_flow_map(ctx, port):
     ctx.release_field(h)
 
 
+def test_fractional_anisotropy_matches_fp64_on_the_same_flow_map(ctx, port):
+    """FA mode (ftle_map_generator.cpp:51-54): FA lies in [0, 1]; the FP32
+    kernel (from the invariants of C) within 1e-5 absolute of the FP64
+    oracle's eigenvalue formula on the same flow map, and the isotropic case
+    (a flow map equal to the identity, C = I up to the FP32 rounding of the
+    lattice positions) gives the oracle's near-zero values."""
+    from pars_gb300 import workloads as W
+    f = W.abc_field(48, noise_sigma=0.01, seed=0)
+    h = ctx.upload_field(f)
+    fm, _ = ctx.flow_map_generate(h, 301, 1.0, 2, 1, 0.01)
+    flow = ctx.download_field(fm)
+    got = ctx.ftle_generate(fm, 3.0, 1, shape=tuple(f.dims))
+    ref = port.ftle_fp64(flow, f.spacing, 3.0, mode=1)
+    assert np.all((ref >= 0) & (ref <= 1 + 1e-12))
+    assert np.abs(got - ref).max() <= 1e-5, np.abs(got - ref).max()
+    # C = I: identity flow map on its own lattice (the seeds of one iteration)
+    fm1, _ = ctx.flow_map_generate(h, 1, 1.0, 2, 1, 0.01)
+    iso = ctx.ftle_generate(fm1, 3.0, 1, shape=tuple(f.dims))
+    iso_ref = port.ftle_fp64(ctx.download_field(fm1), f.spacing, 3.0, mode=1)
+    assert np.abs(iso_ref).max() <= 1e-5
+    assert np.abs(iso - iso_ref).max() <= 1e-6
+    ctx.release_field(fm1)
+    ctx.release_field(fm)
+    ctx.release_field(h)
+
+
 def test_ftle_of_linear_flow_is_analytic(ctx):
     from pars_gb300 import workloads as W
     A = np.array([[0.30, 0.05, 0.00], [0.02, -0.10, 0.04], [0.00, 0.03, -0.20]])

@@ -97,11 +97,14 @@ def test_reference_mode_streamlines_match_the_oracle(service, port):
         assert_colors_equal(c, e["colors"])
 
 
-def test_ftle_request_equals_the_context_path(service, ctx):
+@pytest.mark.parametrize("mode,ftle_mode", [("ftle", 0), ("ftle_fractional_anisotropy", 1)])
+def test_ftle_request_equals_the_context_path(service, ctx, mode, ftle_mode):
+    """A mode containing "fractional_anisotropy" asks for the anisotropy map
+    (ftle_map_generator.cpp:51-54) instead of the FTLE."""
     from pars_gb300 import native, workloads as W
     from pars_gb300.requests import encode_settings
     f = W.abc_field(40, noise_sigma=0.01, seed=4)
-    req = {"mode": "ftle", "dataset_filepath": "abc40", "seed_generation_stride": [1, 1, 1],
+    req = {"mode": mode, "dataset_filepath": "abc40", "seed_generation_stride": [1, 1, 1],
            "seed_generation_iterations": 151, "particle_tracing_integrator": "runge_kutta_4",
            "particle_tracing_step_size": 0.01}
     t = service.submit(encode_settings(req))
@@ -111,7 +114,7 @@ def test_ftle_request_equals_the_context_path(service, ctx):
     service.release(t)
     h = ctx.upload_field(f)
     fm, s = ctx.flow_map_generate(h, 151, 1.0, native.RUNGE_KUTTA_4, native.STAGES_RESAMPLED, 0.01)
-    expected = ctx.ftle_generate(fm, np.float32(0.01) * 151, 0, shape=tuple(f.dims))
+    expected = ctx.ftle_generate(fm, np.float32(0.01) * 151, ftle_mode, shape=tuple(f.dims))
     assert steps == s
     assert np.array_equal(got, expected)
     ctx.release_field(fm)

@@ -57,6 +57,24 @@ def test_ftle_fp64_of_linear_flow_map(port):
     assert np.abs(ftle[2:-2, 2:-2, 2:-2] - expected).max() < 1e-5
 
 
+def test_fractional_anisotropy_fp64_of_linear_flow_map(port):
+    """FA mode (ftle_map_generator.cpp:51-54) on phi(x) = M x: central
+    differences give J = M exactly, so FA is that of the eigenvalues of M^T M."""
+    A = np.array([[0.3, 0.05, 0.0], [0.02, -0.1, 0.04], [0.0, 0.03, -0.2]])
+    M = scipy.linalg.expm(A * 2.0)
+    n, h = 9, 0.1
+    g = np.stack(np.meshgrid(*[np.arange(n) * h] * 3, indexing="ij"), -1)
+    flow = (g @ M.T).astype(np.float32)
+    fa = port.ftle_fp64(flow, np.full(3, h, np.float32), 2.0, mode=1)
+    l = np.linalg.eigvalsh(M.T @ M)
+    expected = np.sqrt(0.5) * np.sqrt((l[0] - l[1]) ** 2 + (l[1] - l[2]) ** 2 + (l[2] - l[0]) ** 2) / np.sqrt((l ** 2).sum())
+    # FP32 flow-map samples limit the agreement
+    assert np.abs(fa[2:-2, 2:-2, 2:-2] - expected).max() < 1e-5
+    # an isotropic map (phi = 2 x): C = 4 I, anisotropy 0
+    iso = port.ftle_fp64((2 * g).astype(np.float32), np.full(3, h, np.float32), 2.0, mode=1)
+    assert np.abs(iso).max() < 1e-6
+
+
 def test_every_integrator_has_its_order_on_an_exact_linear_field(port):
     """The FP64 oracle's re-sampled schemes (the true forms of integrators.hpp:
     16-23) on v = A (x - c) with dyadic A, grid and centre, which trilinear
