@@ -99,9 +99,12 @@ raw_info read_header(int fd)
     PARS_REQUIRE(info.shape[i] >= 1 && info.shape[i] < (1LL << 31), "field file shape out of range");
     PARS_REQUIRE(info.spacing[i] > 0.0f, "field file spacing must be positive");
   }
+  // each extent is below 2^31, so the first product fits; the second must be checked
+  const uint64_t plane = uint64_t(info.shape[0]) * uint64_t(info.shape[1]);
+  PARS_REQUIRE(uint64_t(info.shape[2]) <= (uint64_t(1) << 58) / plane, "field file shape out of range");
   struct stat st {};
   PARS_REQUIRE(::fstat(fd, &st) == 0, "cannot stat the field file");
-  const uint64_t need = raw_header + uint64_t(info.shape[0]) * info.shape[1] * info.shape[2] * info.components * 4;
+  const uint64_t need = raw_header + plane * uint64_t(info.shape[2]) * info.components * 4;
   PARS_REQUIRE(uint64_t(st.st_size) >= need, "field file is shorter than its header says");
   return info;
 }
@@ -215,10 +218,12 @@ int32_t pars_gpu_raw_write(const char* path, int32_t components, const int64_t s
       info.shape[i] = shape[i];
       info.spacing[i] = spacing[i];
     }
+    const uint64_t plane = uint64_t(shape[0]) * uint64_t(shape[1]);
+    PARS_REQUIRE(uint64_t(shape[2]) <= (uint64_t(1) << 58) / plane, "shape out of range");
     pars::file_handle f;
     pars::open_file(f, path, O_WRONLY | O_CREAT | O_TRUNC);
     pars::write_header(f.fd, info);
-    pars::write_exact(f.fd, data, std::size_t(shape[0] * shape[1] * shape[2] * components) * 4, pars::raw_header);
+    pars::write_exact(f.fd, data, std::size_t(plane * uint64_t(shape[2]) * uint64_t(components)) * 4, pars::raw_header);
     return PARS_OK;
   }
   catch (const error& e) { return e.status; }
