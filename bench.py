@@ -120,6 +120,16 @@ class ClockSampler:
         except OSError:
             self.proc = None
 
+    def wait_ready(self, timeout=10.0):
+        """Blocks until the first sample arrives (at most `timeout` s): the
+        first nvidia-smi start on a machine can take a second or more, and
+        its NVML set-up stalls CUDA calls of this process meanwhile, so the
+        timed region starts only after it."""
+        deadline = time.time() + timeout
+        while self.proc and not self.rows and self.proc.poll() is None and time.time() < deadline:
+            time.sleep(0.02)
+        time.sleep(0.2)
+
     def _read(self):
         for line in self.proc.stdout:
             parts = [x.strip() for x in line.split(",")]
@@ -711,7 +721,10 @@ def main():
         ctx.release_field(fm)
         return steps
 
+    # the warm-up also runs the L2 flush: its first launch in a process loads
+    # the fill kernel's module, which on a cold machine pages in from disk
     for _ in range(max(args.warmup, 3)):
+        flush.zero_()
         device_step()
     torch.cuda.synchronize()
     if dist:
@@ -723,7 +736,7 @@ def main():
     ctx.profile_enable(True)
     launches0 = ctx.launch_count()
     sampler.start()
-    time.sleep(0.3)
+    sampler.wait_ready()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     total_steps = 0
     start.record(stream)
