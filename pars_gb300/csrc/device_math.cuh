@@ -9,10 +9,11 @@
 //   linear_interpolate         pa/include/pa/math/linear_interpolate.hpp:6-10
 //   isZero                     Eigen default precision 1e-5f
 //   frozen-velocity step       pa/source/stages/particle_tracer.cpp:315-334
-// The RESAMPLED path (classical RK4 with four samples per step) keeps the
-// reference's contains() test for termination but samples with a consistent
-// cell/weight pair, FMA lerps, and accumulates positions with a compensation
-// term (see cell_consistent and compensated_add).
+// The RESAMPLED paths (stages sampled where they fall) carry a particle in
+// local cell coordinates -- its cell, the offset in the cell and a
+// compensation term (local_position, compensated_add) -- sample with FMA
+// lerps on the register-cached corners of the cell, and end a curve when the
+// cell leaves the grid (local_inside).
 #pragma once
 
 #include <cstdint>
