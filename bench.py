@@ -4,8 +4,8 @@
 Workload (one "step"): the FTLE pipeline on a 256^3 FP32 ABC flow plus
 N(0, 0.01) noise (seed 0): one seed per grid vertex (16,777,216 particles),
 classical RK4 with four field samples per step, h = 0.01, at most 500 steps
-(T = 5), flow map, then the fused gradient / Cauchy-Green / FP64 eigenvalue /
-log FTLE kernel.  Metric: RK4 particle-steps per second (steps actually
+(T = 5), flow map, then the fused gradient / Cauchy-Green / Jacobi eigenvalue /
+log FTLE kernel (FP32).  Metric: RK4 particle-steps per second (steps actually
 taken), with FTLE voxels per second beside it.
 
 value : device-resident input, timed with CUDA events on the library's stream.
@@ -678,7 +678,7 @@ def main():
     max_steps = args.iterations - 1
     config = {"workload": f"ftle_{n}: ABC + N(0,0.01) noise (seed 0) on {n}^3 FP32 vertices of [0,2pi]^3, one seed per vertex "
                           f"({seeds} particles), classical RK4 (4 samples/step) h=0.01, <= {max_steps} steps (T=5), "
-                          "flow map + fused central-difference / Cauchy-Green / FP64 eigenvalue / log FTLE",
+                          "flow map + fused central-difference / Cauchy-Green / FP32 Jacobi eigenvalue / log FTLE",
               "grid": n, "seeds": seeds, "max_steps": max_steps, "step_size": 0.01, "stage_mode": "resampled",
               "ranks": world, "l2": f"inputs larger than L2 ({16 * n ** 3 / 1e6:.0f} MB float4 field) and a 256 MB L2 flush "
                                     "before every step"}

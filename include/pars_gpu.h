@@ -234,8 +234,10 @@ int32_t pars_gpu_color_generate(pars_gpu_context* context, const float* vertices
 int32_t pars_gpu_flow_map_generate(pars_gpu_context* context, int32_t field, int32_t iterations, float resolution_scale,
                                    int32_t integrator, int32_t stage_mode, float step_size, int32_t* flow_map, int64_t* steps);
 /* FTLE of a flow-map field: central-difference gradient (one-sided at the
- * borders), Cauchy-Green tensor, largest eigenvalue in FP64 closed form,
- * log(sqrt(lambda)) / |time| (mode REGULAR) or fractional anisotropy.  Writes
+ * borders), Cauchy-Green tensor C (FP32), then log(sqrt(lambda_max)) / |time|
+ * with lambda_max from cyclic Jacobi rotations (mode REGULAR), or the
+ * fractional anisotropy of C's eigenvalues (mode FRACTIONAL_ANISOTROPY,
+ * ftle_map_generator.cpp:51-54).  Writes
  * the FP32 field to HOST `ftle` (X*Y*Z floats) unless it is NULL, in which case
  * the result stays on the device (pars_gpu_ftle_device_pointer). */
 int32_t pars_gpu_ftle_generate    (pars_gpu_context* context, int32_t flow_map, float time, int32_t mode, float* ftle);

@@ -743,7 +743,7 @@ double largest_eigenvalue_jacobi(const double in[3][3])
 
 // Largest eigenvalue of a symmetric 3x3 matrix (trigonometric closed form,
 // O. K. Smith, "Eigenvalues of a symmetric 3x3 matrix", CACM 4(4), 1961).
-// Kept as a cross-check of the GPU's formula.
+// Kept as an independent cross-check of the Jacobi eigenvalues.
 double largest_eigenvalue(const double a[3][3])
 {
   const double p1 = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
@@ -1194,8 +1194,8 @@ void orc_largest_eigenvalue(const double* matrices, long long n, double* out)
   }
 }
 
-// The same with the trigonometric closed form (cross-check of the formula the
-// GPU's FTLE kernel evaluates).
+// The same with the trigonometric closed form (an independent cross-check of
+// the Jacobi eigenvalues).
 void orc_largest_eigenvalue_closed_form(const double* matrices, long long n, double* out)
 {
   for (long long i = 0; i < n; ++i)

@@ -15,8 +15,8 @@ def test_largest_eigenvalue_agrees_with_lapack(port):
     q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
     a = q @ np.diag([5.0, 5.0, 1.0]) @ q.T
     assert abs(port.largest_eigenvalue(a.reshape(1, 9))[0] - 5.0) < 1e-12
-    # the closed form the GPU evaluates: loses accuracy only near a repeated
-    # largest eigenvalue, and stays far inside the FTLE bar there
+    # the trigonometric closed form (cross-check): loses accuracy only near a
+    # repeated largest eigenvalue, and stays far inside the FTLE bar there
     closed = port.largest_eigenvalue(s.reshape(-1, 9), closed_form=True)
     assert np.allclose(closed, got, rtol=1e-10)
     assert abs(port.largest_eigenvalue(a.reshape(1, 9), closed_form=True)[0] - 5.0) < 1e-7
