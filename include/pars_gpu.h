@@ -260,12 +260,14 @@ int32_t pars_gpu_unsteady_field_upload_device(pars_gpu_context* context, const f
  * advected with the flow-map rules of particle_advector
  * (particle_advector.cpp:74-139: stop on leaving the grid, on a zero velocity,
  * or after max_steps steps).  Pathlines on unsteady fields use classical RK4
- * in space-time with the time of step n = time_begin + n * step_size in FP64. */
+ * in space-time with the time of step n = time_begin + n * step_size (about
+ * 44 bits).  PARS_STAGES_FROZEN jobs run the reference's scheme bit for bit
+ * (any of the eight integrators) on steady fields. */
 typedef struct pars_gpu_batch_job
 {
   int32_t      field;               /* field handle (steady or unsteady) */
-  int32_t      integrator;          /* PARS_EULER or PARS_RUNGE_KUTTA_4 (re-sampled stages; the engine's schemes) */
-  int32_t      stage_mode;          /* PARS_STAGES_RESAMPLED (PARS_STAGES_FROZEN: velocity of the step start) */
+  int32_t      integrator;          /* re-sampled stages: PARS_EULER or PARS_RUNGE_KUTTA_4; frozen: any */
+  int32_t      stage_mode;          /* PARS_STAGES_RESAMPLED, or PARS_STAGES_FROZEN (steady fields) */
   int32_t      max_steps;
   float        step_size;
   int32_t      padding0;
@@ -285,10 +287,12 @@ typedef struct pars_gpu_batch_job
  * seed chunks.  variant selects the launch shape (threads per CTA, register
  * budget) among pars_gpu_batch_variants(); -1 = autotuned: the first call of
  * each job class (steady / unsteady) times every variant on a probe of the
- * batch and keeps the fastest for the context. */
+ * batch and keeps the fastest for the context.  Each class (re-sampled
+ * steady, re-sampled unsteady, frozen) runs in its own launch. */
 int32_t pars_gpu_batch_advect  (pars_gpu_context* context, pars_gpu_batch_job* jobs, int32_t count, int32_t variant);
 int32_t pars_gpu_batch_variants(pars_gpu_context* context, int32_t* count);
-/* The tuned variant of a job class (0 steady, 1 unsteady), -1 if not tuned yet. */
+/* The tuned variant of a job class (0 re-sampled steady, 1 re-sampled
+ * unsteady, 2 frozen), -1 if not tuned yet. */
 int32_t pars_gpu_batch_tuned   (pars_gpu_context* context, int32_t job_class, int32_t* variant, int32_t* threads);
 
 /* ---- request service (pars_service, pars/source/service.cpp:20-69) ----------------

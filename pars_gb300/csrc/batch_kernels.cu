@@ -13,10 +13,13 @@
 // (particle_advector.cpp:74-139): before every step it stops when it has
 // taken max_steps steps, left the grid or meets a zero velocity
 // (|v_i| <= 1e-5); its last position (and optionally its step count) is
-// written to the job's output.  Particles are carried in local cell
-// coordinates (steady and unsteady jobs alike) and test their cell index,
-// which differs from the reference's contains() (floor of the IEEE quotient)
-// only within an ulp of the grid's last face.
+// written to the job's output.  Re-sampled jobs (steady and unsteady alike)
+// carry particles in local cell coordinates and test their cell index, which
+// differs from the reference's contains() (floor of the IEEE quotient) only
+// within an ulp of the grid's last face.  Frozen jobs (the reference's
+// scheme, any of the eight integrators) keep absolute positions and the
+// reference's arithmetic bit for bit, as flow_map_kernel<true> does, one
+// field sample per step on the lane's cached corners.
 #include "context.hpp"
 
 namespace pars
@@ -38,14 +41,14 @@ __device__ __forceinline__ int find_job(const batch_job_device* __restrict__ job
   return lo;
 }
 
-template <bool UNSTEADY>
-struct lane_cache;
-template <> struct lane_cache<false> { corner_cache k; };
-template <> struct lane_cache<true>  { corner_cache2 k; };
+template <int CLASS>
+struct lane_cache { corner_cache k; };
+template <> struct lane_cache<batch_unsteady> { corner_cache2 k; };
 
-// UNSTEADY = false: every job is on a steady field (one slice).
-// UNSTEADY = true: jobs may have several time slices (a steady job works too).
-template <int THREADS, int MIN_BLOCKS, bool UNSTEADY>
+// CLASS batch_steady: re-sampled stages, every job on a steady field (one
+// slice).  batch_unsteady: re-sampled stages, jobs may have several time
+// slices (a steady job works too).  batch_frozen: the frozen scheme.
+template <int THREADS, int MIN_BLOCKS, int CLASS>
 __global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
 batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long long total_pools,
                     unsigned long long* __restrict__ pool_counter)
@@ -64,13 +67,15 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
   int steps = 0;
   float4 pos = make_float4(0.f, 0.f, 0.f, 0.f);   // seed / end position
   local_position local {0, 0, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // cell + offset
-  lane_cache<UNSTEADY> cache;
+  frozen_history hist;                                            // frozen multistep scheme
+  lane_cache<CLASS> cache;
   // current job's parameters (warp-uniform)
   field_view f {};
   time_axis ta {};
   float h = 0.0f;
   int rk4 = 1, max_steps = 0;
   slice_clock clock {};
+  const step_rule* rule = nullptr;   // frozen jobs: the coefficients, read where they lie
 
   for (;;)
   {
@@ -94,7 +99,8 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
             pos = make_float4(__fadd_rn(J.ox, __fmul_rn(J.sx, float(ix))), __fadd_rn(J.oy, __fmul_rn(J.sy, float(iy))),
                               __fadd_rn(J.oz, __fmul_rn(J.sz, float(iz))), 0.0f);
           }
-          local = to_local(f, pos);
+          if constexpr (CLASS == batch_frozen) hist = frozen_history();
+          else local = to_local(f, pos);
           steps = 0;
           alive = true;
         }
@@ -124,7 +130,8 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
         job = pj;
         const batch_job_device& J = jobs[job];
         f = J.field; ta = J.time; h = J.rule.h; rk4 = J.rule.rk4; max_steps = J.max_steps; clock = J.clock;
-        cache = lane_cache<UNSTEADY>();
+        rule = &J.rule;
+        cache = lane_cache<CLASS>();
       }
       pending = -1;
       pool_next = (p - jobs[job].first_pool) * pool_seeds;
@@ -140,7 +147,17 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
     if (alive)
     {
       bool retire = steps >= max_steps;
-      if constexpr (UNSTEADY)
+      if constexpr (CLASS == batch_frozen)
+      {
+        // contains() + interpolate() at the step start, then the frozen step
+        if (!retire)
+        {
+          float3 v;
+          if (!sample_inside_cached(f, cache.k, pos, v) || is_zero(v)) retire = true;
+          else { pos = frozen_step(*rule, pos, v, hist); ++steps; ++job_steps; }
+        }
+      }
+      else if constexpr (CLASS == batch_unsteady)
       {
         // local coordinates as for steady jobs, with the time of this step
         // (start + n h, from n: no accumulated rounding)
@@ -202,15 +219,19 @@ struct variant
 
 // Launch shapes the autotuner chooses from, per job class: threads per CTA and
 // the minimum resident CTAs per SM that the register allocation must allow.
-const variant variants[2][4] = {
-  {{64, 1, (const void*)batch_advect_kernel<64, 1, false>},
-   {128, 1, (const void*)batch_advect_kernel<128, 1, false>},
-   {128, 6, (const void*)batch_advect_kernel<128, 6, false>},
-   {256, 1, (const void*)batch_advect_kernel<256, 1, false>}},
-  {{64, 1, (const void*)batch_advect_kernel<64, 1, true>},
-   {128, 1, (const void*)batch_advect_kernel<128, 1, true>},
-   {128, 3, (const void*)batch_advect_kernel<128, 3, true>},
-   {256, 1, (const void*)batch_advect_kernel<256, 1, true>}},
+const variant variants[batch_classes][4] = {
+  {{64, 1, (const void*)batch_advect_kernel<64, 1, batch_steady>},
+   {128, 1, (const void*)batch_advect_kernel<128, 1, batch_steady>},
+   {128, 6, (const void*)batch_advect_kernel<128, 6, batch_steady>},
+   {256, 1, (const void*)batch_advect_kernel<256, 1, batch_steady>}},
+  {{64, 1, (const void*)batch_advect_kernel<64, 1, batch_unsteady>},
+   {128, 1, (const void*)batch_advect_kernel<128, 1, batch_unsteady>},
+   {128, 3, (const void*)batch_advect_kernel<128, 3, batch_unsteady>},
+   {256, 1, (const void*)batch_advect_kernel<256, 1, batch_unsteady>}},
+  {{64, 1, (const void*)batch_advect_kernel<64, 1, batch_frozen>},
+   {128, 1, (const void*)batch_advect_kernel<128, 1, batch_frozen>},
+   {128, 6, (const void*)batch_advect_kernel<128, 6, batch_frozen>},
+   {256, 1, (const void*)batch_advect_kernel<256, 1, batch_frozen>}},
 };
 }
 

@@ -224,14 +224,14 @@ struct pars_gpu_context
   // batched advection: job table, counters, and the autotuned launch variant
   // per job class (0 = steady, 1 = unsteady); -1 = not tuned yet
   pars::device_buffer                     batch_jobs, batch_counters;
-  int                                     batch_variant[2] = {-1, -1};
+  int                                     batch_variant[3] = {-1, -1, -1};
   // tracing kernel: resident CTAs of 128 threads per SM (frozen, re-sampled
   // RK4 / Euler, re-sampled general schemes)
   // and the device's SM count, queried once
   int                                     trace_ctas_per_sm[3] = {-1, -1, -1};
   int                                     sm_count = 0;
   // batched engine: resident CTAs per SM per job class and launch shape
-  int                                     batch_ctas_per_sm[2][4] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}};
+  int                                     batch_ctas_per_sm[3][4] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}, {-1, -1, -1, -1}};
   static constexpr std::size_t            buffer_cache_limit = std::size_t(8) << 30;
   // instrumentation
   bool                                    profile = false;
@@ -368,10 +368,12 @@ struct batch_job_device
   long long           first_pool;     // pools of all earlier jobs
   unsigned long long* steps;          // per-job step counter
 };
+// Job classes of the batched engine: each class runs in its own launch.
+enum batch_class { batch_steady = 0, batch_unsteady = 1, batch_frozen = 2, batch_classes = 3 };
 int  batch_variant_count();
 int  batch_variant_threads(int variant);
 int  batch_pool_seeds();
-// job_class 0: all jobs steady; 1: some job unsteady.
+// job_class: batch_steady, batch_unsteady or batch_frozen.
 void launch_batch_advect(pars_gpu_context& ctx, int job_class, int variant, const batch_job_device* jobs, int njobs,
                          long long total_chunks, unsigned long long* counter);
 

@@ -542,59 +542,66 @@ void trace_single(pars_gpu_context& ctx, int32_t field, long long count, int32_t
   run_rounds(ctx, blocks, device_blocks, count, block_count, block_max, rule, false, summary);
 }
 
-// Runs batched jobs and returns each job's steps.  Jobs on steady fields (one
-// slice) and jobs on unsteady fields run in two persistent launches, one per
-// job class, so that a job's arithmetic, and so its result, does not depend on
-// the other jobs of the batch.  variant < 0 uses the context's tuned launch
+// Runs batched jobs and returns each job's steps.  Re-sampled jobs on steady
+// fields (one slice), re-sampled jobs on unsteady fields and frozen-scheme
+// jobs run in up to three persistent launches, one per job class, so that a
+// job's arithmetic, and so its result, does not depend on the other jobs of
+// the batch.  variant < 0 uses the context's tuned launch
 // shape for each class, tuning it first if needed: every job of the class
 // capped at 16384 seeds, each shape timed twice with CUDA events, the fastest
 // kept.
 std::vector<unsigned long long> execute_batch(pars_gpu_context& ctx, std::vector<batch_job_device>& jobs, int variant)
 {
   const int count = int(jobs.size());
-  // steady jobs first, then unsteady ones; order[k] = caller's index of job k
+  auto class_of = [](const batch_job_device& j) {
+    return j.rule.frozen ? batch_frozen : (j.time.nt > 1 ? batch_unsteady : batch_steady);
+  };
+  // jobs grouped by class; order[k] = caller's index of job k
   std::vector<int> order;
   order.reserve(count);
-  for (int j = 0; j < count; ++j) if (jobs[j].time.nt <= 1) order.push_back(j);
-  const int steady = int(order.size());
-  for (int j = 0; j < count; ++j) if (jobs[j].time.nt > 1) order.push_back(j);
+  int first[batch_classes], size[batch_classes];
+  for (int c = 0; c < batch_classes; ++c)
+  {
+    first[c] = int(order.size());
+    for (int j = 0; j < count; ++j) if (class_of(jobs[j]) == c) order.push_back(j);
+    size[c] = int(order.size()) - first[c];
+  }
   std::vector<batch_job_device> queue(count);
   for (int k = 0; k < count; ++k)
   {
     queue[k] = jobs[order[k]];
     queue[k].clock = make_slice_clock(queue[k].time, queue[k].time_begin, queue[k].rule.h);
   }
-  const int first[2] = {0, steady}, size[2] = {steady, count - steady};
-
+  constexpr int C = batch_classes;
   ctx.batch_jobs.reserve(sizeof(batch_job_device) * count);
-  ctx.batch_counters.reserve(sizeof(unsigned long long) * (count + 2));
+  ctx.batch_counters.reserve(sizeof(unsigned long long) * (count + C));
   auto* counters = ctx.batch_counters.as<unsigned long long>();
   auto* device_jobs = ctx.batch_jobs.as<batch_job_device>();
 
   // The device queues: each job's seeds in pools of batch_pool_seeds(), numbered
-  // per class; counters 0 and 1 hand out the pools of the two classes, counters
-  // 2.. count each job's steps.
-  long long pools[2] = {0, 0};
+  // per class; counters 0 .. C-1 hand out the pools of the classes, counters
+  // C.. count each job's steps.
+  long long pools[C] = {};
   auto upload = [&] {
     const int pool = batch_pool_seeds();
-    for (int c = 0; c < 2; ++c)
+    for (int c = 0; c < C; ++c)
     {
       pools[c] = 0;
       for (int k = first[c]; k < first[c] + size[c]; ++k)
       {
         queue[k].first_pool = pools[c];
-        queue[k].steps = counters + 2 + k;
+        queue[k].steps = counters + C + k;
         pools[c] += (queue[k].seed_count + pool - 1) / pool;
       }
     }
     PARS_CUDA(cudaMemcpyAsync(device_jobs, queue.data(), sizeof(batch_job_device) * count, cudaMemcpyHostToDevice, ctx.stream));
-    PARS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (count + 2), ctx.stream));
+    PARS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (count + C), ctx.stream));
   };
   auto launch = [&](int c, int v) {
     if (size[c] > 0) launch_batch_advect(ctx, c, v, device_jobs + first[c], size[c], pools[c], counters + c);
   };
 
-  for (int c = 0; c < 2; ++c)
+  for (int c = 0; c < C; ++c)
   {
     if (variant >= 0 || size[c] == 0 || ctx.batch_variant[c] >= 0) continue;
     std::vector<long long> full(count);
@@ -626,12 +633,12 @@ std::vector<unsigned long long> execute_batch(pars_gpu_context& ctx, std::vector
     for (int k = 0; k < count; ++k) queue[k].seed_count = full[k];
   }
   upload();
-  for (int c = 0; c < 2; ++c) launch(c, variant >= 0 ? variant : ctx.batch_variant[c]);
-  std::vector<unsigned long long> steps(count + 2);
-  PARS_CUDA(cudaMemcpyAsync(steps.data(), counters, sizeof(unsigned long long) * (count + 2), cudaMemcpyDeviceToHost, ctx.stream));
+  for (int c = 0; c < C; ++c) launch(c, variant >= 0 ? variant : ctx.batch_variant[c]);
+  std::vector<unsigned long long> steps(count + C);
+  PARS_CUDA(cudaMemcpyAsync(steps.data(), counters, sizeof(unsigned long long) * (count + C), cudaMemcpyDeviceToHost, ctx.stream));
   PARS_CUDA(cudaStreamSynchronize(ctx.stream));
   std::vector<unsigned long long> result(count);
-  for (int k = 0; k < count; ++k) result[order[k]] = steps[2 + k];
+  for (int k = 0; k < count; ++k) result[order[k]] = steps[C + k];
   return result;
 }
 
@@ -1162,9 +1169,12 @@ int32_t pars_gpu_flow_map_generate(pars_gpu_context* ctx, int32_t field, int32_t
       throw error(PARS_ERR_UNSUPPORTED, "unsteady flow maps integrate with RK4 or Euler");
     if (rule.frozen || iterations <= 1 || rule.scheme != scheme_classic)
     {
-      // The reference's scheme, bit for bit (and the iterations <= 1 case,
-      // where every voxel keeps its seed position); re-sampled stages of the
-      // general schemes also run here (one seed per thread).
+      // One seed per thread: the reference's scheme bit for bit (one field
+      // sample per step: at 64 registers this kernel keeps more warps
+      // resident than the batched engine's frozen class, 57 against 53 G
+      // steps/s on the 256^3 flow map), the iterations <= 1 case, where every
+      // voxel keeps its seed position, and the re-sampled stages of the
+      // general schemes.
       ctx->counters.reserve(sizeof(unsigned long long) * 2);
       auto* counter = ctx->counters.as<unsigned long long>();
       PARS_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
@@ -1179,7 +1189,7 @@ int32_t pars_gpu_flow_map_generate(pars_gpu_context* ctx, int32_t field, int32_t
     }
     else
     {
-      // Re-sampled stages: one job of the persistent batched engine.
+      // Re-sampled RK4 / Euler: one job of the persistent batched engine.
       std::vector<batch_job_device> job(1);
       batch_job_device& d = job[0];
       d.field = f.view();
@@ -1228,7 +1238,7 @@ int32_t pars_gpu_batch_variants(pars_gpu_context* ctx, int32_t* count)
 int32_t pars_gpu_batch_tuned(pars_gpu_context* ctx, int32_t job_class, int32_t* variant, int32_t* threads)
 {
   return guarded(ctx, [&] {
-    PARS_REQUIRE(job_class == 0 || job_class == 1, "job_class is 0 (steady) or 1 (unsteady)");
+    PARS_REQUIRE(job_class >= 0 && job_class < batch_classes, "job_class is 0 (steady), 1 (unsteady) or 2 (frozen)");
     const int v = ctx->batch_variant[job_class];
     if (variant) *variant = v;
     if (threads) *threads = v >= 0 ? batch_variant_threads(v) : 0;
@@ -1250,10 +1260,10 @@ int32_t pars_gpu_batch_advect(pars_gpu_context* ctx, pars_gpu_batch_job* jobs, i
       d.field = f.view();
       d.time = f.time();
       d.rule = make_rule(in.integrator, in.stage_mode, in.step_size);
-      if (d.rule.frozen)
-        throw error(PARS_ERR_UNSUPPORTED, "batched advection integrates with re-sampled stages (PARS_STAGES_RESAMPLED)");
-      if (d.rule.scheme != scheme_classic)
-        throw error(PARS_ERR_UNSUPPORTED, "batched advection integrates with RK4 or Euler");
+      if (d.rule.frozen && d.time.nt > 1)
+        throw error(PARS_ERR_UNSUPPORTED, "batched frozen-scheme jobs run on steady fields");
+      if (!d.rule.frozen && d.rule.scheme != scheme_classic)
+        throw error(PARS_ERR_UNSUPPORTED, "batched re-sampled advection integrates with RK4 or Euler");
       d.ux = d.uy = d.uz = 0;
       PARS_REQUIRE(in.max_steps >= 0, "max_steps must be >= 0");
       d.max_steps = in.max_steps;

@@ -345,13 +345,14 @@ void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std:
     jobs.push_back(j);
   }
   clock.mark("ftle.setup");
-  // RK4 / Euler requests: the persistent batched engine; the other
-  // integrators' re-sampled schemes: the per-seed flow-map kernel, one launch each
+  // RK4 / Euler requests and the reference's frozen scheme: the persistent
+  // batched engine; the other integrators' re-sampled schemes: the per-seed
+  // flow-map kernel, one launch each
   std::vector<batch_job_device> classic;
   std::vector<std::size_t> classic_of, general_of;
   for (std::size_t k = 0; k < jobs.size(); ++k)
   {
-    if (jobs[k].rule.scheme == scheme_classic) { classic.push_back(jobs[k]); classic_of.push_back(k); }
+    if (jobs[k].rule.frozen || jobs[k].rule.scheme == scheme_classic) { classic.push_back(jobs[k]); classic_of.push_back(k); }
     else general_of.push_back(k);
   }
   std::vector<unsigned long long> steps(jobs.size(), 0);
@@ -984,8 +985,6 @@ int32_t pars_gpu_service_submit(pars_gpu_service* svc, const uint8_t* message, i
     r->kind = mode.find("ftle") != std::string::npos ? ftle : streamlines;
     if (mode.find("fractional_anisotropy") != std::string::npos) r->ftle_mode = PARS_FTLE_FRACTIONAL_ANISOTROPY;
     r->stage_mode = mode.find("reference") != std::string::npos ? PARS_STAGES_FROZEN : PARS_STAGES_RESAMPLED;
-    if (r->kind == ftle && r->stage_mode == PARS_STAGES_FROZEN)
-      throw error(PARS_ERR_UNSUPPORTED, "served FTLE integrates with re-sampled stages");
     const bool with_volume = mode.find("volume") != std::string::npos;
     if (r->kind == streamlines)
     {

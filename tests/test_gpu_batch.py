@@ -140,3 +140,55 @@ def test_resampled_flow_map_equals_explicit_seed_job(ctx, port):
     assert np.array_equal(ed.cpu().numpy()[:, :3].reshape(flow.shape), flow)
     ctx.release_field(fm)
     ctx.release_field(h)
+
+
+def test_frozen_jobs_match_the_oracle_bit_for_bit_in_a_mixed_batch(ctx, port):
+    """Frozen-scheme jobs (the reference's arithmetic; a weighted-sum, a
+    tableau and the two-step Adams-Bashforth scheme with its per-particle
+    history) run as their own job class next to a re-sampled job: each frozen
+    job's end points equal the oracle's frozen flow map (reference semantics)
+    bit for bit, and the re-sampled job equals itself run alone."""
+    from pars_gb300 import native, workloads as W
+    torch = _torch_buffers()
+    f = W.abc_field(24, noise_sigma=0.01, seed=5)
+    h = ctx.upload_field(f)
+    # the seed lattice of flow_map_generator at scale 1 (seed_generator.cpp:11)
+    counts = [int(np.float32(f.size[i]) / np.float32(f.spacing[i])) for i in range(3)]
+    n = int(np.prod(counts))
+    max_steps, step = 120, 0.02
+
+    def lattice_job(integrator, stage_mode):
+        j = native.BatchJob()
+        j.field = h
+        j.integrator = integrator
+        j.stage_mode = stage_mode
+        j.max_steps = max_steps
+        j.step_size = step
+        j.seeds = None
+        for i in range(3):
+            j.lattice_offset[i] = float(f.offset[i])
+            j.lattice_stride[i] = float(f.spacing[i])
+            j.lattice_count[i] = counts[i]
+        out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+        j.end_positions = out.data_ptr()
+        j.end_steps = None
+        return j, out
+
+    frozen = [native.RUNGE_KUTTA_4, native.INTEGRATORS["runge_kutta_dormand_prince_5"], native.INTEGRATORS["adams_bashforth_2"]]
+    jobs, outs = [], []
+    for k in frozen:
+        j, o = lattice_job(k, native.STAGES_FROZEN)
+        jobs.append(j); outs.append(o)
+    rj, ro = lattice_job(native.RUNGE_KUTTA_4, native.STAGES_RESAMPLED)
+    steps = ctx.batch_advect(jobs + [rj])
+    for k, o, s in zip(frozen, outs, steps):
+        flow, ref_steps = port.flow_map(f, max_steps + 1, 1.0, k, step)
+        assert s == ref_steps
+        expected = flow[:counts[0], :counts[1], :counts[2]].reshape(-1, 3)
+        assert np.array_equal(o.cpu().numpy()[:, :3], expected), k
+    alone_j, alone_o = lattice_job(native.RUNGE_KUTTA_4, native.STAGES_RESAMPLED)
+    alone_steps = ctx.batch_advect([alone_j])
+    assert alone_steps[0] == steps[-1]
+    assert torch.equal(alone_o, ro)
+    assert ctx.batch_tuned(2)[0] >= 0
+    ctx.release_field(h)

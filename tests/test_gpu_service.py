@@ -97,10 +97,11 @@ def test_reference_mode_streamlines_match_the_oracle(service, port):
         assert_colors_equal(c, e["colors"])
 
 
-@pytest.mark.parametrize("mode,ftle_mode", [("ftle", 0), ("ftle_fractional_anisotropy", 1)])
-def test_ftle_request_equals_the_context_path(service, ctx, mode, ftle_mode):
+@pytest.mark.parametrize("mode,ftle_mode,stages", [("ftle", 0, 1), ("ftle_fractional_anisotropy", 1, 1), ("ftle_reference", 0, 0)])
+def test_ftle_request_equals_the_context_path(service, ctx, mode, ftle_mode, stages):
     """A mode containing "fractional_anisotropy" asks for the anisotropy map
-    (ftle_map_generator.cpp:51-54) instead of the FTLE."""
+    (ftle_map_generator.cpp:51-54) instead of the FTLE; one containing
+    "reference" integrates with the reference's frozen scheme."""
     from pars_gb300 import native, workloads as W
     from pars_gb300.requests import encode_settings
     f = W.abc_field(40, noise_sigma=0.01, seed=4)
@@ -113,7 +114,7 @@ def test_ftle_request_equals_the_context_path(service, ctx, mode, ftle_mode):
     steps = service.info(t).steps
     service.release(t)
     h = ctx.upload_field(f)
-    fm, s = ctx.flow_map_generate(h, 151, 1.0, native.RUNGE_KUTTA_4, native.STAGES_RESAMPLED, 0.01)
+    fm, s = ctx.flow_map_generate(h, 151, 1.0, native.RUNGE_KUTTA_4, stages, 0.01)
     expected = ctx.ftle_generate(fm, np.float32(0.01) * 151, ftle_mode, shape=tuple(f.dims))
     assert steps == s
     assert np.array_equal(got, expected)
