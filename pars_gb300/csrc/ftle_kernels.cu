@@ -6,6 +6,9 @@
 //   (particle_advector.cpp:74-139, one block: a particle stops with its current
 //   position when it leaves the grid, meets a zero velocity, or has taken
 //   iterations - 1 steps) and written to its voxel (flow_map_generator.cpp:44-52).
+//   Frozen stages keep absolute positions and the reference's arithmetic;
+//   re-sampled stages of the tableau and Adams schemes run in local cell
+//   coordinates.
 // FTLE: per voxel, the flow map's central-difference gradient J (FP32, one-sided
 //   at the borders), the Cauchy-Green tensor C = J^T J (FP32) and its
 //   eigenvalues by four sweeps of the cyclic Jacobi method (FP32 rotations;
@@ -16,6 +19,8 @@
 //   ftle_map_generator::generate (vector_field.cpp:49-93,
 //   ftle_map_generator.cpp:22-60).  All FP32: a GB300 SM issues FP64 at 1/64
 //   of its FP32 rate, and FP64 evaluation made this kernel FP64-pipe bound.
+//   The fractional-anisotropy mode (ftle_map_generator.cpp:51-54) needs no
+//   eigen-solve: it is evaluated from the invariants of C.
 #include "context.hpp"
 
 namespace pars
