@@ -424,16 +424,23 @@ int32_t pars_gpu_service_profile_get   (pars_gpu_service* service, const char* n
  * library until the process exits).
  *
  * Computes what pars_gpu_field_upload_device + pars_gpu_flow_map_generate
- * (resolution scale 1) + pars_gpu_ftle_generate compute, on the CURRENT CUDA
+ * (resolution scale 1) + pars_gpu_ftle_generate compute (bit for bit with
+ * frozen stages; to rounding with re-sampled RK4 / Euler, which the context
+ * path runs through its batched engine), on the CURRENT CUDA
  * device and `stream` (a cudaStream_t, NULL = default stream): device_xyz is
  * the field in DEVICE memory ([shape0][shape1][shape2][3] FP32), device_ftle
  * receives shape0*shape1*shape2 FP32 values in DEVICE memory, and
  * device_steps (DEVICE int64, may be NULL) the particle-steps taken.
- * Limit: shape0*shape1*shape2 <= 262144 (64^3); larger fields return
- * PARS_ERR_BUDGET.  size / spacing must give at least shape seeds per axis.
+ * Limit: shape0*shape1*shape2 <= 262144 (64^3); larger fields (or any
+ * shape entry above that) return PARS_ERR_BUDGET before any CUDA call.
+ * int(size / spacing) must lie between shape and shape + 1 per axis (one
+ * seed per vertex), else PARS_ERR_INVALID_ARGUMENT.
  * The first call on a device looks up the array's device address (once per
  * device, with that device current); make that first call before any stream
- * capture.  All calls share the one array: calls that overlap on the GPU
+ * capture.  The address is cached per device ordinal for the process's
+ * lifetime: only the device's primary context (the CUDA runtime's) is
+ * supported, and after cudaDeviceReset the process must restart before it
+ * calls this again.  All calls share the one array: calls that overlap on the GPU
  * (different streams or threads without ordering between them) race and
  * corrupt each other's results; order them on one stream. */
 int32_t pars_gpu_ftle_no_alloc(const float* device_xyz, const int32_t shape[3], const float offset[3], const float size[3],
@@ -532,6 +539,16 @@ int32_t pars_gpu_profile_reset (pars_gpu_context* context);
 int32_t pars_gpu_profile_get   (pars_gpu_context* context, const char* name, double* milliseconds, int64_t* launches);
 /* Kernel launches issued by this library on the context since creation. */
 int32_t pars_gpu_launch_count  (pars_gpu_context* context, int64_t* launches);
+/* Gather-bandwidth calibration (no counterpart in the reference; the measured
+ * ceilings for the advection kernels' roofline).  Times 16-byte non-coherent
+ * loads, the instruction the kernels use for cell corners, into a zeroed
+ * device buffer of buffer_bytes (rounded down to a power of two, 4 KiB to
+ * 64 GiB) on the context's stream.  pattern 0: each warp request reads 512
+ * contiguous bytes at a random aligned offset; 1: each lane 16 bytes at its
+ * own random offset; 2: each lane the eight corners of a random cell of a
+ * cube float4 field.  *bytes_per_second receives the bytes delivered to
+ * registers per second.  32 KiB stays in L1, 64 MiB in L2. */
+int32_t pars_gpu_gather_peak   (pars_gpu_context* context, int64_t buffer_bytes, int32_t pattern, double* bytes_per_second);
 
 #ifdef __cplusplus
 }

@@ -241,12 +241,16 @@ void launch_ftle(pars_gpu_context& ctx, const field_view& flow, double time, int
 }
 
 // ---- Allocation-free FTLE ------------------------------------------------------
-// pars_gpu_ftle_no_alloc (declared in pars_gpu.h) runs the same pack, flow-map
-// and FTLE kernels as the context path, but keeps its scratch — the float4
-// copy of the field, the flow map, and the step counter — in the one
-// file-scope device array below instead of allocating it.  Every GPU that
-// loads this library holds the array (no_alloc_max_voxels * 32 bytes + 256,
-// 8 MiB) until the process exits.
+// pars_gpu_ftle_no_alloc (declared in pars_gpu.h) runs the pack kernel, the
+// per-seed flow-map kernel (flow_map_kernel, frozen or re-sampled stages) and
+// the FTLE kernel, and keeps its scratch — the float4 copy of the field, the
+// flow map, and the step counter — in the one file-scope device array below
+// instead of allocating it.  The context path runs re-sampled RK4 / Euler
+// flow maps through the batched engine instead, so for those the two paths
+// agree to rounding (the engine's per-step arithmetic differs), not bit for
+// bit; frozen stages and the other schemes use the same kernel in both.
+// Every GPU that loads this library holds the array (no_alloc_max_voxels * 32
+// bytes + 256, 8 MiB) until the process exits.
 namespace
 {
 constexpr long long no_alloc_max_voxels = 1LL << 18;   // 64^3
@@ -285,6 +289,32 @@ int32_t no_alloc_scratch_address(int device, float4** out)
   return PARS_OK;
 }
 }
+
+// Checks the geometry of an allocation-free call before anything is
+// multiplied or launched: every shape entry within the static scratch on its
+// own (so the voxel product cannot overflow), the product within it, and the
+// seed lattice int(size / spacing) per axis between shape and shape + 1 (the
+// lattice flow_map_generator builds over a block: one seed per vertex), so
+// the seed count and the launch's grid stay small.  Host-only; no CUDA call.
+static int32_t no_alloc_geometry(const int32_t shape[3], const float size[3], const float spacing[3], long long* voxels,
+                          int seeds[3])
+{
+  for (int i = 0; i < 3; ++i)
+  {
+    if (shape[i] < 2 || !(spacing[i] > 0.0f)) return PARS_ERR_INVALID_ARGUMENT;
+    if (shape[i] > no_alloc_max_voxels) return PARS_ERR_BUDGET;
+  }
+  const long long v = (long long)shape[0] * shape[1] * shape[2];   // each factor <= 2^18: no overflow
+  if (v > no_alloc_max_voxels) return PARS_ERR_BUDGET;
+  for (int i = 0; i < 3; ++i)
+  {
+    const float q = size[i] / spacing[i];
+    seeds[i] = (q > 0.0f && q < 2147483647.0f) ? int(q) : 0;
+    if (seeds[i] < shape[i] || seeds[i] > shape[i] + 1) return PARS_ERR_INVALID_ARGUMENT;
+  }
+  *voxels = v;
+  return PARS_OK;
+}
 }
 
 #pragma GCC visibility push(default)
@@ -295,25 +325,18 @@ extern "C" int32_t pars_gpu_ftle_no_alloc(const float* device_xyz, const int32_t
 {
   using namespace pars;
   if (!device_xyz || !shape || !offset || !size || !spacing || !device_ftle) return PARS_ERR_INVALID_ARGUMENT;
-  for (int i = 0; i < 3; ++i)
-    if (shape[i] < 2 || !(spacing[i] > 0.0f)) return PARS_ERR_INVALID_ARGUMENT;
   if (mode != PARS_FTLE_REGULAR && mode != PARS_FTLE_FRACTIONAL_ANISOTROPY) return PARS_ERR_INVALID_ARGUMENT;
   if (time == 0.0f) return PARS_ERR_INVALID_ARGUMENT;
-  const long long voxels = (long long)shape[0] * shape[1] * shape[2];
-  if (voxels > no_alloc_max_voxels) return PARS_ERR_BUDGET;   // larger than the static scratch
-  step_rule rule;
-  try { rule = make_step_rule(integrator, stage_mode, step_size); }
-  catch (const error& e) { return e.status; }
   // Flow map at the field's own resolution (resolution scale 1): one seed per
   // vertex (seed_generator.cpp:11), so every flow-map voxel is written and the
   // flow-map part of the scratch needs no clearing.
+  long long voxels = 0;
   int seeds[3];
-  for (int i = 0; i < 3; ++i)
-  {
-    const float q = size[i] / spacing[i];
-    seeds[i] = (q > 0.0f && q < 2147483647.0f) ? int(q) : 0;
-    if (seeds[i] < shape[i]) return PARS_ERR_INVALID_ARGUMENT;
-  }
+  const int32_t geometry = no_alloc_geometry(shape, size, spacing, &voxels, seeds);
+  if (geometry != PARS_OK) return geometry;   // PARS_ERR_BUDGET: larger than the static scratch
+  step_rule rule;
+  try { rule = make_step_rule(integrator, stage_mode, step_size); }
+  catch (const error& e) { return e.status; }
 
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess) { (void)cudaGetLastError(); return PARS_ERR_CUDA; }
@@ -336,6 +359,7 @@ extern "C" int32_t pars_gpu_ftle_no_alloc(const float* device_xyz, const int32_t
   // The counter keeps the previous call's value: clear it first.
   if (cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s) != cudaSuccess) { (void)cudaGetLastError(); return PARS_ERR_CUDA; }
   pack_into_scratch_kernel<<<(unsigned)((voxels + 255) / 256), 256, 0, s>>>(device_xyz, field_data, voxels);
+  if (cudaGetLastError() != cudaSuccess) return PARS_ERR_CUDA;
 
   flow_map_args a;
   a.f = f; a.rule = rule; a.iterations = iterations;
@@ -347,6 +371,7 @@ extern "C" int32_t pars_gpu_ftle_no_alloc(const float* device_xyz, const int32_t
   const long long total = (long long)a.px * a.py * a.pz;
   if (rule.frozen) flow_map_kernel<true><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(a);
   else             flow_map_kernel<false><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(a);
+  if (cudaGetLastError() != cudaSuccess) return PARS_ERR_CUDA;
 
   ftle_args t;
   t.flow = flow; t.nx = shape[0]; t.ny = shape[1]; t.nz = shape[2];
@@ -355,6 +380,7 @@ extern "C" int32_t pars_gpu_ftle_no_alloc(const float* device_xyz, const int32_t
   t.mode = mode;
   t.out = device_ftle;
   launch_ftle_kernel(t, (unsigned)((voxels + 255) / 256), s);
+  if (cudaGetLastError() != cudaSuccess) return PARS_ERR_CUDA;
   if (device_steps) steps_to_int64_kernel<<<1, 1, 0, s>>>(counter, device_steps);
   if (cudaGetLastError() != cudaSuccess) return PARS_ERR_CUDA;
   return PARS_OK;

@@ -1158,6 +1158,10 @@ int32_t pars_gpu_flow_map_generate(pars_gpu_context* ctx, int32_t field, int32_t
       const float q = f.size[i] / entry->spacing[i];                     // seed_generator.cpp:11
       seeds[i] = (q > 0.0f && q < 2147483647.0f) ? int(q) : 0;
       PARS_REQUIRE(entry->shape[i] >= 1, "flow map would be empty");
+      // The seed lattice covers the flow map's voxels (one seed per vertex,
+      // plus at most one that rounding of size / spacing can add); a larger
+      // lattice would write nothing more and would overflow the seed count.
+      PARS_REQUIRE(seeds[i] <= entry->shape[i] + 1, "size / spacing gives more seeds than the flow map has voxels");
     }
     const long long voxels = (long long)entry->shape[0] * entry->shape[1] * entry->shape[2];
     entry->data = acquire_buffer(*ctx, sizeof(float4) * voxels);

@@ -80,3 +80,35 @@ def test_cpp_drop_in_header_compiles_and_links(tmp_path):
                     os.path.join(ROOT, "tests", "cpp", "drop_in_pipeline.cpp"), "-L" + lib_dir, "-lpars_gpu",
                     "-Wl,-rpath," + lib_dir, "-o", exe], check=True)
     assert os.path.exists(exe)
+
+
+# Shapes whose voxel or seed counts overflow 64-bit or 32-bit arithmetic, or
+# that exceed the static scratch of the allocation-free entry point: each is
+# rejected by the host-side geometry check before any CUDA call, so this runs
+# without a GPU.  (The pointers are host buffers that a rejected call never
+# touches.)
+NO_ALLOC_BAD_GEOMETRY = [
+    # (shape, size, spacing, expected status)
+    ((1 << 21, 1 << 21, 3 << 20), (float(1 << 21), float(1 << 21), float(3 << 20)), (1.0, 1.0, 1.0), -6),
+    (((1 << 21) + 1, (1 << 21) + 1, (1 << 22) + 1), (float(1 << 21), float(1 << 21), float(1 << 22)), (1.0, 1.0, 1.0), -6),
+    ((2, 2, (1 << 18) + 1), (2.0, 2.0, float((1 << 18) + 1)), (1.0, 1.0, 1.0), -6),
+    ((65, 65, 65), (65.0, 65.0, 65.0), (1.0, 1.0, 1.0), -6),
+    ((16, 16, 16), (1e9, 16.0, 16.0), (1.0, 1.0, 1.0), -1),      # seed lattice far beyond the shape
+    ((16, 16, 16), (4e9, 4e9, 4e9), (1.0, 1.0, 1.0), -1),        # int(size / spacing) beyond int32
+    ((16, 16, 16), (8.0, 16.0, 16.0), (1.0, 1.0, 1.0), -1),      # fewer seeds than vertices
+    ((1, 16, 16), (1.0, 16.0, 16.0), (1.0, 1.0, 1.0), -1),
+]
+
+
+@pytest.mark.parametrize("shape,size,spacing,status", NO_ALLOC_BAD_GEOMETRY)
+def test_no_alloc_rejects_bad_geometry_before_any_cuda_call(shape, size, spacing, status):
+    from pars_gb300 import native
+    lib = native.library()
+    dummy = np.zeros(16, np.float32)
+    shape = np.array(shape, np.int32)
+    offset = np.zeros(3, np.float32)
+    size = np.array(size, np.float32)
+    spacing = np.array(spacing, np.float32)
+    got = lib.pars_gpu_ftle_no_alloc(dummy.ctypes.data, shape.ctypes.data, offset.ctypes.data, size.ctypes.data,
+                                     spacing.ctypes.data, 11, 2, 1, 0.01, 0.1, 0, dummy.ctypes.data, None, None)
+    assert got == status

@@ -8,7 +8,9 @@ left in the shared static scratch by the first call would show up in the
 second), and checks each result against the context-based entry points
 (pars_gpu_field_upload_device + pars_gpu_flow_map_generate +
 pars_gpu_ftle_generate): FTLE within the relative 1e-4 used by the other FTLE
-tests (expected bit-identical: same kernels) and the same step count.  The
+tests and the same step count.  (Frozen stages run the same flow-map kernel
+on both paths; re-sampled RK4 runs the batched engine on the context path, so
+there the two agree to rounding, not bit for bit.)  The
 caller's input and output buffers are allocated by the caller (torch here),
 as the entry point expects.  The file is collected last on purpose.
 """
@@ -76,3 +78,26 @@ def test_no_alloc_rejects_fields_beyond_its_static_scratch():
     status = _call(lib, field_dev, field, out_dev, None, torch.cuda.current_stream().cuda_stream, 11, 0.01, 0.1,
                    native.STAGES_RESAMPLED)
     assert status == -6   # PARS_ERR_BUDGET
+
+
+def test_no_alloc_rejects_overflowing_geometry_on_a_device():
+    """Shapes whose voxel or seed products overflow, or that exceed the static
+    scratch, return their status before any launch, with a device current."""
+    import torch
+    from test_cabi import NO_ALLOC_BAD_GEOMETRY
+    from pars_gb300 import native
+
+    lib = native.library()
+    torch.cuda.set_device(0)
+    dev = torch.zeros(16, dtype=torch.float32, device="cuda")
+    for shape, size, spacing, status in NO_ALLOC_BAD_GEOMETRY:
+        shape = np.array(shape, np.int32)
+        offset = np.zeros(3, np.float32)
+        size = np.array(size, np.float32)
+        spacing = np.array(spacing, np.float32)
+        got = lib.pars_gpu_ftle_no_alloc(dev.data_ptr(), shape.ctypes.data, offset.ctypes.data, size.ctypes.data,
+                                         spacing.ctypes.data, 11, 2, 1, 0.01, 0.1, 0, dev.data_ptr(), None,
+                                         torch.cuda.current_stream().cuda_stream)
+        assert got == status, (shape, got)
+    torch.cuda.synchronize()
+    assert torch.isfinite(dev).all() and (dev == 0).all()
