@@ -45,12 +45,18 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--size", type=int, default=256)
     p.add_argument("--iterations", type=int, default=501)
-    p.add_argument("--cpu-sample", type=int, default=1048576, help="seeds in the CPU baseline's bounded sample")
+    p.add_argument("--cpu-stride", type=int, default=16,
+                   help="CPU baseline's bounded sample: every cpu-stride-th seed of the C-order seed list")
+    p.add_argument("--no-extra", action="store_true", help="headline workload only (skip the other workloads' lines)")
+    p.add_argument("--dry-run", action="store_true",
+                   help="check the multi-process launcher only: each rank reports on the CPU (gloo), no workload runs")
     p.add_argument("--requests", type=int, default=300, help="served workload: number of requests")
     p.add_argument("--serve-arms", default="plain,batched,cpu", help="served workload: arms to run (plain, batched, cpu)")
     p.add_argument("--serve-cpu-seconds", type=float, default=15.0, help="served workload: CPU reference arm's sample length")
     p.add_argument("--serve-loads", default="0.5,0.9", help="served workload: offered loads as fractions of saturation")
     p.add_argument("--serve-lanes", type=int, default=1, help="served workload: service lanes of the batched arm")
+    p.add_argument("--domain-edge", type=int, default=512, help="domain workload: edge of the cube domain")
+    p.add_argument("--domain-seeds", type=int, default=1_000_000, help="domain workload: seeds of the Gaussian mixture")
     p.add_argument("--workload", choices=["ftle", "streamlines", "domain", "pathlines", "serve", "render"], default="ftle",
                    help="ftle: the headline line; the others print one line for the other workloads")
     return p.parse_args()
@@ -151,20 +157,28 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def cpu_reference_run(field, iterations, sample, steps, warmup):
+def cpu_reference_run(field, iterations, stride, steps, warmup):
     """The reference's algorithm on the host cores: the oracle port's flow map
-    (frozen-velocity RK4, FP32, the reference's operation order), all threads."""
+    (frozen-velocity RK4, FP32, the reference's operation order), all threads,
+    on every stride-th seed of the C-order seed list (a uniform sample of the
+    whole domain)."""
     import oracle
     port = oracle.port()
     threads = port.max_threads()
     for _ in range(warmup):
-        port.flow_map(field, iterations, 1.0, 2, 0.01, 0, sample)
+        port.flow_map(field, iterations, 1.0, 2, 0.01, 0, None, stride)
     total, t0 = 0, time.perf_counter()
     for _ in range(steps):
-        _, s = port.flow_map(field, iterations, 1.0, 2, 0.01, 0, sample)
+        _, s = port.flow_map(field, iterations, 1.0, 2, 0.01, 0, None, stride)
         total += s
     dt = time.perf_counter() - t0
     return total / dt, threads, dt
+
+
+def cpu_sample_text(seeds, stride, n):
+    count = (seeds + stride - 1) // stride
+    return (f"every {stride}th of the {seeds} seeds in C order ({count} seeds spread over the whole {n}^3 domain) per step, "
+            "frozen-velocity RK4 as the reference computes it (one field sample per step), FP32, all host threads")
 
 
 def _events_time(torch, stream, fn):
@@ -308,7 +322,7 @@ def run_domain(args):
     2000 steps; particles handed between blocks each round on the device."""
     import torch
     from pars_gb300 import native, workloads
-    n = args.size if args.size != 256 else 512
+    n = args.domain_edge
     ctx = native.Context(0)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
@@ -318,7 +332,7 @@ def run_domain(args):
     del xyz
     torch.cuda.empty_cache()
     info = native.partition(ranks, 0, (n, n, n))
-    seeds, offsets = workloads.gaussian_mixture_seeds(1_000_000, n, spacing, info, remaining=2002, seed=2)
+    seeds, offsets = workloads.gaussian_mixture_seeds(args.domain_seeds, n, spacing, info, remaining=2002, seed=2)
     s, dt = None, 0.0
     for _ in range(max(args.warmup, 1)):
         ctx.trace_domain(d, seeds, offsets, native.RUNGE_KUTTA_4, native.STAGES_RESAMPLED, 0.005)
@@ -329,7 +343,7 @@ def run_domain(args):
         total += s["steps"]
         t += dt
     print(json.dumps({"workload": f"domain_{n}: {n}^3 Arnold-Beltrami + 8 Fourier modes, 64 blocks (4x4x4) on one GPU, "
-                                  "1M Gaussian-mixture seeds, RK4 h=0.005, <=2000 steps, device handoff queues",
+                                  f"{args.domain_seeds} Gaussian-mixture seeds, RK4 h=0.005, <=2000 steps, device handoff queues",
                       "metric": METRIC, "unit": UNIT, "value": total / t, "ms_per_step": 1e3 * t / args.steps,
                       "steps_per_run": s["steps"], "rounds": s["rounds"], "batches": s["batches"],
                       "vertices": s["vertices"]}))
@@ -664,8 +678,79 @@ def run_serve(args):
     print(json.dumps(line))
 
 
+def _free_port():
+    import socket
+    with socket.socket() as sock:
+        sock.bind(("127.0.0.1", 0))
+        return sock.getsockname()[1]
+
+
+def launch_replicas(args):
+    """--gpus N > 1 started as a plain process: runs N ranks, one process per
+    GPU, through torch.distributed.run on this node (rendezvous on
+    127.0.0.1), with the same arguments; rank 0 prints the line."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
+def launcher_check(args):
+    """--dry-run: every rank joins a gloo group on the CPU and reports its rank
+    through combine_ranks (rank r: r + 1 seconds, 1000 (r + 1) units), so the
+    launcher and the reduction are checked without a GPU or a workload."""
+    import torch.distributed as dist
+    rank, world, _ = dist_env()
+    dist.init_process_group("gloo")
+    elapsed, units = combine_ranks(dist, float(rank + 1), 1000 * (rank + 1), "cpu")
+    if rank == 0:
+        print(json.dumps({"launcher_check": True, "n_gpus": world, "requested_gpus": args.gpus,
+                          "max_rank_seconds": elapsed, "sum_units": units}))
+    dist.destroy_process_group()
+
+
+def gather_peaks(ctx):
+    """Measured gather ceilings of this GPU (GB/s of 16-byte loads delivered
+    to registers; best of three per case): L1-resident (32 KiB) and
+    L2-resident (64 MiB) buffers, coalesced 512-byte warp requests, one random
+    sector per lane, and eight-corner cell gathers."""
+    out = {}
+    for size, level in ((32 << 10, "l1"), (64 << 20, "l2")):
+        for pattern in ("coalesced", "random", "cells"):
+            out[f"{level}_{pattern}"] = max(ctx.gather_peak(size, pattern) for _ in range(3)) / 1e9
+    return out
+
+
+def extra_workloads(args):
+    """The other workloads, each in its own process (one JSON line each), for
+    the default single-GPU run: streamlines, the partitioned domain, batched
+    pathlines, the ray tracer and a reduced served stream."""
+    runs = {"streamlines": ["--workload", "streamlines", "--steps", "20", "--warmup", "3"],
+            "domain": ["--workload", "domain", "--steps", "3", "--warmup", "1"],
+            "pathlines": ["--workload", "pathlines", "--steps", "2", "--warmup", "1"],
+            "render": ["--workload", "render", "--steps", "5", "--warmup", "3"],
+            "serve": ["--workload", "serve", "--requests", "100", "--serve-loads", "0.5", "--serve-cpu-seconds", "5"]}
+    out = {}
+    for name, extra in runs.items():
+        t0 = time.perf_counter()
+        r = subprocess.run([sys.executable, os.path.abspath(__file__)] + extra, capture_output=True, text=True)
+        line = None
+        for text in reversed(r.stdout.strip().splitlines()):
+            if text.startswith("{"):
+                line = json.loads(text)
+                break
+        out[name] = line if (r.returncode == 0 and line) else {"error": (r.stderr or r.stdout)[-400:],
+                                                              "returncode": r.returncode}
+        out[name]["wall_s"] = time.perf_counter() - t0
+    return out
+
+
 def main():
     args = parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_replicas(args))
+    if args.dry_run:
+        launcher_check(args)
+        return
     if args.workload != "ftle":
         {"streamlines": run_streamlines, "domain": run_domain, "pathlines": run_pathlines, "serve": run_serve,
          "render": run_render}[args.workload](args)
@@ -680,16 +765,18 @@ def main():
                           f"({seeds} particles), classical RK4 (4 samples/step) h=0.01, <= {max_steps} steps (T=5), "
                           "flow map + fused central-difference / Cauchy-Green / FP32 Jacobi eigenvalue / log FTLE",
               "grid": n, "seeds": seeds, "max_steps": max_steps, "step_size": 0.01, "stage_mode": "resampled",
+              "field_samples_per_step": 4, "reference_field_samples_per_step": 1,
               "ranks": world, "l2": f"inputs larger than L2 ({16 * n ** 3 / 1e6:.0f} MB float4 field) and a 256 MB L2 flush "
-                                    "before every step"}
+                                    "before every step",
+              "tested_at_this_size": "tests/test_gpu_fullsize.py: flow map of 100k strided seeds within 1e-3 cells of FP64, "
+                                     "FTLE of an interior 48^3 window within 1e-4 of FP64"}
 
     if args.impl == "reference":
         if rank != 0:
             return
         field = workloads.abc_field(n, noise_sigma=0.01, seed=0)
-        value, threads, dt = cpu_reference_run(field, args.iterations, args.cpu_sample, args.steps, args.warmup)
-        sample = (f"first {args.cpu_sample} of {seeds} seeds (C order) of the {n}^3 FTLE workload per step, frozen-velocity "
-                  "RK4 (one sample per step) as the reference computes it, FP32, all host threads")
+        value, threads, dt = cpu_reference_run(field, args.iterations, args.cpu_stride, args.steps, args.warmup)
+        sample = cpu_sample_text(seeds, args.cpu_stride, n)
         print(json.dumps({"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
                           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
                           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -745,6 +832,8 @@ def main():
         total_steps += device_step()
     stop.record(stream)
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
     clocks = sampler.stop()
     launches = ctx.launch_count() - launches0
     ctx.profile_enable(False)
@@ -756,10 +845,12 @@ def main():
     value = total_steps_all / (elapsed_ms * 1e-3)
     ftle_voxels_per_s = world * seeds * args.steps / (elapsed_ms * 1e-3)
     steps_per_launch = total_steps / args.steps
-    peak, peak_kind = measured_peaks()
+    hbm_peak, hbm_kind = measured_peaks()
     advect_avg_s = advect_ms / max(advect_n, 1) * 1e-3
     achieved = steps_per_launch * BYTES_PER_RK4_STEP / advect_avg_s / 1e9
     ftle_avg_s = ftle_ms / max(ftle_n, 1) * 1e-3
+    traffic = committed_traffic(steps_per_launch)
+    peaks = gather_peaks(ctx)
 
     # The reference's scheme (frozen velocity, one sample per step) on the GPU.
     device_step(native.STAGES_FROZEN)
@@ -790,6 +881,8 @@ def main():
 
     e2e_step()
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
     e2e_steps, t0 = 0, time.perf_counter()
     for _ in range(args.steps):
         flush.zero_()
@@ -801,31 +894,45 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1:
-        cpu_value, threads, _ = cpu_reference_run(field, args.iterations, args.cpu_sample, 1, 0)
+        cpu_value, threads, _ = cpu_reference_run(field, args.iterations, args.cpu_stride, 1, 0)
         cpu = {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"first {args.cpu_sample} of {seeds} seeds (C order) of this workload, frozen-velocity RK4 "
-                         "(one sample per step) as the reference computes it, FP32, all host threads"}
+               "sample": cpu_sample_text(seeds, args.cpu_stride, n)}
 
     if rank == 0:
+        l1 = peaks["l1_coalesced"]
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": max(args.warmup, 3), "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
                 "ftle_voxels_per_s": ftle_voxels_per_s,
                 "frozen_velocity_steps_per_s": frozen_value,
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                             "traffic": committed_traffic(steps_per_launch), "kernel": "batch_advect",
+                "roofline": {"bound": "l1_gather", "achieved": achieved, "peak": l1, "unit": "GB/s", "frac": achieved / l1,
+                             "traffic": traffic, "kernel": "batch_advect",
                              "bytes_per_unit": BYTES_PER_RK4_STEP, "units_per_launch": steps_per_launch,
-                             "avg_launch_ms": advect_avg_s * 1e3, "peak_source": peak_kind,
+                             "avg_launch_ms": advect_avg_s * 1e3,
+                             "peak_source": "measured in this run on this GPU (pars_gpu_gather_peak): 16-byte "
+                                            "ld.global.nc loads, warp requests of 512 contiguous bytes in a 32 KiB "
+                                            "L1-resident buffer; the kernel's corner gathers are served by L1 "
+                                            "(ncu: L1 data-pipe wavefronts are its top unit)",
+                             "gather_peaks_gbs": peaks,
+                             "frac_of_l2_coalesced": achieved / peaks["l2_coalesced"],
+                             "hbm": {"peak_gbs": hbm_peak, "peak_source": hbm_kind,
+                                     "traffic_gbs": (traffic / advect_avg_s / 1e9) if traffic else None},
                              "ftle_kernel": {"avg_launch_ms": ftle_avg_s * 1e3,
                                              "achieved_gbs": seeds * BYTES_PER_FTLE_VOXEL / ftle_avg_s / 1e9}},
                 "cpu_baseline": cpu,
+                "same_scheme_ratio": (frozen_value / cpu["value"]) if cpu else None,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(field.xyz.nbytes),
                         "d2h_bytes_per_step": int(ftle_out.nbytes)},
                 "clocks": clocks, "gpu_launches": launches}
-        print(json.dumps(line))
     ctx.close()
+    del flush
+    torch.cuda.empty_cache()
     if dist:
         dist.destroy_process_group()
+    if rank == 0:
+        if world == 1 and not args.no_extra:
+            line["workloads"] = extra_workloads(args)
+        print(json.dumps(line))
 
 
 if __name__ == "__main__":

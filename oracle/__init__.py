@@ -175,7 +175,7 @@ class Port(_Lib):
         L.orc_max_threads.restype = _I
         L.orc_set_threads.argtypes = [_I]
         L.orc_flow_map.restype = _LL
-        L.orc_flow_map.argtypes = [_P] * 5 + [_I, _F, _I, _F, _LL, _LL, _P]
+        L.orc_flow_map.argtypes = [_P] * 5 + [_I, _F, _I, _F, _LL, _LL, _LL, _P]
         L.orc_advect_fp64.restype = None
         L.orc_advect_fp64.argtypes = [_P] * 5 + [_P, _LL, _I, _I, _D, _LL, _P, _P, _P, _D, ctypes.c_ulonglong]
         L.orc_ftle_fp64.restype = None
@@ -243,15 +243,17 @@ class Port(_Lib):
     def set_threads(self, n):
         self.lib.orc_set_threads(n)
 
-    def flow_map(self, field, iterations, scale=1.0, integrator=2, step=0.01, first=0, count=None):
-        """Frozen-velocity FP32 flow map (reference semantics).  Returns
+    def flow_map(self, field, iterations, scale=1.0, integrator=2, step=0.01, first=0, count=None, stride=1):
+        """Frozen-velocity FP32 flow map (reference semantics) of the seeds
+        first + k * stride, k < count (default: all from `first`).  Returns
         (flow [X',Y',Z',3] f32 with NaN where no particle landed, steps)."""
         fm = [int(np.float32(d) * np.float32(scale)) for d in field.dims]
         flow = np.full(fm + [3], np.nan, np.float32)
         total = int(np.prod(fm))
         if count is None:
-            count = total - first
-        steps = self.lib.orc_flow_map(*field.ctypes_args(), iterations, scale, integrator, step, first, count, _ptr(flow))
+            count = (total - first + stride - 1) // stride
+        steps = self.lib.orc_flow_map(*field.ctypes_args(), iterations, scale, integrator, step, first, count, stride,
+                                      _ptr(flow))
         return flow, steps
 
     def advect_fp64(self, field, start, max_steps, integrator=2, mode=1, step=0.01, keep_vertices=False, noise=0.0, seed=0):

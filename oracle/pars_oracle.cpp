@@ -977,10 +977,11 @@ void orc_color_generate(const float* vertices, long long n, const int* indices, 
 // the reference's rules (particle_advector.cpp:74-139, one block): a particle
 // stops with its current position when it leaves the grid, meets a zero
 // velocity, or completes iterations - 1 steps.  flow: [X'][Y'][Z'][3].
-// Particles [first, first+count) of the C-order seed list only (a bounded
-// sample); returns the steps taken.
+// Particles first + k * stride (k < count) of the C-order seed list only (a
+// bounded sample; stride 1: a contiguous range); returns the steps taken.
 long long orc_flow_map(const float* xyz, const int dims[3], const float offset[3], const float size[3], const float spacing[3],
-                       int iterations, float scale, int integrator, float step, long long first, long long count, float* flow)
+                       int iterations, float scale, int integrator, float step, long long first, long long count,
+                       long long stride, float* flow)
 {
   field f {xyz, {dims[0], dims[1], dims[2]}, {offset[0], offset[1], offset[2]}, {size[0], size[1], size[2]}, {spacing[0], spacing[1], spacing[2]}};
   const frozen_weights w = make_frozen_weights(integrator, step);
@@ -991,8 +992,9 @@ long long orc_flow_map(const float* xyz, const int dims[3], const float offset[3
   for (int i = 0; i < 3; ++i) per_dimension[i] = int(size[i] / fm_spacing[i]);
   long long steps = 0;
   #pragma omp parallel for schedule(dynamic, 64) reduction(+ : steps)
-  for (long long index = first; index < first + count; ++index)
+  for (long long k = 0; k < count; ++k)
   {
+    const long long index = first + k * stride;
     int idx[3];
     unravel(index, per_dimension, idx);
     float pos[4];

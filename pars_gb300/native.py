@@ -160,6 +160,7 @@ SIGNATURES = {
     "pars_gpu_profile_reset": [_P],
     "pars_gpu_profile_get": [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)],
     "pars_gpu_launch_count": [_P, ctypes.POINTER(_I64)],
+    "pars_gpu_gather_peak": [_P, _I64, _I32, ctypes.POINTER(ctypes.c_double)],
 }
 _RESTYPES = {"pars_gpu_last_error": ctypes.c_char_p}
 
@@ -515,6 +516,15 @@ class Context:
         n = _I64()
         self._call("pars_gpu_launch_count", ctypes.byref(n))
         return n.value
+
+    GATHER_PATTERNS = {"coalesced": 0, "random": 1, "cells": 2}
+
+    def gather_peak(self, buffer_bytes, pattern):
+        """Measured gather bandwidth (bytes/s) of 16-byte loads into a buffer
+        of buffer_bytes; pattern "coalesced", "random" or "cells"."""
+        out = ctypes.c_double()
+        self._call("pars_gpu_gather_peak", int(buffer_bytes), self.GATHER_PATTERNS[pattern], ctypes.byref(out))
+        return out.value
 
 
 # -- field files (pa::data_io) ----------------------------------------------------------

@@ -49,3 +49,22 @@ def test_single_process_passes_through():
     sys.path.insert(0, ROOT)
     import bench
     assert bench.combine_ranks(None, 2.5, 7, "cpu") == (2.5, 7.0)
+
+
+def test_bench_launches_one_process_per_gpu():
+    """`bench.py --gpus 2` started as a plain process launches two ranks
+    (torch.distributed.run on 127.0.0.1) and rank 0 prints one line with
+    n_gpus = 2.  --dry-run makes each rank report over gloo on the CPU instead
+    of running the workload."""
+    import json
+    import subprocess
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT")}
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "2", "--dry-run"], capture_output=True,
+                       text=True, timeout=180, env=env, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    line = lines[0]
+    assert line["launcher_check"] is True
+    assert line["n_gpus"] == 2 and line["requested_gpus"] == 2
+    assert line["max_rank_seconds"] == 2.0 and line["sum_units"] == 3000.0
