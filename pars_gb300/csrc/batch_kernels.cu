@@ -169,7 +169,7 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
           if (is_zero_local(f, k1)) retire = true;
           else { local_unsteady_step(f, ta, clock, cache.k, rk4, h, local, k1, t); ++steps; ++job_steps; }
         }
-        if (retire) pos = to_absolute(f, local, 0.0f);
+        if (retire) pos = flow_position(f, local);
       }
       else
       {
@@ -181,7 +181,7 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
           if (is_zero_local(f, k1)) retire = true;
           else { local_step(f, cache.k, rk4, h, local, k1); ++steps; ++job_steps; }
         }
-        if (retire) pos = to_absolute(f, local, 0.0f);
+        if (retire) pos = flow_position(f, local);
       }
       if (retire)
       {
@@ -222,7 +222,7 @@ struct variant
 const variant variants[batch_classes][4] = {
   {{64, 1, (const void*)batch_advect_kernel<64, 1, batch_steady>},
    {128, 1, (const void*)batch_advect_kernel<128, 1, batch_steady>},
-   {128, 6, (const void*)batch_advect_kernel<128, 6, batch_steady>},
+   {128, 5, (const void*)batch_advect_kernel<128, 5, batch_steady>},
    {256, 1, (const void*)batch_advect_kernel<256, 1, batch_steady>}},
   {{64, 1, (const void*)batch_advect_kernel<64, 1, batch_unsteady>},
    {128, 1, (const void*)batch_advect_kernel<128, 1, batch_unsteady>},

@@ -323,6 +323,33 @@ __device__ __forceinline__ void compensated_add(float& hi, float& lo, float delt
   hi = s;
 }
 
+// Knuth's error-free TwoSum: s = RN(a + b) and e = (a + b) - s exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+  s = a + b;
+  const float bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
+}
+
+// u (with its compensation term l) += h6 (k1 + 2 k2 + 2 k3 + k4): the RK4
+// weighted sum is formed with TwoSums and the product with its exact FMA
+// error, and both errors go into the compensation term, so the only rounding
+// left is that of the (tiny) compensation term itself.  A plain FP32 sum and
+// product lose about two ulps of the increment per step, which the flow's
+// stretching amplifies: on the 256^3 ABC workload this halves the largest
+// end-point errors against an FP64 integration.
+__device__ __forceinline__ void rk4_update(float& u, float& l, float h6, float k1, float k2, float k3, float k4)
+{
+  float a, ea, b, eb, t, et;
+  two_sum(k1, k4, a, ea);
+  two_sum(k2, k3, b, eb);
+  two_sum(a, 2.0f * b, t, et);
+  const float e = (ea + 2.0f * eb) + et;
+  const float p = h6 * t;
+  l += fmaf(h6, e, fmaf(h6, t, -p));
+  compensated_add(u, l, p);
+}
+
 // Butcher tableaux of the re-sampled general schemes (stage matrix a, weights
 // b), FP32 quotients of the published fractions.
 struct rk_tableau
@@ -557,6 +584,74 @@ __device__ __forceinline__ float4 to_absolute(const field_view& f, const local_p
                      fmaf(float(q.iz) + q.uz, f.hz, f.oz), w);
 }
 
+// ---- Flow-map positions with sub-ulp residuals ---------------------------------
+// An FTLE is a difference quotient of neighbouring flow-map positions, so the
+// FP32 rounding of the stored positions (half an ulp: about 1e-5 cells at
+// |x| ~ 6 on a 256^3 grid of [0, 2 pi]^3) bounds its accuracy where the FTLE is
+// small.  The re-sampled advection kernels therefore store each end position
+// as its correctly rounded FP32 coordinates plus, in the otherwise unused w
+// lane, the rounding residual of each coordinate as a signed 10-bit code:
+// coordinate = x + code / 1022 * ulp(x) (bits 0-9: x, 10-19: y, 20-29: z; the
+// top two bits are zero, so w reads as an ordinary float in [0, 2)).  That
+// carries each coordinate to about 34 bits.  Frozen-scheme flow maps, the
+// reference's FP32 state, store w = 0 (no residual).
+
+// ulp of a normal FP32 x with |x| >= 2^-103; 0 for smaller x (no residual).
+__device__ __forceinline__ float residual_ulp(float x)
+{
+  const unsigned e = __float_as_uint(x) & 0x7f800000u;
+  return e > (23u << 23) ? __uint_as_float(e - (23u << 23)) : 0.0f;
+}
+
+// 1 / ulp(x) for a normal x with |x| >= 2^-103 (a power of two, so scaling
+// by it is exact).
+__device__ __forceinline__ float residual_inverse_ulp(float x)
+{
+  const unsigned e = __float_as_uint(x) & 0x7f800000u;
+  return __uint_as_float((277u << 23) - e);
+}
+
+// The residual of x coded in w's bits [shift, shift + 10).
+__device__ __forceinline__ float residual_value(float x, unsigned w, int shift)
+{
+  const int q = int(w << (22 - shift)) >> 22;
+  return float(q) * (residual_ulp(x) * (1.0f / 1022.0f));
+}
+
+// One coordinate o + (i + u + l) h of a local position as its correctly
+// rounded FP32 value and residual code, in FP32 error-free arithmetic (the
+// FP64 pipe of a GB300 SM runs at 1/64 of the FP32 rate, and a retiring lane
+// would run it for its whole warp): TwoSum for i + u, the exact FMA error of
+// the product with h, TwoSum for the addition of o.
+__device__ __forceinline__ float coordinate_with_residual(int i, float u, float l, float h, float o, unsigned& code)
+{
+  float s, e1;
+  two_sum(float(i), u, s, e1);
+  const float p = s * h;
+  const float lo1 = fmaf(e1 + l, h, fmaf(s, h, -p));
+  float t, e2;
+  two_sum(o, p, t, e2);
+  const float lo = lo1 + e2;
+  const float x = t + lo;                       // RN(t + lo): the correctly rounded coordinate
+  const float r = (t - x) + lo;                 // what the rounding dropped
+  const unsigned exponent = __float_as_uint(x) & 0x7f800000u;
+  if (exponent <= (23u << 23)) { code = 0u; return x; }
+  const int q = __float2int_rn(r * residual_inverse_ulp(x) * 1022.0f);
+  code = unsigned(max(-511, min(511, q))) & 0x3ffu;
+  return x;
+}
+
+// The end position of a particle carried in local coordinates, with the
+// residual codes in w.
+__device__ __forceinline__ float4 flow_position(const field_view& f, const local_position& q)
+{
+  unsigned cx, cy, cz;
+  const float x = coordinate_with_residual(q.ix, q.ux, q.lx, f.hx, f.ox, cx);
+  const float y = coordinate_with_residual(q.iy, q.uy, q.ly, f.hy, f.oy, cy);
+  const float z = coordinate_with_residual(q.iz, q.uz, q.lz, f.hz, f.oz, cz);
+  return make_float4(x, y, z, __uint_as_float(cx | (cy << 10) | (cz << 20)));
+}
+
 __device__ __forceinline__ bool local_inside(const field_view& f, const local_position& q)
 {
   // 0 <= i < n - 1 as one unsigned compare per axis (false for every i when n = 1)
@@ -585,9 +680,9 @@ __device__ __forceinline__ void local_step(const field_view& f, corner_cache& k,
   const float3 k3 = sample_local(f, k, q.ix, q.iy, q.iz, fmaf(hh, k2.x, q.ux), fmaf(hh, k2.y, q.uy), fmaf(hh, k2.z, q.uz));
   const float3 k4 = sample_local(f, k, q.ix, q.iy, q.iz, fmaf(h, k3.x, q.ux), fmaf(h, k3.y, q.uy), fmaf(h, k3.z, q.uz));
   const float h6 = h * (1.0f / 6.0f);
-  compensated_add(q.ux, q.lx, h6 * (k1.x + 2.0f * (k2.x + k3.x) + k4.x));
-  compensated_add(q.uy, q.ly, h6 * (k1.y + 2.0f * (k2.y + k3.y) + k4.y));
-  compensated_add(q.uz, q.lz, h6 * (k1.z + 2.0f * (k2.z + k3.z) + k4.z));
+  rk4_update(q.ux, q.lx, h6, k1.x, k2.x, k3.x, k4.x);
+  rk4_update(q.uy, q.ly, h6, k1.y, k2.y, k3.y, k4.y);
+  rk4_update(q.uz, q.lz, h6, k1.z, k2.z, k3.z, k4.z);
   renormalize(q);
 }
 

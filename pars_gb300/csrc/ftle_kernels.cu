@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(256) flow_map_kernel(const __grid_constant__ f
         general_step_local(a.f, cache, a.rule, q, v, hist);
         ++steps;
       }
-      if (steps) pos = to_absolute(a.f, q, 0.0f);
+      if (steps) pos = flow_position(a.f, q);
     }
     // With iterations <= 1 the reference never assigns the voxel; it keeps the
     // seed position here.
@@ -162,10 +162,15 @@ __global__ void __launch_bounds__(256) ftle_kernel(const ftle_args a)
     if (idx[j] == 0)                 { hi = i + stride[j]; denominator = h[j]; }
     else if (idx[j] == ext[j] - 1)   { lo = i - stride[j]; denominator = h[j]; }
     else                             { lo = i - stride[j]; hi = i + stride[j]; denominator = 2.0f * h[j]; }
+    // positions with their sub-ulp residuals (w = 0: none); the FP32
+    // difference of neighbouring coordinates is exact where they lie within a
+    // factor of two of each other (Sterbenz), the residuals' difference is
+    // added to it
     const float4 A = __ldg(a.flow + lo), B = __ldg(a.flow + hi);
-    J[0][j] = __fdiv_rn(__fsub_rn(B.x, A.x), denominator);
-    J[1][j] = __fdiv_rn(__fsub_rn(B.y, A.y), denominator);
-    J[2][j] = __fdiv_rn(__fsub_rn(B.z, A.z), denominator);
+    const unsigned wa = __float_as_uint(A.w), wb = __float_as_uint(B.w);
+    J[0][j] = __fdiv_rn(__fsub_rn(B.x, A.x) + (residual_value(B.x, wb, 0) - residual_value(A.x, wa, 0)), denominator);
+    J[1][j] = __fdiv_rn(__fsub_rn(B.y, A.y) + (residual_value(B.y, wb, 10) - residual_value(A.y, wa, 10)), denominator);
+    J[2][j] = __fdiv_rn(__fsub_rn(B.z, A.z) + (residual_value(B.z, wb, 20) - residual_value(A.z, wa, 20)), denominator);
   }
   // Cauchy-Green tensor C = J^T J (FP32) and its eigenvalues.
   float C[3][3];
