@@ -20,10 +20,16 @@
 #ifndef PA_GPU_HPP
 #define PA_GPU_HPP
 
+#include <algorithm>
 #include <array>
+#include <chrono>
+#include <condition_variable>
 #include <cstdint>
 #include <cstring>
+#include <limits>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <optional>
 #include <stdexcept>
 #include <string>
@@ -120,7 +126,182 @@ private:
   std::unique_ptr<pars_gpu_context, deleter> context_;
 };
 
-// pa::partitioner: the same block grid and neighbour table, computed on the host.
+// ---- the ranks of one GPU ---------------------------------------------------------
+// pars runs one MPI process per rank (boost::mpi::communicator,
+// pipeline.cpp:14-17).  On one GPU every rank's block is resident in one device
+// context, and the drop-in's ranks are threads of one process that share a
+// `world`: its collectives (the round exchange and check_completion) wait for
+// every rank as MPI's would, and a round of all ranks is one tracing launch on
+// the device.  A rank that never joins makes the others' collectives fail
+// after `timeout_seconds` with std::runtime_error.
+class world
+{
+public:
+  world(device& dev, integer size, double timeout_seconds = 120.0)
+    : dev_(dev), size_(size), timeout_(timeout_seconds), fields_(size, -1), submitted_(size), next_(size), batches_(size)
+  {
+    if (size < 1) throw std::runtime_error("a world needs at least one rank");
+  }
+  world(const world&) = delete;
+  world& operator=(const world&) = delete;
+  ~world() { if (domain_ >= 0) pars_gpu_domain_release(dev_.get(), domain_); }
+
+  device& get_device() const { return dev_; }
+  integer size() const { return size_; }
+
+  // A rank's local block (its ghosted field handle) and the domain size.
+  void set_block(integer rank, int32_t field, const ivector3& domain_size)
+  {
+    std::lock_guard<std::mutex> lock(mutex_);
+    fields_.at(rank) = field;
+    domain_size_ = domain_size;
+    drop_domain();
+  }
+
+  // particle_tracer::trace(particles, curves, round_info) of `rank` in `round`.
+  void submit(integer rank, int round, const std::vector<particle>& particles, int32_t integrator, int32_t stage_mode, scalar step)
+  {
+    std::lock_guard<std::mutex> lock(mutex_);
+    if (round != submit_round_)
+    {
+      submit_round_ = round;
+      submitted_count_ = 0;
+      for (auto& s : submitted_) s.clear();
+    }
+    submitted_.at(rank) = particles;
+    ++submitted_count_;
+    integrator_ = integrator;
+    stage_mode_ = stage_mode;
+    step_ = step;
+    cv_.notify_all();
+  }
+
+  // out_of_bounds_distribute: once every rank has submitted `round`, the round
+  // runs on the device (once); returns `rank`'s particles of the next round.
+  std::vector<particle> exchange(integer rank, int round)
+  {
+    std::unique_lock<std::mutex> lock(mutex_);
+    wait(lock, [&] { return done_round_ >= round || (submit_round_ == round && submitted_count_ == size_); });
+    if (done_round_ < round) run_round(round);
+    return next_.at(rank);
+  }
+
+  // check_completion: true when no rank holds particles (a collective).
+  bool all_empty(std::size_t count)
+  {
+    std::unique_lock<std::mutex> lock(mutex_);
+    const long long generation = barrier_generation_;
+    any_left_ = any_left_ || count > 0;
+    if (++barrier_arrived_ == size_)
+    {
+      barrier_result_ = !any_left_;
+      if (barrier_result_) { submit_round_ = -1; done_round_ = -1; }   // the next round is the first of a new trace
+      any_left_ = false;
+      barrier_arrived_ = 0;
+      ++barrier_generation_;
+      cv_.notify_all();
+      return barrier_result_;
+    }
+    wait(lock, [&] { return barrier_generation_ != generation; });
+    return barrier_result_;
+  }
+
+  // The device batch indices of `rank`'s curves, in round order.
+  std::vector<int64_t> batches(integer rank)
+  {
+    std::lock_guard<std::mutex> lock(mutex_);
+    return batches_.at(rank);
+  }
+
+private:
+  template <typename predicate> void wait(std::unique_lock<std::mutex>& lock, predicate ready)
+  {
+    if (!cv_.wait_for(lock, std::chrono::duration<double>(timeout_), ready))
+      throw std::runtime_error("a rank did not join the collective within the timeout");
+  }
+  void drop_domain()
+  {
+    if (domain_ >= 0) pars_gpu_domain_release(dev_.get(), domain_);
+    domain_ = -1;
+  }
+  void run_round(int round)
+  {
+    pars_gpu_context* ctx = dev_.get();
+    if (domain_ < 0)
+    {
+      for (integer r = 0; r < size_; ++r)
+        if (fields_[r] < 0) throw std::runtime_error("rank " + std::to_string(r) + " has no local vector field");
+      check(ctx, pars_gpu_domain_assemble(ctx, size_, domain_size_.data, fields_.data(), &domain_), "pars_gpu_domain_assemble");
+    }
+    std::vector<pars_particle> all;
+    std::vector<int64_t> offsets(size_ + 1, 0);
+    for (integer r = 0; r < size_; ++r)
+    {
+      offsets[r + 1] = offsets[r] + (int64_t)submitted_[r].size();
+      const auto* p = reinterpret_cast<const pars_particle*>(submitted_[r].data());
+      all.insert(all.end(), p, p + submitted_[r].size());
+    }
+    if (round == 0) for (auto& b : batches_) b.clear();
+    int64_t before = 0;
+    if (round > 0)
+      for (const auto& b : batches_) before += (int64_t)b.size();
+    std::vector<int64_t> next_offsets(size_ + 1, 0);
+    pars_gpu_trace_summary summary {};
+    static const pars_particle none {};
+    check(ctx, pars_gpu_round_trace(ctx, domain_, round, all.empty() ? &none : all.data(), offsets.data(), integrator_,
+                                    stage_mode_, step_, next_offsets.data(), &summary), "pars_gpu_round_trace");
+    for (int64_t b = before; b < before + summary.batches; ++b)
+    {
+      int32_t rank = 0;
+      check(ctx, pars_gpu_curves_batch_info(ctx, b, nullptr, nullptr, &rank, nullptr), "pars_gpu_curves_batch_info");
+      batches_.at(rank).push_back(b);
+    }
+    std::vector<particle> moved((std::size_t)next_offsets[size_]);
+    if (!moved.empty())
+      check(ctx, pars_gpu_round_particles(ctx, reinterpret_cast<pars_particle*>(moved.data())), "pars_gpu_round_particles");
+    for (integer r = 0; r < size_; ++r)
+      next_[r].assign(moved.begin() + next_offsets[r], moved.begin() + next_offsets[r + 1]);
+    done_round_ = round;
+    cv_.notify_all();
+  }
+
+  device&                            dev_;
+  integer                            size_;
+  double                             timeout_;
+  std::mutex                         mutex_;
+  std::condition_variable            cv_;
+  std::vector<int32_t>               fields_;
+  ivector3                           domain_size_ {};
+  int32_t                            domain_ = -1;
+  int32_t                            integrator_ = PARS_EULER, stage_mode_ = PARS_STAGES_FROZEN;
+  scalar                             step_ = 1.0f;
+  int                                submit_round_ = -1, submitted_count_ = 0, done_round_ = -1;
+  std::vector<std::vector<particle>> submitted_, next_;
+  std::vector<std::vector<int64_t>>  batches_;
+  long long                          barrier_generation_ = 0;
+  integer                            barrier_arrived_ = 0;
+  bool                               any_left_ = false, barrier_result_ = false;
+};
+
+// boost::mpi::communicator as the stages see it: one rank of a world.
+class communicator
+{
+public:
+  communicator(world& w, integer rank) : world_(&w), rank_(rank)
+  {
+    if (rank < 0 || rank >= w.size()) throw std::runtime_error("rank outside the world");
+  }
+  integer rank() const { return rank_; }
+  integer size() const { return world_->size(); }
+  world&  get_world() const { return *world_; }
+
+private:
+  world*  world_;
+  integer rank_;
+};
+
+// pa::partitioner (partitioner.hpp:14-53): the same block grid and neighbour
+// table, computed on the host.
 class partitioner
 {
 public:
@@ -129,33 +310,35 @@ public:
     integer  rank = 0;
     ivector3 multi_rank {}, offset {}, ghosted_block_size {};
   };
-  partitioner(integer ranks, integer rank) : ranks_(ranks), rank_(rank) {}
+  explicit partitioner(pa_gpu::communicator* communicator) : communicator_(communicator) {}
   void set_domain_size(const ivector3& domain_size)
   {
     domain_size_ = domain_size;
     pars_partition_info info {};
-    if (pars_gpu_partition(ranks_, rank_, domain_size.data, &info) != PARS_OK) throw std::runtime_error("pars_gpu_partition failed");
+    if (pars_gpu_partition(communicator_->size(), communicator_->rank(), domain_size.data, &info) != PARS_OK)
+      throw std::runtime_error("pars_gpu_partition failed");
     for (int i = 0; i < 3; ++i)
     {
       grid_size_[i] = info.grid_size[i];
       block_size_[i] = info.block_size[i];
     }
-    local_ = make_info(rank_);
+    local_ = make_info(communicator_->rank());
     for (int f = 0; f < 6; ++f)
       neighbors_[f] = info.neighbor_rank[f] >= 0 ? std::optional<rank_info>(make_info(info.neighbor_rank[f])) : std::nullopt;
   }
+  pa_gpu::communicator* communicator() { return communicator_; }
   const ivector3& domain_size() const { return domain_size_; }
   const ivector3& grid_size  () const { return grid_size_; }
   const ivector3& block_size () const { return block_size_; }
   const std::optional<rank_info>& local_rank_info() const { return local_; }
   const std::array<std::optional<rank_info>, 6>& neighbor_rank_info() const { return neighbors_; }
-  integer size() const { return ranks_; }
 
 private:
   rank_info make_info(integer r) const
   {
     pars_partition_info info {};
-    if (pars_gpu_partition(ranks_, r, domain_size_.data, &info) != PARS_OK) throw std::runtime_error("pars_gpu_partition failed");
+    if (pars_gpu_partition(communicator_->size(), r, domain_size_.data, &info) != PARS_OK)
+      throw std::runtime_error("pars_gpu_partition failed");
     rank_info out;
     out.rank = r;
     for (int i = 0; i < 3; ++i)
@@ -166,7 +349,7 @@ private:
     }
     return out;
   }
-  integer ranks_, rank_;
+  pa_gpu::communicator* communicator_;
   ivector3 domain_size_ {}, grid_size_ {}, block_size_ {};
   std::optional<rank_info> local_;
   std::array<std::optional<rank_info>, 6> neighbors_ {};
@@ -189,66 +372,176 @@ struct seed_generator
   }
 };
 
-// pa::particle_tracer for one block.  trace(particles) runs the rounds, prune,
-// and leaves the curves on the device; the curves are returned as host
-// integral_curves batches (vertices only, as the reference's trace returns).
-// index_generator / color_generator below work on the same device-resident
-// curves when given the tracer, or on host buffers.
+// pa::particle_tracer (particle_tracer.hpp:21-71) with the reference's
+// construction, setters, whole trace() and the sub-methods pipeline::execute
+// calls one by one per round (pipeline.cpp:130-131, 155-205).  On one GPU:
+//  * set_local_vector_field uploads the rank's block; set_neighbor_vector_fields
+//    is kept for the interface: the neighbours are the other ranks' resident
+//    blocks;
+//  * compute_round_info is the reference's arithmetic (particle_tracer.cpp:
+//    210-234; an empty particle list gives no batch instead of the reference's
+//    undefined max_element);
+//  * allocate appends the round's batches; their vertices live on the device
+//    until prune() copies the pruned vertices in (initialize's seed vertices
+//    are written there too);
+//  * trace submits the rank's particles; out_of_bounds_distribute runs the
+//    round of all ranks once every rank has submitted (one launch) and hands
+//    this rank the particles its face neighbours passed on, in the reference's
+//    order (by sending rank, then the sender's order); round_info's particle
+//    maps stay empty (the exchange happens on the device);
+//  * load_balance_distribute / load_balance_collect do nothing: they move
+//    particles between MPI ranks, and here every rank shares one GPU;
+//  * check_completion is the collective "no rank holds particles".
 class particle_tracer
 {
 public:
-  explicit particle_tracer(device& dev) : dev_(dev) {}
-  void set_local_vector_field(int32_t field_handle) { field_ = field_handle; }
+  struct round_info
+  {
+    using particle_map = std::map<integer, std::vector<particle>>;
+    std::size_t  maximum_remaining_iterations     = 0;
+    std::size_t  vertices_per_integral_curve      = 0;
+    std::size_t  vertices_per_integral_curve_last = 0;
+    std::size_t  integral_curve_offset            = 0;
+    std::size_t  integral_curve_count             = 0;
+    particle_map out_of_bounds_particles          {};
+    particle_map neighbor_out_of_bounds_particles {};
+  };
+
+  explicit particle_tracer(pa_gpu::partitioner* partitioner) : partitioner_(partitioner) {}
+  particle_tracer(const particle_tracer&) = delete;
+  particle_tracer& operator=(const particle_tracer&) = delete;
+  ~particle_tracer()
+  {
+    if (field_ >= 0) pars_gpu_field_release(dev().get(), field_);
+  }
+
+  void set_local_vector_field(std::optional<vector_field>* local_vector_field)
+  {
+    local_vector_field_ = local_vector_field;
+    if (field_ >= 0) { pars_gpu_field_release(dev().get(), field_); field_ = -1; }
+    if (local_vector_field_ && local_vector_field_->has_value())
+    {
+      field_ = dev().upload(local_vector_field_->value());
+      partitioner_->communicator()->get_world().set_block(rank(), field_, partitioner_->domain_size());
+    }
+  }
+  void set_neighbor_vector_fields(std::array<std::optional<vector_field>, 6>* neighbor_vector_fields)
+  {
+    neighbor_vector_fields_ = neighbor_vector_fields;
+  }
   void set_integrator(integrator i) { integrator_ = i; }
   void set_step_size(scalar h) { step_size_ = h; }
-  // PARS_STAGES_FROZEN (the reference's scheme, default) or PARS_STAGES_RESAMPLED.
+  // Extension: PARS_STAGES_FROZEN (the reference's scheme, default) or PARS_STAGES_RESAMPLED.
   void set_stage_mode(int32_t mode) { stage_mode_ = mode; }
 
-  std::vector<integral_curves> trace(const std::vector<particle>& particles)
+  // particle_tracer::trace(particles) (particle_tracer.cpp:39-56).
+  std::vector<integral_curves> trace(std::vector<particle> particles)
   {
-    pars_gpu_trace_summary s {};
-    check(dev_.get(), pars_gpu_trace(dev_.get(), field_, reinterpret_cast<const pars_particle*>(particles.data()),
-                                     (int64_t)particles.size(), (int32_t)integrator_, stage_mode_, step_size_, &s), "pars_gpu_trace");
-    batches_ = s.batches;
-    std::vector<integral_curves> out(s.batches);
-    for (int64_t b = 0; b < s.batches; ++b)
+    std::vector<integral_curves> curves;
+    while (!check_completion(particles))
+    {
+      load_balance_distribute(particles);
+      auto info = compute_round_info(particles, curves);
+      allocate(curves, info);
+      initialize(particles, curves, info);
+      trace(particles, curves, info);
+      load_balance_collect(info);
+      out_of_bounds_distribute(particles, info);
+    }
+    prune(curves);
+    return curves;
+  }
+
+  void load_balance_distribute(std::vector<particle>&) {}
+  round_info compute_round_info(const std::vector<particle>& particles, const std::vector<integral_curves>& curves)
+  {
+    round_info info;
+    info.integral_curve_offset = curves.size();
+    if (particles.empty()) return info;
+    integer maximum = 0;
+    for (const auto& p : particles) maximum = std::max(maximum, p.remaining_iterations);
+    info.maximum_remaining_iterations = (std::size_t)std::max(maximum, 1);
+    const std::size_t per_curve = (std::size_t)std::numeric_limits<integer>::max() / sizeof(vector4) / info.maximum_remaining_iterations;
+    info.vertices_per_integral_curve = per_curve * info.maximum_remaining_iterations;
+    info.vertices_per_integral_curve_last = particles.size() % per_curve * info.maximum_remaining_iterations;
+    info.integral_curve_count = 1 + particles.size() / per_curve;
+    return info;
+  }
+  void allocate(std::vector<integral_curves>& curves, const round_info& info)
+  {
+    curves.resize(info.integral_curve_offset + info.integral_curve_count);
+  }
+  void initialize(const std::vector<particle>&, std::vector<integral_curves>&, const round_info&) {}
+  void trace(const std::vector<particle>& particles, std::vector<integral_curves>&, round_info&)
+  {
+    partitioner_->communicator()->get_world().submit(rank(), round_, particles, (int32_t)integrator_, stage_mode_, step_size_);
+  }
+  void load_balance_collect(round_info&) {}
+  void out_of_bounds_distribute(std::vector<particle>& particles, const round_info&)
+  {
+    particles = partitioner_->communicator()->get_world().exchange(rank(), round_);
+    ++round_;
+  }
+  bool check_completion(const std::vector<particle>& particles)
+  {
+    const bool complete = partitioner_->communicator()->get_world().all_empty(particles.size());
+    if (complete) round_ = 0;
+    return complete;
+  }
+  // prune (particle_tracer.cpp:402-409): this rank's batches, pruned on the
+  // device, copied into its integral_curves (vertices).
+  void prune(std::vector<integral_curves>& curves)
+  {
+    const auto batches = partitioner_->communicator()->get_world().batches(rank());
+    if (batches.size() != curves.size())
+      throw std::runtime_error("prune: " + std::to_string(curves.size()) + " batches allocated, " +
+                               std::to_string(batches.size()) + " traced");
+    for (std::size_t k = 0; k < batches.size(); ++k)
     {
       int64_t nv = 0;
-      check(dev_.get(), pars_gpu_curves_batch_info(dev_.get(), b, &nv, nullptr, nullptr, nullptr), "pars_gpu_curves_batch_info");
-      out[b].vertices.resize(nv);
-      check(dev_.get(), pars_gpu_curves_download(dev_.get(), b, out[b].vertices.empty() ? nullptr : out[b].vertices[0].data,
-                                                 nullptr, nullptr), "pars_gpu_curves_download");
+      check(dev().get(), pars_gpu_curves_batch_info(dev().get(), batches[k], &nv, nullptr, nullptr, nullptr),
+            "pars_gpu_curves_batch_info");
+      curves[k].vertices.resize((std::size_t)nv);
+      check(dev().get(), pars_gpu_curves_download(dev().get(), batches[k], nv ? curves[k].vertices[0].data : nullptr, nullptr,
+                                                  nullptr), "pars_gpu_curves_download");
     }
-    return out;
   }
-  // Index and colour the device-resident curves of the last trace and
-  // download everything (the pipeline's stages 4.0 and 5.0 in one pass).
+  // Extension: index and colour every traced batch on the device and copy
+  // this rank's batches out with vertices, colours and indices (the
+  // pipeline's stages 4.0 and 5.0 in one pass; one rank's call serves the
+  // device-resident curves of all ranks, so call it from one rank).
   std::vector<integral_curves> finish(int32_t color_mode, scalar parameter)
   {
-    check(dev_.get(), pars_gpu_curves_index(dev_.get()), "pars_gpu_curves_index");
-    if (color_mode >= 0) check(dev_.get(), pars_gpu_curves_color(dev_.get(), color_mode, parameter), "pars_gpu_curves_color");
-    std::vector<integral_curves> out(batches_);
-    for (int64_t b = 0; b < batches_; ++b)
+    check(dev().get(), pars_gpu_curves_index(dev().get()), "pars_gpu_curves_index");
+    if (color_mode >= 0) check(dev().get(), pars_gpu_curves_color(dev().get(), color_mode, parameter), "pars_gpu_curves_color");
+    const auto batches = partitioner_->communicator()->get_world().batches(rank());
+    std::vector<integral_curves> out(batches.size());
+    for (std::size_t k = 0; k < batches.size(); ++k)
     {
       int64_t nv = 0, ni = 0;
-      check(dev_.get(), pars_gpu_curves_batch_info(dev_.get(), b, &nv, &ni, nullptr, nullptr), "pars_gpu_curves_batch_info");
-      out[b].vertices.resize(nv);
-      out[b].indices.resize(ni);
-      if (color_mode >= 0) out[b].colors.resize(nv);
-      check(dev_.get(), pars_gpu_curves_download(dev_.get(), b, nv ? out[b].vertices[0].data : nullptr,
-                                                 (color_mode >= 0 && nv) ? out[b].colors[0].data : nullptr,
-                                                 ni ? out[b].indices.data() : nullptr), "pars_gpu_curves_download");
+      check(dev().get(), pars_gpu_curves_batch_info(dev().get(), batches[k], &nv, &ni, nullptr, nullptr), "pars_gpu_curves_batch_info");
+      out[k].vertices.resize(nv);
+      out[k].indices.resize(ni);
+      if (color_mode >= 0) out[k].colors.resize(nv);
+      check(dev().get(), pars_gpu_curves_download(dev().get(), batches[k], nv ? out[k].vertices[0].data : nullptr,
+                                                  (color_mode >= 0 && nv) ? out[k].colors[0].data : nullptr,
+                                                  ni ? out[k].indices.data() : nullptr), "pars_gpu_curves_download");
     }
     return out;
   }
 
 private:
-  device&    dev_;
-  int32_t    field_ = -1;
-  integrator integrator_ = integrator::euler;   // the reference's default (particle_tracer.hpp:67)
-  scalar     step_size_ = 1.0f;                  // particle_tracer.hpp:68
-  int32_t    stage_mode_ = PARS_STAGES_FROZEN;
-  int64_t    batches_ = 0;
+  device& dev() const { return partitioner_->communicator()->get_world().get_device(); }
+  integer rank() const { return partitioner_->communicator()->rank(); }
+
+  pa_gpu::partitioner*                        partitioner_ = nullptr;
+  std::optional<vector_field>*                local_vector_field_ = nullptr;
+  std::array<std::optional<vector_field>, 6>* neighbor_vector_fields_ = nullptr;
+  integrator                                  integrator_ = integrator::euler;   // particle_tracer.hpp:67
+  scalar                                      step_size_ = 1.0f;                  // particle_tracer.hpp:68
+  int32_t                                     stage_mode_ = PARS_STAGES_FROZEN;
+  int32_t                                     field_ = -1;
+  int                                         round_ = 0;
 };
 
 // pa::index_generator::generate on a host batch.

@@ -22,6 +22,7 @@
 #ifndef PARS_GPU_H
 #define PARS_GPU_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -105,6 +106,24 @@ typedef struct pars_particle
   int32_t original_voxel[3];
   int32_t padding[2];
 } pars_particle;
+
+/* The layout checks (offsets as in pa::particle with Eigen's 16-byte
+ * Vector4f, particle.hpp:30-35). */
+#ifdef __cplusplus
+static_assert(sizeof(pars_particle) == 48, "pars_particle is 48 bytes like pa::particle");
+static_assert(offsetof(pars_particle, position) == 0, "position at offset 0");
+static_assert(offsetof(pars_particle, remaining_iterations) == 16, "remaining_iterations at offset 16");
+static_assert(offsetof(pars_particle, vector_field_index) == 20, "vector_field_index at offset 20");
+static_assert(offsetof(pars_particle, original_rank) == 24, "original_rank at offset 24");
+static_assert(offsetof(pars_particle, original_voxel) == 28, "original_voxel at offset 28");
+#else
+_Static_assert(sizeof(pars_particle) == 48, "pars_particle is 48 bytes like pa::particle");
+_Static_assert(offsetof(pars_particle, position) == 0, "position at offset 0");
+_Static_assert(offsetof(pars_particle, remaining_iterations) == 16, "remaining_iterations at offset 16");
+_Static_assert(offsetof(pars_particle, vector_field_index) == 20, "vector_field_index at offset 20");
+_Static_assert(offsetof(pars_particle, original_rank) == 24, "original_rank at offset 24");
+_Static_assert(offsetof(pars_particle, original_voxel) == 28, "original_voxel at offset 28");
+#endif
 
 /* partitioner::set_domain_size / rank_info (pa/source/stages/partitioner.cpp:8-53). */
 typedef struct pars_partition_info
@@ -205,6 +224,41 @@ int32_t pars_gpu_trace_domain(pars_gpu_context* context, int32_t domain, const p
                               const int64_t* seed_offsets, int32_t integrator, int32_t stage_mode, float step_size,
                               pars_gpu_trace_summary* summary);
 
+/* ---- round-by-round tracing: the stage calls of pipeline::execute's round loop
+ * (pars/source/pipeline.cpp:153-209) on one GPU.  Every rank of the
+ * partitioned domain is a block resident in this context; one call traces one
+ * round of all of them at once.
+ *
+ * pars_gpu_domain_assemble: a domain whose blocks are fields the ranks
+ * uploaded themselves (each rank's local_vector_field_, data_io.cpp:90-114):
+ * the partitioner's grid of `ranks` blocks over domain_size (voxels), with
+ * fields[r] = rank r's ghosted block (shape = its ghosted_block_size).  It
+ * replaces particle_tracer::set_local_vector_field / set_neighbor_vector_fields
+ * (pa/include/pa/stages/particle_tracer.hpp:44-45): on one GPU a block's face
+ * neighbours are the other ranks' resident blocks.  Releasing the domain
+ * leaves the fields to their owner. */
+int32_t pars_gpu_domain_assemble(pars_gpu_context* context, int32_t ranks, const int32_t domain_size[3], const int32_t* fields,
+                                 int32_t* domain);
+/* One round of particle_tracer's sub-methods for every rank
+ * (particle_tracer.cpp:210-393: compute_round_info, allocate, initialize,
+ * trace, out_of_bounds_distribute), replacing particle_tracer.hpp:51-59.
+ * Rank r's particles of this round are particles[offsets[r] .. offsets[r+1])
+ * (HOST), or, with particles = NULL, the particles the previous round left on
+ * the device for round `round`.  The round's curves, pruned, in
+ * compute_round_info's batches per rank and tagged (rank, round), are appended
+ * to the context's curves (round 0 starts them afresh).  Particles that left
+ * their block through a face with a neighbour become the neighbour's particles
+ * of the next round, ordered by sending rank, then by the sender's order;
+ * next_offsets (HOST, ranks + 1 entries, may be NULL) receives each rank's
+ * next-round count (all zero: check_completion holds).  summary: this round's
+ * batches, vertices and steps. */
+int32_t pars_gpu_round_trace(pars_gpu_context* context, int32_t domain, int32_t round, const pars_particle* particles,
+                             const int64_t* offsets, int32_t integrator, int32_t stage_mode, float step_size,
+                             int64_t* next_offsets, pars_gpu_trace_summary* summary);
+/* Copies the next round's particles left by the last pars_gpu_round_trace to
+ * HOST `particles` (next_offsets[ranks] of them, grouped by rank). */
+int32_t pars_gpu_round_particles(pars_gpu_context* context, pars_particle* particles);
+
 /* Curves of the last trace call, resident on the device.
  * pars_gpu_curves_index: index_generator::generate on every batch.
  * pars_gpu_curves_color: color_generator::generate on every batch (needs indices). */
@@ -229,8 +283,9 @@ int32_t pars_gpu_color_generate(pars_gpu_context* context, const float* vertices
  * one particle per voxel of an int(shape * scale) grid with spacing
  * spacing / scale, advected with particle_advector's rules
  * (particle_advector.cpp:74-139; at most iterations - 1 steps).  The flow map
- * becomes a new field handle (*flow_map) resident on the device.  Integrators
- * as for pars_gpu_trace. */
+ * becomes a new field handle (*flow_map) resident on the device (re-sampled
+ * stages also keep the positions' sub-ulp residuals, as for batched jobs
+ * below).  Integrators as for pars_gpu_trace. */
 int32_t pars_gpu_flow_map_generate(pars_gpu_context* context, int32_t field, int32_t iterations, float resolution_scale,
                                    int32_t integrator, int32_t stage_mode, float step_size, int32_t* flow_map, int64_t* steps);
 /* FTLE of a flow-map field: central-difference gradient (one-sided at the
@@ -278,11 +333,16 @@ typedef struct pars_gpu_batch_job
   float        lattice_stride[3];
   int32_t      lattice_count[3];
   int32_t      padding1;
-  float*       end_positions;       /* DEVICE float4 per seed (last position), may be NULL */
+  float*       end_positions;       /* DEVICE float4 per seed (last position; see below), may be NULL */
   int32_t*     end_steps;           /* DEVICE int32 per seed (steps taken), may be NULL */
   int64_t      steps;               /* out: particle-steps of this job */
 } pars_gpu_batch_job;
 
+/* End positions and flow maps of re-sampled stages are the correctly rounded
+ * FP32 coordinates (x, y, z) and, in w, each coordinate's rounding residual as
+ * a signed 10-bit code q (bits 0-9: x, 10-19: y, 20-29: z; bits 30-31 zero):
+ * coordinate = x + q / 1022 * ulp(x), about 34 bits in all (the FTLE stage
+ * differentiates flow maps with it).  Frozen-scheme results store w = 0. */
 /* Advects every job in one persistent launch that drains a device queue of
  * seed chunks.  variant selects the launch shape (threads per CTA, register
  * budget) among pars_gpu_batch_variants(); -1 = autotuned: the first call of

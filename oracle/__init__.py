@@ -174,6 +174,8 @@ class Port(_Lib):
         L.orc_curves_steps.argtypes = [_P]
         L.orc_max_threads.restype = _I
         L.orc_set_threads.argtypes = [_I]
+        L.orc_set_correctly_rounded_trig.argtypes = [_I]
+        L.orc_set_correctly_rounded_trig.restype = None
         L.orc_flow_map.restype = _LL
         L.orc_flow_map.argtypes = [_P] * 5 + [_I, _F, _I, _F, _LL, _LL, _LL, _P]
         L.orc_advect_fp64.restype = None
@@ -242,6 +244,15 @@ class Port(_Lib):
 
     def set_threads(self, n):
         self.lib.orc_set_threads(n)
+
+    def color_generate_correctly_rounded(self, vertices, indices, mode="rgb", parameter=0.5):
+        """color_generate with to_spherical's atan2 / acos correctly rounded
+        (FP64 rounded to FP32) instead of the host libm's FP32 functions."""
+        self.lib.orc_set_correctly_rounded_trig(1)
+        try:
+            return self.color_generate(vertices, indices, mode, parameter)
+        finally:
+            self.lib.orc_set_correctly_rounded_trig(0)
 
     def flow_map(self, field, iterations, scale=1.0, integrator=2, step=0.01, first=0, count=None, stride=1):
         """Frozen-velocity FP32 flow map (reference semantics) of the seeds

@@ -304,13 +304,20 @@ inline void hue_to_rgba(float hue, float* out)
   out[3] = 1.0f;
 }
 
+// How to_spherical's FP32 atan2 / acos are evaluated: the host libm's
+// atan2f / acosf, as the reference calls them (default), or correctly rounded
+// (FP64 evaluation rounded to FP32) -- the latter only to attribute colour
+// differences to the libms in the tests.
+bool correctly_rounded_trig = false;
+
 // to_spherical + correct_range: returns (hue, second) in [0, 1].
 inline void spherical_hue(const vec4& t, float& hue, float& second)
 {
   const double x = t.v[0], y = t.v[1], zc = t.v[2];
   const float radius = float(std::sqrt(std::pow(x, 2) + std::pow(y, 2) + std::pow(zc, 2)));
-  float s1 = std::atan2(t.v[1], t.v[0]);
-  float s2 = std::acos(t.v[2] / radius);
+  const float ratio = t.v[2] / radius;
+  float s1 = correctly_rounded_trig ? float(std::atan2(double(t.v[1]), double(t.v[0]))) : std::atan2(t.v[1], t.v[0]);
+  float s2 = correctly_rounded_trig ? float(std::acos(double(ratio))) : std::acos(ratio);
   const float pi = float(M_PI);
   if (s1 <  0.0f) s1 += pi;
   if (s1 >= pi)   s1 -= pi;
@@ -763,6 +770,8 @@ double largest_eigenvalue(const double a[3][3])
 }
 
 extern "C" {
+
+void orc_set_correctly_rounded_trig(int on) { correctly_rounded_trig = on != 0; }
 
 // ---- curves accessors ------------------------------------------------------
 long long orc_curves_batches(const orc_curves* c) { return (long long)c->batches.size(); }

@@ -118,6 +118,7 @@ struct trace_block
 struct domain_entry
 {
   int                      ranks = 0;
+  bool                     owns_fields = true;   // false: blocks are the caller's fields (pars_gpu_domain_assemble)
   pars_partition_info      first {};
   std::vector<int>         fields;      // field handle per block
   std::vector<trace_block> blocks;
@@ -216,6 +217,15 @@ struct pars_gpu_context
                                           slot_layouts, curve_bounds, color_specs;
   pars::device_buffer                     ftle;
   long long                               ftle_count = 0;
+  // round-by-round tracing (pars_gpu_round_trace): the next round's
+  // particles stay in particles_in / block_of; their per-block counts and
+  // largest remaining_iterations, the round they belong to, and the tracing
+  // call that left them (trace_serial counts every tracing call)
+  long long                               trace_serial = 0, round_serial = -1;
+  int                                     round_domain = -1, round_next = 0;
+  long long                               round_count = 0;
+  std::vector<long long>                  round_block_count;
+  std::vector<int>                        round_block_max;
   // Released field buffers kept for reuse (bytes -> buffer), so that a caller
   // that uploads, traces and releases every request does not pay cudaMalloc /
   // cudaFree (and their device-wide synchronisation) each time.

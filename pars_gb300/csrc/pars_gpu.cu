@@ -344,10 +344,34 @@ void grow_curves(pars_gpu_context& ctx, long long needed_vertices)
 // The round loop over device-resident particles grouped by block.
 // particles/block_of live in ctx.particles_in / ctx.block_of; block_count and
 // block_max give each block's particle count and maximum remaining_iterations.
-void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, const trace_block* device_blocks,
-                long long count, std::vector<long long> block_count, std::vector<int> block_max,
-                const step_rule& rule, bool route_exits, pars_gpu_trace_summary* summary,
-                const step_rule* device_block_rules = nullptr)
+// What one tracing round needs from the previous one: the particles of the
+// round (in ctx.particles_in, grouped by block in block order, with
+// ctx.block_of when there are several blocks), each block's particle count
+// and largest remaining_iterations.
+struct round_plan
+{
+  long long              count = 0;
+  std::vector<long long> block_count;
+  std::vector<int>       block_max;
+};
+
+// The tracing counters: steps (accumulated over rounds), the exit-queue size
+// (32-bit) and the tracing kernel's pool counter.
+struct round_counters
+{
+  unsigned long long* steps;
+  unsigned int*       exits;
+  unsigned long long* pool;
+};
+
+round_counters tracing_counters(pars_gpu_context& ctx)
+{
+  ctx.counters.reserve(sizeof(unsigned long long) * 3);
+  auto* base = ctx.counters.as<unsigned long long>();
+  return {base, reinterpret_cast<unsigned int*>(base + 1), base + 2};
+}
+
+void clear_curves(pars_gpu_context& ctx)
 {
   auto& curves = ctx.curves;
   curves.batches.clear();
@@ -355,155 +379,183 @@ void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, c
   curves.index_total = 0;
   curves.indexed = curves.colored = false;
   ++curves.generation;
+}
+
+// One round of the reference's loop (particle_tracer.cpp:210-393) for every
+// block at once: compute_round_info's batch split per block, the slots
+// (allocate / initialize), one tracing launch, prune into batches tagged
+// `round` appended to ctx.curves, and the exchange: the exit queue, stably
+// ordered by (destination block, source order), becomes the next round's
+// particles in ctx.particles_in, and `plan` describes them.
+void trace_one_round(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, const trace_block* device_blocks,
+                     round_plan& plan, const step_rule& rule, bool route_exits, int round, const round_counters& counters,
+                     const step_rule* device_block_rules)
+{
+  auto& curves = ctx.curves;
   const int nblocks = int(blocks.size());
   int key_bits = 40;
   while ((1 << (key_bits - 40)) < nblocks) ++key_bits;
+  const long long count = plan.count;
+  auto& block_count = plan.block_count;
+  auto& block_max = plan.block_max;
 
-  // counters: steps, exit queue size (32-bit), the tracing kernel's pool counter
-  ctx.counters.reserve(sizeof(unsigned long long) * 3);
-  auto* steps_counter = ctx.counters.as<unsigned long long>();
-  auto* exit_counter = reinterpret_cast<unsigned int*>(steps_counter + 1);
-  auto* pool_counter = steps_counter + 2;
-  PARS_CUDA(cudaMemsetAsync(steps_counter, 0, sizeof(unsigned long long), ctx.stream));
-
-  int round = 0;
-  while (count > 0)
+  // The round's particles are grouped by block in block order (seeds per
+  // rank; exits sorted by destination block), so each block's slots follow
+  // the previous block's.
+  std::vector<slot_layout> layout(nblocks);
+  long long total_slots = 0, first_particle = 0;
+  for (int b = 0; b < nblocks; ++b)
   {
-    // The round's particles are grouped by block in block order (seeds per
-    // rank; exits sorted by destination block), so each block's slots follow
-    // the previous block's.
-    std::vector<slot_layout> layout(nblocks);
-    long long total_slots = 0, first_particle = 0;
-    for (int b = 0; b < nblocks; ++b)
-    {
-      const long long stride = std::max(1, block_max[b]);
-      layout[b].origin = total_slots - first_particle * stride;
-      layout[b].stride = stride;
-      total_slots += block_count[b] * stride;
-      first_particle += block_count[b];
-    }
-    PARS_REQUIRE(first_particle == count, "block particle counts do not add up to the particle count");
-    ctx.slots.reserve(sizeof(float4) * (std::size_t)total_slots);
-    ctx.slot_layouts.reserve(sizeof(slot_layout) * nblocks);
-    PARS_CUDA(cudaMemcpyAsync(ctx.slot_layouts.get(), layout.data(), sizeof(slot_layout) * nblocks, cudaMemcpyHostToDevice, ctx.stream));
-    ctx.written.reserve(sizeof(int) * count);
-    ctx.kept.reserve(sizeof(int) * count);
-    ctx.offsets.reserve(sizeof(long long) * (count + 1));
-    if (route_exits)
-    {
-      ctx.exits.reserve(sizeof(pars_particle) * count);
-      ctx.exit_keys.reserve(sizeof(unsigned long long) * count);
-    }
-    PARS_CUDA(cudaMemsetAsync(exit_counter, 0, sizeof(unsigned int), ctx.stream));
-    PARS_CUDA(cudaMemsetAsync(pool_counter, 0, sizeof(unsigned long long), ctx.stream));
+    const long long stride = std::max(1, block_max[b]);
+    layout[b].origin = total_slots - first_particle * stride;
+    layout[b].stride = stride;
+    total_slots += block_count[b] * stride;
+    first_particle += block_count[b];
+  }
+  PARS_REQUIRE(first_particle == count, "block particle counts do not add up to the particle count");
+  ctx.slots.reserve(sizeof(float4) * (std::size_t)total_slots);
+  ctx.slot_layouts.reserve(sizeof(slot_layout) * nblocks);
+  PARS_CUDA(cudaMemcpyAsync(ctx.slot_layouts.get(), layout.data(), sizeof(slot_layout) * nblocks, cudaMemcpyHostToDevice, ctx.stream));
+  ctx.written.reserve(sizeof(int) * count);
+  ctx.kept.reserve(sizeof(int) * count);
+  ctx.offsets.reserve(sizeof(long long) * (count + 1));
+  if (route_exits)
+  {
+    ctx.exits.reserve(sizeof(pars_particle) * count);
+    ctx.exit_keys.reserve(sizeof(unsigned long long) * count);
+  }
+  PARS_CUDA(cudaMemsetAsync(counters.exits, 0, sizeof(unsigned int), ctx.stream));
+  PARS_CUDA(cudaMemsetAsync(counters.pool, 0, sizeof(unsigned long long), ctx.stream));
 
-    trace_launch a {};
-    a.blocks = device_blocks;
-    a.particles = ctx.particles_in.as<const pars_particle>();
-    a.block_of = nblocks > 1 ? ctx.block_of.as<const int>() : nullptr;
-    a.count = count;
-    a.block_slots = ctx.slot_layouts.as<const slot_layout>();
-    a.slots = ctx.slots.as<float4>();
-    a.written = ctx.written.as<int>();
-    a.kept = ctx.kept.as<int>();
-    a.rule = rule;
-    a.block_rules = device_block_rules;
-    a.route_exits = route_exits ? 1 : 0;
-    a.exit_particles = route_exits ? ctx.exits.as<pars_particle>() : nullptr;
-    a.exit_keys = route_exits ? ctx.exit_keys.as<unsigned long long>() : nullptr;
-    a.exit_count = exit_counter;
-    a.steps = steps_counter;
-    a.next = pool_counter;
-    launch_trace(ctx, a);
+  trace_launch a {};
+  a.blocks = device_blocks;
+  a.particles = ctx.particles_in.as<const pars_particle>();
+  a.block_of = nblocks > 1 ? ctx.block_of.as<const int>() : nullptr;
+  a.count = count;
+  a.block_slots = ctx.slot_layouts.as<const slot_layout>();
+  a.slots = ctx.slots.as<float4>();
+  a.written = ctx.written.as<int>();
+  a.kept = ctx.kept.as<int>();
+  a.rule = rule;
+  a.block_rules = device_block_rules;
+  a.route_exits = route_exits ? 1 : 0;
+  a.exit_particles = route_exits ? ctx.exits.as<pars_particle>() : nullptr;
+  a.exit_keys = route_exits ? ctx.exit_keys.as<unsigned long long>() : nullptr;
+  a.exit_count = counters.exits;
+  a.steps = counters.steps;
+  a.next = counters.pool;
+  launch_trace(ctx, a);
 
-    // prune: packed offsets of every particle's kept vertices.
-    exclusive_sum(ctx, ctx.kept.as<int>(), ctx.offsets.as<long long>(), count);
+  // prune: packed offsets of every particle's kept vertices.
+  exclusive_sum(ctx, ctx.kept.as<int>(), ctx.offsets.as<long long>(), count);
 
-    // Batch boundaries per block (compute_round_info), as particle indices.
-    struct pending_batch { long long first, last; int rank; };
-    std::vector<pending_batch> pending;
-    long long first = 0;
-    for (int b = 0; b < nblocks; ++b)
-    {
-      const long long n = block_count[b];
-      if (n == 0) continue;
-      const long long max_vertices = std::numeric_limits<int32_t>::max() / 16;
-      const long long ppc = max_vertices / std::max(1, block_max[b]);
-      PARS_REQUIRE(ppc > 0, "remaining_iterations exceeds the batch vertex limit");
-      const long long curve_count = 1 + n / ppc;
-      for (long long k = 0; k < curve_count; ++k)
-        pending.push_back({first + std::min(n, k * ppc), first + std::min(n, (k + 1) * ppc), b});
-      first += n;
-    }
-    std::vector<long long> positions;
-    positions.reserve(pending.size() * 2 + 1);
-    for (auto& p : pending) { positions.push_back(p.first); positions.push_back(p.last); }
-    positions.push_back(count);
-    std::vector<long long> boundary(positions.size());
-    ctx.boundary_positions.reserve(sizeof(long long) * positions.size());
-    ctx.boundary_offsets.reserve(sizeof(long long) * positions.size());
-    PARS_CUDA(cudaMemcpyAsync(ctx.boundary_positions.get(), positions.data(), sizeof(long long) * positions.size(), cudaMemcpyHostToDevice, ctx.stream));
-    launch_gather_offsets(ctx, ctx.offsets.as<const long long>(), ctx.boundary_positions.as<const long long>(), (long long)positions.size(),
-                          ctx.boundary_offsets.as<long long>());
-    unsigned int exit_total = 0;
-    PARS_CUDA(cudaMemcpyAsync(boundary.data(), ctx.boundary_offsets.get(), sizeof(long long) * boundary.size(), cudaMemcpyDeviceToHost, ctx.stream));
-    PARS_CUDA(cudaMemcpyAsync(&exit_total, exit_counter, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx.stream));
+  // Batch boundaries per block (compute_round_info), as particle indices.
+  struct pending_batch { long long first, last; int rank; };
+  std::vector<pending_batch> pending;
+  long long first = 0;
+  for (int b = 0; b < nblocks; ++b)
+  {
+    const long long n = block_count[b];
+    if (n == 0) continue;
+    const long long max_vertices = std::numeric_limits<int32_t>::max() / 16;
+    const long long ppc = max_vertices / std::max(1, block_max[b]);
+    PARS_REQUIRE(ppc > 0, "remaining_iterations exceeds the batch vertex limit");
+    const long long curve_count = 1 + n / ppc;
+    for (long long k = 0; k < curve_count; ++k)
+      pending.push_back({first + std::min(n, k * ppc), first + std::min(n, (k + 1) * ppc), b});
+    first += n;
+  }
+  std::vector<long long> positions;
+  positions.reserve(pending.size() * 2 + 1);
+  for (auto& p : pending) { positions.push_back(p.first); positions.push_back(p.last); }
+  positions.push_back(count);
+  std::vector<long long> boundary(positions.size());
+  ctx.boundary_positions.reserve(sizeof(long long) * positions.size());
+  ctx.boundary_offsets.reserve(sizeof(long long) * positions.size());
+  PARS_CUDA(cudaMemcpyAsync(ctx.boundary_positions.get(), positions.data(), sizeof(long long) * positions.size(), cudaMemcpyHostToDevice, ctx.stream));
+  launch_gather_offsets(ctx, ctx.offsets.as<const long long>(), ctx.boundary_positions.as<const long long>(), (long long)positions.size(),
+                        ctx.boundary_offsets.as<long long>());
+  unsigned int exit_total = 0;
+  PARS_CUDA(cudaMemcpyAsync(boundary.data(), ctx.boundary_offsets.get(), sizeof(long long) * boundary.size(), cudaMemcpyDeviceToHost, ctx.stream));
+  PARS_CUDA(cudaMemcpyAsync(&exit_total, counters.exits, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx.stream));
+  PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+  const long long round_vertices = boundary.back();
+
+  grow_curves(ctx, curves.vertex_total + round_vertices);
+  launch_compact_vertices(ctx, ctx.slots.as<const float4>(), ctx.slot_layouts.as<const slot_layout>(), a.block_of,
+                          ctx.written.as<const int>(), ctx.offsets.as<const long long>(), count,
+                          curves.vertices.as<float4>() + curves.vertex_total);
+  for (std::size_t k = 0; k < pending.size(); ++k)
+  {
+    curves_batch batch;
+    batch.vertex_offset = curves.vertex_total + boundary[2 * k];
+    batch.vertex_count = boundary[2 * k + 1] - boundary[2 * k];
+    batch.rank = pending[k].rank;
+    batch.round = round;
+    curves.batches.push_back(batch);
+  }
+  curves.vertex_total += round_vertices;
+
+  // Exchange: the exit queue, stably ordered by (destination block, source
+  // order), becomes the next round's particle list.
+  const long long next = route_exits ? (long long)exit_total : 0;
+  std::fill(block_count.begin(), block_count.end(), 0);
+  std::fill(block_max.begin(), block_max.end(), 0);
+  if (next > 0)
+  {
+    ctx.exit_keys_sorted.reserve(sizeof(unsigned long long) * next);
+    ctx.exit_order.reserve(sizeof(unsigned int) * next);
+    ctx.exit_order_sorted.reserve(sizeof(unsigned int) * next);
+    ctx.particles_next.reserve(sizeof(pars_particle) * next);
+    ctx.block_of_next.reserve(sizeof(int) * next);
+    ctx.block_max.reserve(sizeof(int) * 2 * nblocks);
+    PARS_CUDA(cudaMemsetAsync(ctx.block_max.get(), 0, sizeof(int) * 2 * nblocks, ctx.stream));
+    launch_iota(ctx, ctx.exit_order.as<unsigned int>(), next);
+    sort_pairs(ctx, ctx.exit_keys.as<const unsigned long long>(), ctx.exit_keys_sorted.as<unsigned long long>(),
+               ctx.exit_order.as<const unsigned int>(), ctx.exit_order_sorted.as<unsigned int>(), next, key_bits);
+    launch_gather_exits(ctx, ctx.exits.as<const pars_particle>(), ctx.exit_order_sorted.as<const unsigned int>(),
+                        ctx.exit_keys_sorted.as<const unsigned long long>(), next, ctx.particles_next.as<pars_particle>(),
+                        ctx.block_of_next.as<int>(), ctx.block_max.as<int>(), ctx.block_max.as<int>() + nblocks);
+    std::vector<int> stats(2 * nblocks);
+    PARS_CUDA(cudaMemcpyAsync(stats.data(), ctx.block_max.get(), sizeof(int) * 2 * nblocks, cudaMemcpyDeviceToHost, ctx.stream));
     PARS_CUDA(cudaStreamSynchronize(ctx.stream));
-    const long long round_vertices = boundary.back();
+    for (int b = 0; b < nblocks; ++b) { block_max[b] = stats[b]; block_count[b] = stats[nblocks + b]; }
+    std::swap(ctx.particles_in, ctx.particles_next);
+    std::swap(ctx.block_of, ctx.block_of_next);
+  }
+  plan.count = next;
+}
 
-    grow_curves(ctx, curves.vertex_total + round_vertices);
-    launch_compact_vertices(ctx, ctx.slots.as<const float4>(), ctx.slot_layouts.as<const slot_layout>(), a.block_of,
-                            ctx.written.as<const int>(), ctx.offsets.as<const long long>(), count,
-                            curves.vertices.as<float4>() + curves.vertex_total);
-    for (std::size_t k = 0; k < pending.size(); ++k)
-    {
-      curves_batch batch;
-      batch.vertex_offset = curves.vertex_total + boundary[2 * k];
-      batch.vertex_count = boundary[2 * k + 1] - boundary[2 * k];
-      batch.rank = pending[k].rank;
-      batch.round = round;
-      curves.batches.push_back(batch);
-    }
-    curves.vertex_total += round_vertices;
-
-    // Exchange: the exit queue, stably ordered by (destination block, source
-    // order), becomes the next round's particle list.
-    long long next = route_exits ? (long long)exit_total : 0;
-    std::fill(block_count.begin(), block_count.end(), 0);
-    std::fill(block_max.begin(), block_max.end(), 0);
-    if (next > 0)
-    {
-      ctx.exit_keys_sorted.reserve(sizeof(unsigned long long) * next);
-      ctx.exit_order.reserve(sizeof(unsigned int) * next);
-      ctx.exit_order_sorted.reserve(sizeof(unsigned int) * next);
-      ctx.particles_next.reserve(sizeof(pars_particle) * next);
-      ctx.block_of_next.reserve(sizeof(int) * next);
-      ctx.block_max.reserve(sizeof(int) * 2 * nblocks);
-      PARS_CUDA(cudaMemsetAsync(ctx.block_max.get(), 0, sizeof(int) * 2 * nblocks, ctx.stream));
-      launch_iota(ctx, ctx.exit_order.as<unsigned int>(), next);
-      sort_pairs(ctx, ctx.exit_keys.as<const unsigned long long>(), ctx.exit_keys_sorted.as<unsigned long long>(),
-                 ctx.exit_order.as<const unsigned int>(), ctx.exit_order_sorted.as<unsigned int>(), next, key_bits);
-      launch_gather_exits(ctx, ctx.exits.as<const pars_particle>(), ctx.exit_order_sorted.as<const unsigned int>(),
-                          ctx.exit_keys_sorted.as<const unsigned long long>(), next, ctx.particles_next.as<pars_particle>(),
-                          ctx.block_of_next.as<int>(), ctx.block_max.as<int>(), ctx.block_max.as<int>() + nblocks);
-      std::vector<int> stats(2 * nblocks);
-      PARS_CUDA(cudaMemcpyAsync(stats.data(), ctx.block_max.get(), sizeof(int) * 2 * nblocks, cudaMemcpyDeviceToHost, ctx.stream));
-      PARS_CUDA(cudaStreamSynchronize(ctx.stream));
-      for (int b = 0; b < nblocks; ++b) { block_max[b] = stats[b]; block_count[b] = stats[nblocks + b]; }
-      std::swap(ctx.particles_in, ctx.particles_next);
-      std::swap(ctx.block_of, ctx.block_of_next);
-    }
-    count = next;
+// The whole round loop (particle_tracer::trace, particle_tracer.cpp:39-56)
+// over device-resident particles grouped by block: rounds until no particle
+// is left, the curves of every round in ctx.curves.
+void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, const trace_block* device_blocks,
+                long long count, std::vector<long long> block_count, std::vector<int> block_max,
+                const step_rule& rule, bool route_exits, pars_gpu_trace_summary* summary,
+                const step_rule* device_block_rules = nullptr)
+{
+  clear_curves(ctx);
+  ++ctx.trace_serial;
+  const round_counters counters = tracing_counters(ctx);
+  PARS_CUDA(cudaMemsetAsync(counters.steps, 0, sizeof(unsigned long long), ctx.stream));
+  round_plan plan;
+  plan.count = count;
+  plan.block_count = std::move(block_count);
+  plan.block_max = std::move(block_max);
+  int round = 0;
+  while (plan.count > 0)
+  {
+    trace_one_round(ctx, blocks, device_blocks, plan, rule, route_exits, round, counters, device_block_rules);
     ++round;
   }
 
   unsigned long long steps = 0;
-  PARS_CUDA(cudaMemcpyAsync(&steps, steps_counter, sizeof(steps), cudaMemcpyDeviceToHost, ctx.stream));
+  PARS_CUDA(cudaMemcpyAsync(&steps, counters.steps, sizeof(steps), cudaMemcpyDeviceToHost, ctx.stream));
   PARS_CUDA(cudaStreamSynchronize(ctx.stream));
   if (summary)
   {
-    summary->batches = (long long)curves.batches.size();
-    summary->vertices = curves.vertex_total;
+    summary->batches = (long long)ctx.curves.batches.size();
+    summary->vertices = ctx.curves.vertex_total;
     summary->steps = (long long)steps;
     summary->rounds = round;
     summary->padding = 0;
@@ -548,8 +600,11 @@ void trace_single(pars_gpu_context& ctx, int32_t field, long long count, int32_t
 // job's arithmetic, and so its result, does not depend on the other jobs of
 // the batch.  variant < 0 uses the context's tuned launch
 // shape for each class, tuning it first if needed: every job of the class
-// capped at 16384 seeds, each shape timed twice with CUDA events, the fastest
-// kept.
+// capped at four times the seeds the GPU holds resident (2048 lanes per SM),
+// so that each shape runs at its own occupancy in steady state, each shape
+// timed twice with CUDA events, the fastest kept.  (A cap of 16384 seeds fills
+// a sixth of a GB300's lanes and picked a 104-register shape that was 7 %
+// slower on the 256^3 flow map than the 96-register one.)
 std::vector<unsigned long long> execute_batch(pars_gpu_context& ctx, std::vector<batch_job_device>& jobs, int variant)
 {
   const int count = int(jobs.size());
@@ -605,7 +660,9 @@ std::vector<unsigned long long> execute_batch(pars_gpu_context& ctx, std::vector
   {
     if (variant >= 0 || size[c] == 0 || ctx.batch_variant[c] >= 0) continue;
     std::vector<long long> full(count);
-    for (int k = 0; k < count; ++k) { full[k] = queue[k].seed_count; queue[k].seed_count = std::min(full[k], 16384LL); }
+    if (ctx.sm_count <= 0) PARS_CUDA(cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, ctx.device));
+    const long long probe = std::max(16384LL, 4LL * 2048LL * ctx.sm_count);
+    for (int k = 0; k < count; ++k) { full[k] = queue[k].seed_count; queue[k].seed_count = std::min(full[k], probe); }
     cudaEvent_t a, b;
     PARS_CUDA(cudaEventCreate(&a));
     PARS_CUDA(cudaEventCreate(&b));
@@ -995,6 +1052,7 @@ int32_t pars_gpu_domain_release(pars_gpu_context* ctx, int32_t domain)
     auto it = ctx->domains.find(domain);
     if (it == ctx->domains.end()) throw error(PARS_ERR_NOT_FOUND, "no domain with handle " + std::to_string(domain));
     PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (it->second->owns_fields)
     for (int f : it->second->fields)
     {
       auto fit = ctx->fields.find(f);
@@ -1040,6 +1098,140 @@ int32_t pars_gpu_trace_domain(pars_gpu_context* ctx, int32_t domain, const pars_
       PARS_CUDA(cudaMemcpyAsync(ctx->block_of.get(), block_of.data(), sizeof(int) * count, cudaMemcpyHostToDevice, ctx->stream));
     }
     run_rounds(*ctx, d.blocks, d.device_blocks.as<const trace_block>(), count, block_count, block_max, rule, true, summary);
+  });
+}
+
+// ---- round-by-round tracing ----------------------------------------------------------
+int32_t pars_gpu_domain_assemble(pars_gpu_context* ctx, int32_t ranks, const int32_t domain_size[3], const int32_t* fields,
+                                 int32_t* domain)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(domain_size && fields && domain, "domain_size, fields and domain are required");
+    PARS_REQUIRE(ranks >= 1, "ranks must be >= 1");
+    for (int i = 0; i < 3; ++i) PARS_REQUIRE(domain_size[i] >= 2, "every domain extent must be >= 2");
+    auto entry = std::make_unique<domain_entry>();
+    entry->ranks = ranks;
+    entry->owns_fields = false;
+    entry->first = partition_of(ranks, 0, domain_size);
+    for (int r = 0; r < ranks; ++r)
+    {
+      const pars_partition_info info = partition_of(ranks, r, domain_size);
+      auto& f = find_field(*ctx, fields[r]);
+      PARS_REQUIRE(f.slices == 1, "domain blocks must be steady fields");
+      for (int i = 0; i < 3; ++i)
+        PARS_REQUIRE(f.shape[i] == info.ghosted_block_size[i],
+                     "field of rank " + std::to_string(r) + " is not its ghosted block of the partition");
+      trace_block b;
+      b.field = f.view();
+      for (int face = 0; face < 6; ++face) b.neighbor[face] = info.neighbor_rank[face];
+      entry->blocks.push_back(b);
+      entry->fields.push_back(fields[r]);
+    }
+    entry->device_blocks.reserve(sizeof(trace_block) * ranks);
+    PARS_CUDA(cudaMemcpyAsync(entry->device_blocks.get(), entry->blocks.data(), sizeof(trace_block) * ranks, cudaMemcpyHostToDevice,
+                              ctx->stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int32_t handle = ctx->next_handle++;
+    ctx->domains[handle] = std::move(entry);
+    *domain = handle;
+  });
+}
+
+int32_t pars_gpu_round_trace(pars_gpu_context* ctx, int32_t domain, int32_t round, const pars_particle* particles,
+                             const int64_t* offsets, int32_t integrator, int32_t stage_mode, float step_size, int64_t* next_offsets,
+                             pars_gpu_trace_summary* summary)
+{
+  return guarded(ctx, [&] {
+    auto it = ctx->domains.find(domain);
+    if (it == ctx->domains.end()) throw error(PARS_ERR_NOT_FOUND, "no domain with handle " + std::to_string(domain));
+    auto& d = *it->second;
+    PARS_REQUIRE(round >= 0, "round must be >= 0");
+    const step_rule rule = make_rule(integrator, stage_mode, step_size);
+    const int nblocks = d.ranks;
+    round_plan plan;
+    if (particles)
+    {
+      PARS_REQUIRE(offsets, "offsets are required with host particles");
+      const long long count = offsets[nblocks] - offsets[0];
+      PARS_REQUIRE(count >= 0, "offsets must be non-decreasing");
+      plan.count = count;
+      plan.block_count.assign(nblocks, 0);
+      plan.block_max.assign(nblocks, 0);
+      std::vector<int> block_of(std::max<long long>(count, 1));
+      for (int b = 0; b < nblocks; ++b)
+      {
+        const long long begin = offsets[b] - offsets[0], end = offsets[b + 1] - offsets[0];
+        PARS_REQUIRE(end >= begin, "offsets must be non-decreasing");
+        plan.block_count[b] = end - begin;
+        for (long long i = begin; i < end; ++i)
+        {
+          block_of[i] = b;
+          plan.block_max[b] = std::max(plan.block_max[b], particles[offsets[0] + i].remaining_iterations);
+        }
+      }
+      ctx->particles_in.reserve(checked_bytes(std::max<long long>(count, 1), sizeof(pars_particle)));
+      ctx->block_of.reserve(checked_bytes(std::max<long long>(count, 1), sizeof(int)));
+      if (count > 0)
+      {
+        PARS_CUDA(cudaMemcpyAsync(ctx->particles_in.get(), particles + offsets[0], sizeof(pars_particle) * count,
+                                  cudaMemcpyHostToDevice, ctx->stream));
+        PARS_CUDA(cudaMemcpyAsync(ctx->block_of.get(), block_of.data(), sizeof(int) * count, cudaMemcpyHostToDevice, ctx->stream));
+      }
+    }
+    else
+    {
+      if (ctx->round_serial != ctx->trace_serial || ctx->round_domain != domain || ctx->round_next != round)
+        throw error(PARS_ERR_STATE, "no device-resident particles of round " + std::to_string(round) + " on this domain");
+      plan.count = ctx->round_count;
+      plan.block_count = ctx->round_block_count;
+      plan.block_max = ctx->round_block_max;
+    }
+    if (round == 0) clear_curves(*ctx);
+    ++ctx->trace_serial;
+    const long long batches_before = (long long)ctx->curves.batches.size();
+    const long long vertices_before = ctx->curves.vertex_total;
+    const round_counters counters = tracing_counters(*ctx);
+    PARS_CUDA(cudaMemsetAsync(counters.steps, 0, sizeof(unsigned long long), ctx->stream));
+    if (plan.count > 0)
+      trace_one_round(*ctx, d.blocks, d.device_blocks.as<const trace_block>(), plan, rule, true, round, counters, nullptr);
+    else
+      std::fill(plan.block_count.begin(), plan.block_count.end(), 0);
+    unsigned long long steps = 0;
+    PARS_CUDA(cudaMemcpyAsync(&steps, counters.steps, sizeof(steps), cudaMemcpyDeviceToHost, ctx->stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->round_serial = ctx->trace_serial;
+    ctx->round_domain = domain;
+    ctx->round_next = round + 1;
+    ctx->round_count = plan.count;
+    ctx->round_block_count = plan.block_count;
+    ctx->round_block_max = plan.block_max;
+    if (next_offsets)
+    {
+      next_offsets[0] = 0;
+      for (int b = 0; b < nblocks; ++b) next_offsets[b + 1] = next_offsets[b] + plan.block_count[b];
+    }
+    if (summary)
+    {
+      summary->batches = (long long)ctx->curves.batches.size() - batches_before;
+      summary->vertices = ctx->curves.vertex_total - vertices_before;
+      summary->steps = (long long)steps;
+      summary->rounds = round + 1;
+      summary->padding = 0;
+    }
+  });
+}
+
+int32_t pars_gpu_round_particles(pars_gpu_context* ctx, pars_particle* particles)
+{
+  return guarded(ctx, [&] {
+    if (ctx->round_serial != ctx->trace_serial) throw error(PARS_ERR_STATE, "no round-by-round tracing to read particles from");
+    PARS_REQUIRE(particles || ctx->round_count == 0, "particles is required");
+    if (ctx->round_count > 0)
+    {
+      PARS_CUDA(cudaMemcpyAsync(particles, ctx->particles_in.get(), sizeof(pars_particle) * ctx->round_count, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+      PARS_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
   });
 }
 

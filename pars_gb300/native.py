@@ -106,6 +106,9 @@ SIGNATURES = {
     "pars_gpu_domain_release": [_P, _I32],
     "pars_gpu_domain_create_device": [_P, _P, _P, _P, _I32, ctypes.POINTER(_I32)],
     "pars_gpu_trace_domain": [_P, _I32, _P, _P, _I32, _I32, _F, ctypes.POINTER(TraceSummary)],
+    "pars_gpu_domain_assemble": [_P, _I32, _P, _P, ctypes.POINTER(_I32)],
+    "pars_gpu_round_trace": [_P, _I32, _I32, _P, _P, _I32, _I32, _F, _P, ctypes.POINTER(TraceSummary)],
+    "pars_gpu_round_particles": [_P, _P],
     "pars_gpu_curves_index": [_P],
     "pars_gpu_curves_color": [_P, _I32, _F],
     "pars_gpu_curves_batch_info": [_P, _I64, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I32), ctypes.POINTER(_I32)],
@@ -338,6 +341,35 @@ class Context:
         s = TraceSummary()
         self._call("pars_gpu_trace_domain", domain, _ptr(particles), _ptr(offs), integrator, stage_mode, step, ctypes.byref(s))
         return {"batches": s.batches, "vertices": s.vertices, "steps": s.steps, "rounds": s.rounds}
+
+    def domain_assemble(self, ranks, domain_size, fields):
+        """A domain from per-rank block fields (pars_gpu_domain_assemble)."""
+        h = _I32()
+        d = _i3(domain_size)
+        f = np.ascontiguousarray(fields, np.int32)
+        self._call("pars_gpu_domain_assemble", ranks, _ptr(d), _ptr(f), ctypes.byref(h))
+        return h.value
+
+    def round_trace(self, domain, round_index, particles, offsets, ranks, integrator=RUNGE_KUTTA_4, stage_mode=STAGES_FROZEN,
+                    step=0.01):
+        """One round of every rank (pars_gpu_round_trace).  particles None: the
+        device-resident particles of the previous round.  Returns (summary,
+        next_offsets)."""
+        s = TraceSummary()
+        nxt = np.zeros(ranks + 1, np.int64)
+        if particles is None:
+            p, o = None, None
+        else:
+            particles = np.ascontiguousarray(particles, PARTICLE_DTYPE)
+            offsets = np.ascontiguousarray(offsets, np.int64)
+            p, o = _ptr(particles), _ptr(offsets)
+        self._call("pars_gpu_round_trace", domain, round_index, p, o, integrator, stage_mode, step, _ptr(nxt), ctypes.byref(s))
+        return {"batches": s.batches, "vertices": s.vertices, "steps": s.steps, "rounds": s.rounds}, nxt
+
+    def round_particles(self, count):
+        out = np.zeros(max(count, 1), PARTICLE_DTYPE)
+        self._call("pars_gpu_round_particles", _ptr(out))
+        return out[:count]
 
     def curves_index(self):
         self._call("pars_gpu_curves_index")
