@@ -55,6 +55,10 @@ def parse_args():
     p.add_argument("--serve-cpu-seconds", type=float, default=15.0, help="served workload: CPU reference arm's sample length")
     p.add_argument("--serve-loads", default="0.5,0.9", help="served workload: offered loads as fractions of saturation")
     p.add_argument("--serve-lanes", type=int, default=1, help="served workload: service lanes of the batched arm")
+    p.add_argument("--serve-reply", choices=["curves", "image"], default="image",
+                   help="served workload: what a streamline request returns to the client -- the pars_service reply, "
+                        "an image of the curves ray traced on the GPU (pipeline.cpp:264-337), or every curve buffer")
+    p.add_argument("--serve-image", default="960x540", help="served workload: image size of the image reply")
     p.add_argument("--domain-edge", type=int, default=512, help="domain workload: edge of the cube domain")
     p.add_argument("--domain-seeds", type=int, default=1_000_000, help="domain workload: seeds of the Gaussian mixture")
     p.add_argument("--workload", choices=["ftle", "streamlines", "domain", "pathlines", "serve", "render"], default="ftle",
@@ -463,17 +467,30 @@ def run_serve(args):
     from pars_gb300.requests import encode_settings
     ds, reqs = workloads.served_stream_config(seed=4, requests=args.requests)
     f32 = np.float32
+    image_reply = args.serve_reply == "image"
+    width, height = (int(x) for x in args.serve_image.split("x"))
     messages, specs = [], []
     for r in reqs:
         d = ds[r["dataset"]]
         step = 0.01 if d["kind"] == "abc" else 0.05
         iterations = r["steps"] + (2 if r["kind"] == "streamlines" else 1)
-        specs.append({"kind": r["kind"], "dataset": r["dataset"], "stride": r["stride"], "iterations": iterations, "step": step})
-        messages.append(encode_settings({
+        # camera: the dataset's centre seen along +z from 1.6 extents away (fovy 68)
+        extent = np.array([2 * np.pi] * 3 if d["kind"] == "abc" else [2.0, 1.0, 1.0])
+        centre = extent / 2
+        camera = (float(centre[0]), float(centre[1]), float(-1.6 * extent.max()))
+        radius = float(f32(0.1) * f32(extent[0] / (d["edge"] - 1)))
+        specs.append({"kind": r["kind"], "dataset": r["dataset"], "stride": r["stride"], "iterations": iterations, "step": step,
+                      "camera": camera, "radius": radius})
+        message = {
             "mode": r["kind"], "dataset_filepath": d["name"], "seed_generation_stride": [r["stride"]] * 3,
             "seed_generation_iterations": iterations,
             "particle_tracing_integrator": "runge_kutta_4", "particle_tracing_step_size": step,
-            "color_generation_mode": "hsv_constant_s", "color_generation_free_parameter": 0.75}))
+            "color_generation_mode": "hsv_constant_s", "color_generation_free_parameter": 0.75}
+        if image_reply and r["kind"] == "streamlines":
+            message.update({"raytracing_camera_position": list(camera), "raytracing_camera_forward": [0.0, 0.0, 1.0],
+                            "raytracing_camera_up": [0.0, 1.0, 0.0], "raytracing_image_size": [width, height],
+                            "raytracing_streamline_radius": radius, "raytracing_iterations": 1})
+        messages.append(encode_settings(message))
 
     # Datasets on the device (for the service) and in pinned host memory (for
     # the plain path, which uploads the request's field every time).
@@ -503,6 +520,7 @@ def run_serve(args):
     cbuf = torch.empty(cap_vertices * 4, dtype=torch.float32, pin_memory=True)
     ibuf = torch.empty(cap_vertices, dtype=torch.int32, pin_memory=True)
     fbuf = torch.empty(cap_voxels, dtype=torch.float32, pin_memory=True)
+    frame = torch.empty(width * height * 4, dtype=torch.uint8, pin_memory=True)
     collected = {"bytes": 0}
 
     def plain_request(ctx, k):
@@ -515,10 +533,21 @@ def run_serve(args):
             summary = ctx.trace(h, seeds, native.RUNGE_KUTTA_4, native.STAGES_RESAMPLED, s["step"])
             ctx.curves_index()
             ctx.curves_color("hsv_constant_s", 0.75)
-            for b in range(summary["batches"]):
-                nv, ni, _, _ = ctx.batch_info(b)
-                ctx._call("pars_gpu_curves_download", b, vbuf.data_ptr(), cbuf.data_ptr(), ibuf.data_ptr())
-                collected["bytes"] += 32 * nv + 4 * ni
+            if image_reply:
+                # pipeline.cpp:264-337: the curves ray traced, the image to the client
+                ctx.ray_tracer_set_image_size(width, height)
+                ctx.ray_tracer_set_camera(s["camera"], (0.0, 0.0, 1.0), (0.0, 1.0, 0.0))
+                ctx.ray_tracer_clear_volume()
+                ctx.ray_tracer_set_integral_curves(s["radius"])
+                ctx.ray_tracer_trace(1)
+                size = np.zeros(2, np.int32)
+                ctx._call("pars_gpu_ray_tracer_serialize", frame.data_ptr(), size.ctypes.data)
+                collected["bytes"] += width * height * 4
+            else:
+                for b in range(summary["batches"]):
+                    nv, ni, _, _ = ctx.batch_info(b)
+                    ctx._call("pars_gpu_curves_download", b, vbuf.data_ptr(), cbuf.data_ptr(), ibuf.data_ptr())
+                    collected["bytes"] += 32 * nv + 4 * ni
             steps = summary["steps"]
         else:
             fm, steps = ctx.flow_map_generate(h, s["iterations"], float(f32(1.0) / f32(s["stride"])), native.RUNGE_KUTTA_4,
@@ -551,7 +580,10 @@ def run_serve(args):
 
     def collect(svc, ticket):
         info = svc.info(ticket)
-        if info.kind == 0:
+        if info.kind == 0 and image_reply:
+            w, hgt = svc.image_into(ticket, frame.data_ptr())
+            collected["bytes"] += w * hgt * 4
+        elif info.kind == 0:
             for b in range(info.batches):
                 nv, ni = svc.batch_into(ticket, b, vbuf.data_ptr(), cbuf.data_ptr(), ibuf.data_ptr())
                 collected["bytes"] += 32 * nv + 4 * ni
@@ -664,10 +696,13 @@ def run_serve(args):
 
     if "cpu" in arms:
         results["cpu_reference"] = run_cpu_reference(specs, host_fields, args.serve_cpu_seconds)
+    reply = (f"streamline requests reply with a {width}x{height} image of their curves ray traced on the GPU (the "
+             "pars_service reply)" if image_reply else "streamline requests return every curve buffer")
     line = {"workload": f"served_{len(messages)}: {len(messages)} requests (seed 4), 70% streamlines / 30% FTLE on "
                         f"{len(ds)} ABC / double-gyre fields (edge 64-512), seeds 1k-2M (streamlines <= 16384), "
-                        "200-2000 RK4 steps, Poisson arrivals; results collected into pinned host buffers",
-            "datasets": ds}
+                        f"200-2000 RK4 steps, Poisson arrivals; {reply}, FTLE requests their FTLE field; results "
+                        "collected into pinned host buffers",
+            "reply": args.serve_reply, "datasets": ds}
     line.update(results)
     if "plain" in results and "batched" in results:
         line["throughput_ratio_at_saturation"] = (results["batched"]["saturation_requests_per_s"] /
@@ -710,13 +745,13 @@ def launcher_check(args):
 
 def gather_peaks(ctx):
     """Measured gather ceilings of this GPU (GB/s of 16-byte loads delivered
-    to registers; best of three per case): L1-resident (32 KiB) and
+    to registers; best of two per case): L1-resident (32 KiB) and
     L2-resident (64 MiB) buffers, coalesced 512-byte warp requests, one random
     sector per lane, and eight-corner cell gathers."""
     out = {}
     for size, level in ((32 << 10, "l1"), (64 << 20, "l2")):
         for pattern in ("coalesced", "random", "cells"):
-            out[f"{level}_{pattern}"] = max(ctx.gather_peak(size, pattern) for _ in range(3)) / 1e9
+            out[f"{level}_{pattern}"] = max(ctx.gather_peak(size, pattern) for _ in range(2)) / 1e9
     return out
 
 

@@ -2,12 +2,13 @@
 # Builds oracle/_ref/libpars_ref.so: the reference's own hot-path sources,
 # compiled unmodified from the reference checkout, against the stand-ins in
 # oracle/ref_shim/include and the reference's vendored Eigen 3.3.7.
-# Usage: oracle/build_ref.sh [reference-root]   (default /root/reference)
+# Usage: oracle/build_ref.sh [reference-root]
+# (default: $PARS_REFERENCE, else a `reference` directory beside the repository)
 # Default x86-64 code generation (SSE2, no FMA) matches the reference build
 # flags (pa/CMakeLists.txt:37-43).
 set -e
-REF=${1:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${1:-${PARS_REFERENCE:-$(dirname "$(dirname "$HERE")")/reference}}
 OUT="$HERE/_ref"
 [ -d "$REF/pa/source" ] || { echo "reference sources not found under $REF" >&2; exit 1; }
 mkdir -p "$OUT"

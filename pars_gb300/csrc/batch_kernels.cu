@@ -236,6 +236,14 @@ const variant variants[batch_classes][4] = {
 }
 
 int batch_variant_count() { return 4; }
+
+int batch_resident_warps(pars_gpu_context& ctx, int job_class, int v)
+{
+  const variant& var = variants[job_class][v];
+  int& per_sm = ctx.batch_ctas_per_sm[job_class][v];
+  if (per_sm < 0) PARS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, var.kernel, var.threads, 0));
+  return per_sm * var.threads / 32;
+}
 int batch_variant_threads(int v) { return variants[0][v].threads; }
 int batch_pool_seeds() { return pool_seeds; }
 

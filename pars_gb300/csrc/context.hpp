@@ -381,6 +381,8 @@ struct batch_job_device
 // Job classes of the batched engine: each class runs in its own launch.
 enum batch_class { batch_steady = 0, batch_unsteady = 1, batch_frozen = 2, batch_classes = 3 };
 int  batch_variant_count();
+// Resident warps per SM of a job class's launch shape.
+int  batch_resident_warps(pars_gpu_context& ctx, int job_class, int variant);
 int  batch_variant_threads(int variant);
 int  batch_pool_seeds();
 // job_class: batch_steady, batch_unsteady or batch_frozen.

@@ -760,6 +760,14 @@ class Service:
         self._check(self.lib.pars_gpu_service_add_volume(self.handle, name.encode(), _ptr(v), _ptr(s), _ptr(o), _ptr(sp)),
                     "pars_gpu_service_add_volume")
 
+    def image_into(self, ticket, rgba_ptr):
+        """Copies the request's image to a host address (width * height * 4
+        bytes); returns (width, height), (0, 0) without an image."""
+        size = np.zeros(2, np.int32)
+        self._check(self.lib.pars_gpu_service_result_image(self.handle, ticket, rgba_ptr, _ptr(size)),
+                    "pars_gpu_service_result_image")
+        return int(size[0]), int(size[1])
+
     def image(self, ticket):
         """The request's image, [height, width, 4] uint8 (None without one)."""
         size = np.zeros(2, np.int32)
