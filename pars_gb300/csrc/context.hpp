@@ -217,6 +217,9 @@ struct pars_gpu_context
                                           slot_layouts, curve_bounds, color_specs;
   pars::device_buffer                     ftle;
   long long                               ftle_count = 0;
+  // asynchronous rounds: segment table, vertex chunks, round order
+  pars::device_buffer                     async_segments, async_chunks, async_counters, async_order, async_positions,
+                                          async_cursor;
   // round-by-round tracing (pars_gpu_round_trace): the next round's
   // particles stay in particles_in / block_of; their per-block counts and
   // largest remaining_iterations, the round they belong to, and the tracing
@@ -239,6 +242,7 @@ struct pars_gpu_context
   // RK4 / Euler, re-sampled general schemes)
   // and the device's SM count, queried once
   int                                     trace_ctas_per_sm[3] = {-1, -1, -1};
+  int                                     async_ctas_per_sm[3] = {-1, -1, -1};
   int                                     sm_count = 0;
   // batched engine: resident CTAs per SM per job class and launch shape
   int                                     batch_ctas_per_sm[3][4] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}, {-1, -1, -1, -1}};
@@ -319,6 +323,64 @@ struct trace_launch
   unsigned long long*  next;          // pool counter (zero before the launch)
 };
 void launch_trace(pars_gpu_context& ctx, const trace_launch& a);
+
+// Asynchronous rounds: every round of a partitioned domain traced in one
+// persistent launch.  A segment is one particle's trace through one block in
+// one round; the launch starts with the seeds as round-0 segments, and a
+// particle that leaves its block through a face with a neighbour appends its
+// continuation (round + 1, the neighbour's block) to the segment table, where
+// any lane picks it up at once.  Vertices go to chunks of async_chunk
+// vertices taken from a pool and linked per segment; the rounds' order and
+// batches are rebuilt afterwards.
+constexpr int async_chunk = 32;
+constexpr int async_slab = 64;      // chunks a warp takes from the pool at once
+constexpr int async_claims = 32;    // segment ids a warp takes at once
+enum async_counter { async_head = 0, async_alloc = 1, async_done = 2, async_chunks = 3, async_steps = 4, async_counters = 5 };
+enum async_error { async_ok = 0, async_segments_full = 1, async_chunks_full = 2, async_wait_limit = 3 };
+struct async_launch
+{
+  const trace_block*  blocks;
+  step_rule           rule;
+  pars_particle*      seg_particle;     // segment start state
+  int*                seg_block;
+  int*                seg_round;
+  long long*          seg_parent;       // the segment it continues (-1: a seed)
+  int*                seg_ready;        // 1 once the record is written
+  int*                seg_written;      // vertices written (slots of the reference's layout)
+  int*                seg_kept;         // of them not invalid
+  int*                seg_first_chunk;
+  long long           capacity;         // segments
+  float4*             chunks;           // async_chunk vertices each
+  int*                chunk_next;
+  long long           chunk_capacity;
+  unsigned long long* counters;         // async_counter
+  int*                error;            // async_error
+};
+// Launches the persistent kernel; returns its warps (each may leave part of a
+// chunk slab unused).
+long long launch_async_trace(pars_gpu_context& ctx, const async_launch& a, bool count_only = false);
+// Round-0 segments from ctx.particles_in / block_of (count particles).
+void launch_async_seed(pars_gpu_context& ctx, const async_launch& a, const pars_particle* particles, const int* block_of,
+                       long long count);
+// Histogram of segment rounds (rounds_cap bins) and the largest round.
+void launch_round_histogram(pars_gpu_context& ctx, const int* seg_round, long long count, int rounds_cap, int* histogram,
+                            int* max_round);
+// Segment ids grouped by round: ids[first[r] + k] for the k-th segment of round r met (any order).
+void launch_round_scatter(pars_gpu_context& ctx, const int* seg_round, long long count, const long long* first, int* cursor,
+                          unsigned int* ids);
+// key[k] = (seg_block[ids[k]] << 40) | position[seg_parent[ids[k]]] for a round's segments (the
+// segment's own id for seeds).
+void launch_round_keys(pars_gpu_context& ctx, const unsigned int* ids, long long n, const int* seg_block, const long long* seg_parent,
+                       const long long* position, unsigned long long* keys);
+// position[ids[k]] = first + k.
+void launch_round_positions(pars_gpu_context& ctx, const unsigned int* ids, long long n, long long first, long long* position);
+// Per (round, block): segments and largest remaining_iterations, stats[2 * (round * blocks + block) + {0, 1}];
+// kept_ordered[g] = seg_kept[order[g]].
+void launch_round_stats(pars_gpu_context& ctx, const unsigned int* order, long long n, const int* seg_round, const int* seg_block,
+                        const pars_particle* seg_particle, const int* seg_kept, int blocks, int* stats, int* kept_ordered);
+// Copies each segment's kept vertices (chunk by chunk) to out + offsets[g], in the order `order`.
+void launch_async_assemble(pars_gpu_context& ctx, const async_launch& a, const unsigned int* order, const long long* offsets,
+                           long long n, float4* out);
 void launch_compact_vertices(pars_gpu_context& ctx, const float4* slots, const slot_layout* block_slots, const int* block_of,
                              const int* written,
                              const long long* offsets, long long count, float4* out);

@@ -562,6 +562,198 @@ void run_rounds(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, c
   }
 }
 
+// ---- Asynchronous rounds -------------------------------------------------------------
+// Every round of a partitioned domain in one persistent launch (async_launch,
+// trace_kernels.cu): no round waits for the slowest particle of the previous
+// one.  The rounds' order is rebuilt afterwards exactly as the round loop
+// forms it (a block's particles of round r + 1 ordered by the sender's
+// position in round r), then compute_round_info's batches per (round, block),
+// prune, and the packed vertices.  Returns false, with nothing kept, when the
+// segment table, the vertex chunks or the round histogram overflowed, a wait
+// ran out, or the buffers would take more than a quarter of the free device
+// memory: the caller then traces round by round.
+bool run_rounds_async(pars_gpu_context& ctx, const std::vector<trace_block>& blocks, const trace_block* device_blocks,
+                      long long count, const std::vector<long long>& block_count, const std::vector<int>& block_max,
+                      const step_rule& rule, pars_gpu_trace_summary* summary)
+{
+  const int nblocks = int(blocks.size());
+  if (count <= 0) return false;
+  async_launch a {};
+  a.blocks = device_blocks;
+  a.rule = rule;
+  long long vertex_bound = 0;   // sum of remaining_iterations over the seeds, at most
+  for (int b = 0; b < nblocks; ++b) vertex_bound += block_count[b] * std::max(1, block_max[b]);
+  const long long warps = launch_async_trace(ctx, a, true);
+  const long long capacity = std::min<long long>(std::max<long long>(16 * count, 1 << 16), (1LL << 31) - 1);
+  // every segment's vertices in whole chunks, plus the slabs warps leave unused
+  const long long chunk_capacity = (vertex_bound + capacity) / async_chunk + capacity + async_slab * (warps + 1);
+  if (chunk_capacity > (1LL << 31) - 1) return false;
+  auto align = [](std::size_t b) { return (b + 255) & ~std::size_t(255); };
+  const std::size_t seg_bytes = align(sizeof(pars_particle) * capacity) + 6 * align(sizeof(int) * capacity) +
+                                align(sizeof(long long) * capacity);
+  const std::size_t chunk_bytes = align(sizeof(float4) * async_chunk * chunk_capacity) + align(sizeof(int) * chunk_capacity);
+  if (seg_bytes > ctx.async_segments.bytes() || chunk_bytes > ctx.async_chunks.bytes())
+  {
+    std::size_t free_bytes = 0, total_bytes = 0;
+    PARS_CUDA(cudaMemGetInfo(&free_bytes, &total_bytes));
+    const std::size_t have = ctx.async_segments.bytes() + ctx.async_chunks.bytes();
+    if (seg_bytes + chunk_bytes > have + free_bytes / 4) return false;
+  }
+
+  ctx.async_segments.reserve(seg_bytes);
+  ctx.async_chunks.reserve(chunk_bytes);
+  ctx.async_counters.reserve(sizeof(unsigned long long) * async_counters + 256);
+  char* sp = ctx.async_segments.as<char>();
+  auto carve = [&](std::size_t bytes) { char* p = sp; sp += align(bytes); return p; };
+  a.seg_particle = reinterpret_cast<pars_particle*>(carve(sizeof(pars_particle) * capacity));
+  a.seg_block = reinterpret_cast<int*>(carve(sizeof(int) * capacity));
+  a.seg_round = reinterpret_cast<int*>(carve(sizeof(int) * capacity));
+  a.seg_ready = reinterpret_cast<int*>(carve(sizeof(int) * capacity));
+  a.seg_written = reinterpret_cast<int*>(carve(sizeof(int) * capacity));
+  a.seg_kept = reinterpret_cast<int*>(carve(sizeof(int) * capacity));
+  a.seg_first_chunk = reinterpret_cast<int*>(carve(sizeof(int) * capacity));
+  a.seg_parent = reinterpret_cast<long long*>(carve(sizeof(long long) * capacity));
+  a.capacity = capacity;
+  a.chunks = ctx.async_chunks.as<float4>();
+  a.chunk_next = reinterpret_cast<int*>(ctx.async_chunks.as<char>() + align(sizeof(float4) * async_chunk * chunk_capacity));
+  a.chunk_capacity = chunk_capacity;
+  a.counters = ctx.async_counters.as<unsigned long long>();
+  a.error = reinterpret_cast<int*>(a.counters + async_counters);
+
+  // the seeds as round-0 segments; nothing else published
+  PARS_CUDA(cudaMemsetAsync(a.seg_ready, 0, sizeof(int) * capacity, ctx.stream));
+  PARS_CUDA(cudaMemsetAsync(ctx.async_counters.get(), 0, sizeof(unsigned long long) * async_counters + sizeof(int), ctx.stream));
+  const unsigned long long allocated0 = (unsigned long long)count;
+  PARS_CUDA(cudaMemcpyAsync(a.counters + async_alloc, &allocated0, sizeof(allocated0), cudaMemcpyHostToDevice, ctx.stream));
+  launch_async_seed(ctx, a, ctx.particles_in.as<const pars_particle>(), nblocks > 1 ? ctx.block_of.as<const int>() : nullptr, count);
+  launch_async_trace(ctx, a);
+  unsigned long long counters[async_counters + 1] = {};
+  PARS_CUDA(cudaMemcpyAsync(counters, a.counters, sizeof(unsigned long long) * async_counters + sizeof(int), cudaMemcpyDeviceToHost,
+                            ctx.stream));
+  PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+  int error = 0;
+  std::memcpy(&error, counters + async_counters, sizeof(int));
+  if (error != async_ok) return false;
+  const long long n = (long long)counters[async_alloc];
+
+  // rounds: histogram, then each round's segments sorted by (block, the
+  // sender's position in the previous round), positions concatenated
+  constexpr int rounds_cap = 65536;
+  ctx.async_cursor.reserve(sizeof(int) * (2 * rounds_cap + 1));
+  int* histogram = ctx.async_cursor.as<int>();
+  int* max_round = histogram + rounds_cap;
+  int* cursor = max_round + 1;
+  PARS_CUDA(cudaMemsetAsync(histogram, 0, sizeof(int) * (2 * rounds_cap + 1), ctx.stream));
+  launch_round_histogram(ctx, a.seg_round, n, rounds_cap, histogram, max_round);
+  int rounds = 0;
+  PARS_CUDA(cudaMemcpyAsync(&rounds, max_round, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+  PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+  ++rounds;
+  if (rounds > rounds_cap) return false;
+  std::vector<int> per_round(rounds);
+  PARS_CUDA(cudaMemcpyAsync(per_round.data(), histogram, sizeof(int) * rounds, cudaMemcpyDeviceToHost, ctx.stream));
+  PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+  std::vector<long long> first(rounds + 1, 0);
+  long long widest = 0;
+  for (int r = 0; r < rounds; ++r) { first[r + 1] = first[r] + per_round[r]; widest = std::max<long long>(widest, per_round[r]); }
+
+  ctx.async_order.reserve(sizeof(unsigned int) * 2 * n + sizeof(long long) * (rounds + 1) + 256);
+  unsigned int* grouped = ctx.async_order.as<unsigned int>();
+  unsigned int* order = grouped + n;
+  long long* device_first = reinterpret_cast<long long*>(ctx.async_order.as<char>() + align(sizeof(unsigned int) * 2 * n));
+  ctx.async_positions.reserve(sizeof(long long) * (n + 1));
+  long long* position = ctx.async_positions.as<long long>();
+  PARS_CUDA(cudaMemcpyAsync(device_first, first.data(), sizeof(long long) * (rounds + 1), cudaMemcpyHostToDevice, ctx.stream));
+  launch_round_scatter(ctx, a.seg_round, n, device_first, cursor, grouped);
+  ctx.exit_keys.reserve(sizeof(unsigned long long) * widest);
+  ctx.exit_keys_sorted.reserve(sizeof(unsigned long long) * widest);
+  int key_bits = 40;
+  while ((1 << (key_bits - 40)) < nblocks) ++key_bits;
+  for (int r = 0; r < rounds; ++r)
+  {
+    const long long m = per_round[r];
+    if (m == 0) continue;
+    launch_round_keys(ctx, grouped + first[r], m, a.seg_block, a.seg_parent, position, ctx.exit_keys.as<unsigned long long>());
+    sort_pairs(ctx, ctx.exit_keys.as<const unsigned long long>(), ctx.exit_keys_sorted.as<unsigned long long>(), grouped + first[r],
+               order + first[r], m, key_bits);
+    launch_round_positions(ctx, order + first[r], m, first[r], position);
+  }
+
+  // per (round, block): segments and largest remaining_iterations; kept
+  // vertices in that order, and their offsets in the packed buffer
+  ctx.block_max.reserve(sizeof(int) * 2 * (std::size_t)rounds * nblocks);
+  int* stats = ctx.block_max.as<int>();
+  PARS_CUDA(cudaMemsetAsync(stats, 0, sizeof(int) * 2 * (std::size_t)rounds * nblocks, ctx.stream));
+  ctx.kept.reserve(sizeof(int) * n);
+  ctx.offsets.reserve(sizeof(long long) * (n + 1));
+  launch_round_stats(ctx, order, n, a.seg_round, a.seg_block, a.seg_particle, a.seg_kept, nblocks, stats, ctx.kept.as<int>());
+  exclusive_sum(ctx, ctx.kept.as<int>(), ctx.offsets.as<long long>(), n);
+  std::vector<int> host_stats(2 * (std::size_t)rounds * nblocks);
+  PARS_CUDA(cudaMemcpyAsync(host_stats.data(), stats, sizeof(int) * host_stats.size(), cudaMemcpyDeviceToHost, ctx.stream));
+  PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+
+  // compute_round_info's batches of every (round, block), as positions
+  struct pending_batch { long long first, last; int rank, round; };
+  std::vector<pending_batch> pending;
+  long long g = 0;
+  for (int r = 0; r < rounds; ++r)
+    for (int b = 0; b < nblocks; ++b)
+    {
+      const long long m = host_stats[2 * ((std::size_t)r * nblocks + b)];
+      const int maximum = host_stats[2 * ((std::size_t)r * nblocks + b) + 1];
+      if (m == 0) continue;
+      const long long max_vertices = std::numeric_limits<int32_t>::max() / 16;
+      const long long ppc = max_vertices / std::max(1, maximum);
+      PARS_REQUIRE(ppc > 0, "remaining_iterations exceeds the batch vertex limit");
+      const long long curve_count = 1 + m / ppc;
+      for (long long k = 0; k < curve_count; ++k)
+        pending.push_back({g + std::min(m, k * ppc), g + std::min(m, (k + 1) * ppc), b, r});
+      g += m;
+    }
+  PARS_REQUIRE(g == n, "round statistics do not cover the segments");
+  std::vector<long long> positions;
+  positions.reserve(pending.size() * 2 + 1);
+  for (auto& p : pending) { positions.push_back(p.first); positions.push_back(p.last); }
+  positions.push_back(n);
+  std::vector<long long> boundary(positions.size());
+  ctx.boundary_positions.reserve(sizeof(long long) * positions.size());
+  ctx.boundary_offsets.reserve(sizeof(long long) * positions.size());
+  PARS_CUDA(cudaMemcpyAsync(ctx.boundary_positions.get(), positions.data(), sizeof(long long) * positions.size(), cudaMemcpyHostToDevice,
+                            ctx.stream));
+  launch_gather_offsets(ctx, ctx.offsets.as<const long long>(), ctx.boundary_positions.as<const long long>(), (long long)positions.size(),
+                        ctx.boundary_offsets.as<long long>());
+  PARS_CUDA(cudaMemcpyAsync(boundary.data(), ctx.boundary_offsets.get(), sizeof(long long) * boundary.size(), cudaMemcpyDeviceToHost,
+                            ctx.stream));
+  PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+  const long long total_vertices = boundary.back();
+
+  clear_curves(ctx);
+  ++ctx.trace_serial;
+  auto& curves = ctx.curves;
+  grow_curves(ctx, total_vertices);
+  launch_async_assemble(ctx, a, order, ctx.offsets.as<const long long>(), n, curves.vertices.as<float4>());
+  for (std::size_t k = 0; k < pending.size(); ++k)
+  {
+    curves_batch batch;
+    batch.vertex_offset = boundary[2 * k];
+    batch.vertex_count = boundary[2 * k + 1] - boundary[2 * k];
+    batch.rank = pending[k].rank;
+    batch.round = pending[k].round;
+    curves.batches.push_back(batch);
+  }
+  curves.vertex_total = total_vertices;
+  PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+  if (summary)
+  {
+    summary->batches = (long long)curves.batches.size();
+    summary->vertices = total_vertices;
+    summary->steps = (long long)counters[async_steps];
+    summary->rounds = rounds;
+    summary->padding = 0;
+  }
+  return true;
+}
+
 // Single block: one trace_block with no neighbours, kept in a small device array.
 const trace_block* single_block(pars_gpu_context& ctx, const field_entry& f, std::vector<trace_block>& blocks)
 {
@@ -1108,7 +1300,10 @@ int32_t pars_gpu_trace_domain(pars_gpu_context* ctx, int32_t domain, const pars_
       PARS_CUDA(cudaMemcpyAsync(ctx->particles_in.get(), particles + seed_offsets[0], sizeof(pars_particle) * count, cudaMemcpyHostToDevice, ctx->stream));
       PARS_CUDA(cudaMemcpyAsync(ctx->block_of.get(), block_of.data(), sizeof(int) * count, cudaMemcpyHostToDevice, ctx->stream));
     }
-    run_rounds(*ctx, d.blocks, d.device_blocks.as<const trace_block>(), count, block_count, block_max, rule, true, summary);
+    // one persistent launch over all rounds; round by round when its
+    // buffers do not fit or overflow
+    if (!run_rounds_async(*ctx, d.blocks, d.device_blocks.as<const trace_block>(), count, block_count, block_max, rule, summary))
+      run_rounds(*ctx, d.blocks, d.device_blocks.as<const trace_block>(), count, block_count, block_max, rule, true, summary);
   });
 }
 
