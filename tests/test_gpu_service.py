@@ -252,3 +252,40 @@ def test_requests_with_the_other_integrators_equal_the_context_path(service, ctx
     assert np.array_equal(got_ftle, expected_ftle, equal_nan=True)
     ctx.release_field(fm)
     ctx.release_field(h)
+
+
+def test_requests_admitted_mid_flight_equal_their_results_alone(service):
+    """Continuous admission: while a long FTLE request runs on one lane, the
+    requests submitted after it has started are admitted by the other lane
+    and run at the same time on the device; each gives bit for bit what it
+    gives alone."""
+    import time
+    from pars_gb300.requests import encode_settings
+    long_request = {"mode": "ftle", "dataset_filepath": "abc40", "seed_generation_stride": [1, 1, 1],
+                    "seed_generation_iterations": 20001, "particle_tracing_integrator": "runge_kutta_4",
+                    "particle_tracing_step_size": 0.001}
+    reqs = _requests()
+    t_long = service.submit(encode_settings(long_request))
+    t0 = time.perf_counter()
+    while service.wait(t_long, 0) == 0:      # queued: wait until it runs
+        time.sleep(0.0005)
+    submitted, tickets = [], []
+    for r in reqs:
+        submitted.append(time.perf_counter())
+        tickets.append(service.submit(encode_settings(r)))
+    for t in tickets + [t_long]:
+        assert service.wait(t) == 2
+    long_info = service.info(t_long)
+    long_end = t0 + long_info.latency_ms / 1e3
+    started = [s + service.info(t).queue_ms / 1e3 for s, t in zip(submitted, tickets)]
+    assert sum(s < long_end for s in started) >= 1, "no request started while the long one ran"
+    mixed = [_result(service, t, "ftle" if "ftle" in r["mode"] else "streamlines") for t, r in zip(tickets, reqs)]
+    for t in tickets + [t_long]:
+        service.release(t)
+    for r, m in zip(reqs, mixed):
+        kind = "ftle" if "ftle" in r["mode"] else "streamlines"
+        t = service.submit(encode_settings(r))
+        assert service.wait(t) == 2
+        alone = _result(service, t, kind)
+        service.release(t)
+        assert _same(alone, m, kind), r
