@@ -473,6 +473,23 @@ int32_t pars_gpu_service_release     (pars_gpu_service* service, int64_t ticket)
 int32_t pars_gpu_service_profile_enable(pars_gpu_service* service, int32_t enable);
 int32_t pars_gpu_service_profile_get   (pars_gpu_service* service, const char* name, double* milliseconds, int64_t* count);
 
+/* ---- the service's transport (pars_service's ZeroMQ PAIR socket,
+ * pars/source/service.cpp:20-69) ------------------------------------------------
+ * ZMTP 3.0 (ZeroMQ RFC 23) over TCP with the NULL mechanism, as a PAIR socket,
+ * without libzmq, so the reference's clients (a ZeroMQ PAIR socket that
+ * connects and sends `settings` messages) talk to the service unchanged.
+ * pars_gpu_transport_listen binds a TCP listener on an IPv4 address and port
+ * (0: any free port, returned in *bound_port) and returns it in *listener.
+ * pars_gpu_service_serve accepts one peer on it, answers each message with
+ * the request's `image` message (pars_gpu_image_encode; width and height 0
+ * when the request made no image or failed), and returns once the peer
+ * closes or max_requests messages (<= 0: no limit) were answered; *served
+ * receives the count.  It blocks the calling thread; call it again for the
+ * next peer.  Host-only; the service does the GPU work. */
+int32_t pars_gpu_transport_listen(const char* address, int32_t port, int32_t* bound_port, int64_t* listener);
+int32_t pars_gpu_transport_close (int64_t listener);
+int32_t pars_gpu_service_serve   (pars_gpu_service* service, int64_t listener, int64_t max_requests, int64_t* served);
+
 /* ---- allocation-free FTLE --------------------------------------------------------
  * No counterpart in the reference.  For callers that may not allocate device
  * memory: plugins running inside a host application that owns the GPU's

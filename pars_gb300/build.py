@@ -17,7 +17,8 @@ BUILD = os.path.join(HERE, "_build")
 LIBRARY = os.path.join(HERE, "libpars_gpu.so")
 
 SOURCES = ["pars_gpu.cu", "trace_kernels.cu", "curve_kernels.cu", "ftle_kernels.cu", "field_kernels.cu", "batch_kernels.cu",
-           "service.cu", "render_kernels.cu", "field_io.cu", "vtk_export.cu", "calibrate.cu"]
+           "service.cu", "render_kernels.cu", "field_io.cu", "vtk_export.cu", "calibrate.cu",
+           "transport.cu"]
 # Per-source flags: the ray tracer rounds every operation separately (no FMA
 # contraction), as its CPU restatement does.
 SOURCE_FLAGS = {"render_kernels.cu": ["--fmad=false"]}

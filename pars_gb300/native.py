@@ -164,6 +164,9 @@ SIGNATURES = {
     "pars_gpu_profile_get": [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)],
     "pars_gpu_launch_count": [_P, ctypes.POINTER(_I64)],
     "pars_gpu_gather_peak": [_P, _I64, _I32, ctypes.POINTER(ctypes.c_double)],
+    "pars_gpu_transport_listen": [ctypes.c_char_p, _I32, ctypes.POINTER(_I32), ctypes.POINTER(_I64)],
+    "pars_gpu_transport_close": [_I64],
+    "pars_gpu_service_serve": [_P, _I64, _I64, ctypes.POINTER(_I64)],
 }
 _RESTYPES = {"pars_gpu_last_error": ctypes.c_char_p}
 
@@ -559,6 +562,23 @@ class Context:
         return out.value
 
 
+# -- the service's transport -----------------------------------------------------------
+def transport_listen(address="127.0.0.1", port=0):
+    """A TCP listener for pars_gpu_service_serve; returns (listener, port)."""
+    lib = library()
+    bound, handle = _I32(), _I64()
+    status = lib.pars_gpu_transport_listen(address.encode(), port, ctypes.byref(bound), ctypes.byref(handle))
+    if status:
+        raise ParsGpuError(status, "pars_gpu_transport_listen")
+    return handle.value, bound.value
+
+
+def transport_close(listener):
+    status = library().pars_gpu_transport_close(listener)
+    if status:
+        raise ParsGpuError(status, "pars_gpu_transport_close")
+
+
 # -- field files (pa::data_io) ----------------------------------------------------------
 def raw_write(path, data, spacing):
     """Writes a dataset: data [X, Y, Z, 3] (vector field) or [X, Y, Z] (scalar)."""
@@ -759,6 +779,13 @@ class Service:
         s, o, sp = _i3(v.shape), _f3(offset), _f3(spacing)
         self._check(self.lib.pars_gpu_service_add_volume(self.handle, name.encode(), _ptr(v), _ptr(s), _ptr(o), _ptr(sp)),
                     "pars_gpu_service_add_volume")
+
+    def serve(self, listener, max_requests=0):
+        """Answers one ZMTP PAIR peer on `listener` (pars_gpu_service_serve);
+        returns the number of requests answered."""
+        n = _I64()
+        self._check(self.lib.pars_gpu_service_serve(self.handle, listener, max_requests, ctypes.byref(n)), "pars_gpu_service_serve")
+        return n.value
 
     def image_into(self, ticket, rgba_ptr):
         """Copies the request's image to a host address (width * height * 4
