@@ -355,6 +355,36 @@ int32_t pars_gpu_batch_variants(pars_gpu_context* context, int32_t* count);
  * unsteady, 2 frozen), -1 if not tuned yet. */
 int32_t pars_gpu_batch_tuned   (pars_gpu_context* context, int32_t job_class, int32_t* variant, int32_t* threads);
 
+/* ---- continuous batched advection --------------------------------------------------
+ * The batched engine above with a job table that grows while it runs: jobs are
+ * submitted at any time and join at the next horizon launch.  Each
+ * pars_gpu_engine_advance runs one launch per job class with work, in which
+ * every warp takes at most `iterations` steps and then parks its particles and
+ * the rest of its seed pool in device memory; the next launch resumes them
+ * before it starts the jobs submitted meanwhile.  A job's results (end
+ * positions, step counts) are the same bits as pars_gpu_batch_advect's,
+ * however its work is split into launches.  A job's field and output buffers
+ * must stay valid until it is reported done.  Replaces, for a server, the
+ * reference's one-request-at-a-time loop around particle_advector
+ * (pars/source/service.cpp:41-68, pa/source/stages/particle_advector.cpp:74-139):
+ * requests that arrive while others run share the device from the next
+ * horizon on. */
+typedef struct pars_gpu_engine_done
+{
+  int64_t ticket;
+  int64_t steps;     /* particle-steps of the job */
+} pars_gpu_engine_done;
+
+/* Appends a job (same rules as pars_gpu_batch_advect; `steps` is ignored) and
+ * returns its ticket.  The first job of a class tunes the class's launch shape
+ * if the context has not tuned it yet. */
+int32_t pars_gpu_engine_submit (pars_gpu_context* context, const pars_gpu_batch_job* job, int64_t* ticket);
+/* One horizon launch per job class with work (iterations >= 1 steps per warp),
+ * then returns up to `capacity` completed jobs (the rest on later calls) and,
+ * in *open, the jobs submitted and not yet returned. */
+int32_t pars_gpu_engine_advance(pars_gpu_context* context, int32_t iterations, pars_gpu_engine_done* done, int32_t capacity,
+                                int32_t* done_count, int64_t* open);
+
 /* ---- request service (pars_service, pars/source/service.cpp:20-69) ----------------
  * Requests are the reference's binary proto3 `settings` messages
  * (pars/proto/settings.proto).  `mode` is read as the reference reads it:
@@ -368,7 +398,11 @@ int32_t pars_gpu_batch_tuned   (pars_gpu_context* context, int32_t job_class, in
  * The service queues requests as they arrive.  `lanes` worker threads, each
  * with its own CUDA stream, take batches of queued requests of one kind that
  * fit into the device-memory budget (requests arriving while others run are
- * admitted as memory frees up) and run each batch as one launch.  A request's
+ * admitted as memory frees up).  A streamline batch runs as one tracing round
+ * loop; FTLE requests run on the lane's continuous engine, which admits FTLE
+ * requests that arrive while it runs at its next horizon launch and hands out
+ * each request as soon as its own flow map completes
+ * (pars_gpu_service_set_horizon).  A request's
  * results stay in device memory until the client copies them out
  * (pars_gpu_service_result_batch / _result_ftle, into any host buffers; pinned
  * ones copy fastest) and releases the request; held results count against
@@ -424,6 +458,13 @@ int32_t pars_gpu_settings_decode     (const uint8_t* message, int64_t length, pa
 int32_t pars_gpu_service_create      (pars_gpu_service** service, int32_t device, int64_t budget_bytes, int32_t lanes,
                                       int32_t max_batch);
 int32_t pars_gpu_service_destroy     (pars_gpu_service* service);
+/* FTLE requests run through the lane's continuous batched engine
+ * (pars_gpu_engine_advance) with `iterations` steps per warp per launch
+ * (default 1024): between launches finished requests are handed out and FTLE
+ * requests that arrived meanwhile join the running launch sequence.  0 runs
+ * each FTLE batch to completion in one launch instead.  Results are the same
+ * bits either way. */
+int32_t pars_gpu_service_set_horizon (pars_gpu_service* service, int32_t iterations);
 /* Registers a dataset (HOST xyz [X][Y][Z][3], as pars_gpu_field_upload) under `name`. */
 int32_t pars_gpu_service_add_dataset (pars_gpu_service* service, const char* name, const float* xyz, const int32_t shape[3],
                                       const float offset[3], const float size[3], const float spacing[3]);

@@ -20,6 +20,16 @@
 // scheme, any of the eight integrators) keep absolute positions and the
 // reference's arithmetic bit for bit, as flow_map_kernel<true> does, one
 // field sample per step on the lane's cached corners.
+//
+// Horizon launches (HORIZON = true) bound a launch's length so that a host can
+// append jobs between launches (continuous admission): a warp that has taken
+// `iterations` steps parks its state -- its job, its live particles, the
+// unconsumed seeds of its pool and a pool it has taken but not begun -- as one
+// group and leaves (and raises a flag that makes every other warp park within
+// 16 steps); the next launch's warps resume the parked groups first (one
+// each) and then take pools from the same counter.  A particle's
+// arithmetic does not depend on where it runs, so a job's results are the
+// same bits however its work is split into launches.
 #include "context.hpp"
 
 namespace pars
@@ -41,6 +51,20 @@ __device__ __forceinline__ int find_job(const batch_job_device* __restrict__ job
   return lo;
 }
 
+// Device-scope relaxed accesses to the horizon launch's stop flag (PTX
+// ld.relaxed.gpu / st.relaxed.gpu: they bypass the SM's L1, so a flag raised on
+// one SM is seen on the others).
+__device__ __forceinline__ unsigned int load_relaxed(const unsigned int* p)
+{
+  unsigned int v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void store_relaxed(unsigned int* p, unsigned int v)
+{
+  asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
 template <int CLASS>
 struct lane_cache { corner_cache k; };
 template <> struct lane_cache<batch_unsteady> { corner_cache2 k; };
@@ -48,10 +72,10 @@ template <> struct lane_cache<batch_unsteady> { corner_cache2 k; };
 // CLASS batch_steady: re-sampled stages, every job on a steady field (one
 // slice).  batch_unsteady: re-sampled stages, jobs may have several time
 // slices (a steady job works too).  batch_frozen: the frozen scheme.
-template <int THREADS, int MIN_BLOCKS, int CLASS>
+template <int THREADS, int MIN_BLOCKS, int CLASS, bool HORIZON = false>
 __global__ void __launch_bounds__(THREADS, MIN_BLOCKS)
 batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long long total_pools,
-                    unsigned long long* __restrict__ pool_counter)
+                    unsigned long long* __restrict__ pool_counter, const __grid_constant__ batch_horizon_args hz)
 {
   const int lane = threadIdx.x & 31;
   const unsigned lanes_below = (1u << lane) - 1u;
@@ -76,6 +100,42 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
   int rk4 = 1, max_steps = 0;
   slice_clock clock {};
   const step_rule* rule = nullptr;   // frozen jobs: the coefficients, read where they lie
+  // horizon launches: steps this warp has taken
+  int iteration = 0;
+
+  if constexpr (HORIZON)
+  {
+    // resume one parked group (the host launches at least as many warps as
+    // there are groups)
+    unsigned int g = 0;
+    if (lane == 0) g = atomicAdd(hz.in_counter, 1u);
+    g = __shfl_sync(full_mask, g, 0);
+    if (g < unsigned(hz.in_count))
+    {
+      const batch_parked_group G = hz.in_groups[g];
+      job = G.job;
+      const batch_job_device& J = jobs[job];
+      f = J.field; ta = J.time; h = J.rule.h; rk4 = J.rule.rk4; max_steps = J.max_steps; clock = J.clock;
+      rule = &J.rule;
+      pool_next = G.pool_next;
+      pool_end = G.pool_end;
+      pending = G.pending;
+      if (lane < G.count)
+      {
+        const batch_parked_lane& P = hz.in_lanes[(long long)g * 32 + lane];
+        seed = P.seed;
+        steps = P.steps;
+        if constexpr (CLASS == batch_frozen)
+        {
+          pos = P.pos;
+          hist.v = P.hist_v;
+          hist.started = P.started;
+        }
+        else local = local_position {P.ix, P.iy, P.iz, P.ux, P.uy, P.uz, P.lx, P.ly, P.lz};
+        alive = true;
+      }
+    }
+  }
 
   for (;;)
   {
@@ -141,6 +201,51 @@ batch_advect_kernel(const batch_job_device* __restrict__ jobs, int njobs, long l
     {
       if (exhausted) break;
       continue;   // switch to the pending job
+    }
+
+    if constexpr (HORIZON)
+    {
+      // The first warp to reach the horizon raises the launch's stop flag;
+      // the others see it within 16 steps, so the launch ends with every SM
+      // busy to the end instead of waiting for its slowest warp.
+      ++iteration;
+      bool stop = iteration > hz.iterations;
+      if (!stop && (iteration & 15) == 0)
+      {
+        unsigned int flag = 0;
+        if (lane == 0) flag = load_relaxed(hz.stop);
+        stop = __shfl_sync(full_mask, flag, 0) != 0u;
+      }
+      if (stop)
+      {
+        if (lane == 0 && iteration > hz.iterations) store_relaxed(hz.stop, 1u);
+        // park: the group record, then the live lanes' particles in lane order
+        const unsigned live = __ballot_sync(full_mask, alive);
+        unsigned int g = 0;
+        if (lane == 0) g = atomicAdd(hz.out_count, 1u);
+        g = __shfl_sync(full_mask, g, 0);
+        if (alive)
+        {
+          // each class parks only the state it carries
+          batch_parked_lane& P = hz.out_lanes[(long long)g * 32 + __popc(live & lanes_below)];
+          P.seed = seed;
+          P.steps = steps;
+          if constexpr (CLASS == batch_frozen)
+          {
+            P.pos = pos;
+            P.hist_v = hist.v;
+            P.started = hist.started;
+          }
+          else
+          {
+            P.ix = local.ix; P.iy = local.iy; P.iz = local.iz;
+            P.ux = local.ux; P.uy = local.uy; P.uz = local.uz;
+            P.lx = local.lx; P.ly = local.ly; P.lz = local.lz;
+          }
+        }
+        if (lane == 0) hz.out_groups[g] = batch_parked_group {job, __popc(live), pool_next, pool_end, pending};
+        break;
+      }
     }
 
     // ---- one step of every live lane -------------------------------------------
@@ -215,24 +320,21 @@ struct variant
 {
   int threads, min_blocks;
   const void* kernel;
+  const void* horizon_kernel;
 };
+#define PARS_BATCH_VARIANT(T, M, C) {T, M, (const void*)batch_advect_kernel<T, M, C>, (const void*)batch_advect_kernel<T, M, C, true>}
 
 // Launch shapes the autotuner chooses from, per job class: threads per CTA and
 // the minimum resident CTAs per SM that the register allocation must allow.
 const variant variants[batch_classes][4] = {
-  {{64, 1, (const void*)batch_advect_kernel<64, 1, batch_steady>},
-   {128, 1, (const void*)batch_advect_kernel<128, 1, batch_steady>},
-   {128, 5, (const void*)batch_advect_kernel<128, 5, batch_steady>},
-   {256, 1, (const void*)batch_advect_kernel<256, 1, batch_steady>}},
-  {{64, 1, (const void*)batch_advect_kernel<64, 1, batch_unsteady>},
-   {128, 1, (const void*)batch_advect_kernel<128, 1, batch_unsteady>},
-   {128, 3, (const void*)batch_advect_kernel<128, 3, batch_unsteady>},
-   {256, 1, (const void*)batch_advect_kernel<256, 1, batch_unsteady>}},
-  {{64, 1, (const void*)batch_advect_kernel<64, 1, batch_frozen>},
-   {128, 1, (const void*)batch_advect_kernel<128, 1, batch_frozen>},
-   {128, 6, (const void*)batch_advect_kernel<128, 6, batch_frozen>},
-   {256, 1, (const void*)batch_advect_kernel<256, 1, batch_frozen>}},
+  {PARS_BATCH_VARIANT(64, 1, batch_steady), PARS_BATCH_VARIANT(128, 1, batch_steady),
+   PARS_BATCH_VARIANT(128, 5, batch_steady), PARS_BATCH_VARIANT(256, 1, batch_steady)},
+  {PARS_BATCH_VARIANT(64, 1, batch_unsteady), PARS_BATCH_VARIANT(128, 1, batch_unsteady),
+   PARS_BATCH_VARIANT(128, 3, batch_unsteady), PARS_BATCH_VARIANT(256, 1, batch_unsteady)},
+  {PARS_BATCH_VARIANT(64, 1, batch_frozen), PARS_BATCH_VARIANT(128, 1, batch_frozen),
+   PARS_BATCH_VARIANT(128, 6, batch_frozen), PARS_BATCH_VARIANT(256, 1, batch_frozen)},
 };
+#undef PARS_BATCH_VARIANT
 }
 
 int batch_variant_count() { return 4; }
@@ -258,8 +360,32 @@ void launch_batch_advect(pars_gpu_context& ctx, int job_class, int v, const batc
   const long long persistent = (long long)std::max(per_sm, 1) * ctx.sm_count;
   const long long warps_needed = total_pools;   // at least one pool per warp
   const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>(persistent, (warps_needed * 32 + var.threads - 1) / var.threads));
+  const batch_horizon_args none {};
   launch_scope scope(ctx, "batch_advect");
-  void* args[] = {(void*)&jobs, (void*)&njobs, (void*)&total_pools, (void*)&counter};
+  void* args[] = {(void*)&jobs, (void*)&njobs, (void*)&total_pools, (void*)&counter, (void*)&none};
   PARS_CUDA(cudaLaunchKernel(var.kernel, grid, var.threads, args, 0, ctx.stream));
+}
+
+long long batch_horizon_warps(pars_gpu_context& ctx, int job_class, int v)
+{
+  const variant& var = variants[job_class][v];
+  int& per_sm = ctx.horizon_ctas_per_sm[job_class][v];
+  if (per_sm < 0) PARS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, var.horizon_kernel, var.threads, 0));
+  if (ctx.sm_count <= 0) PARS_CUDA(cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, ctx.device));
+  return (long long)std::max(per_sm, 1) * ctx.sm_count * (var.threads / 32);
+}
+
+void launch_batch_advect_horizon(pars_gpu_context& ctx, int job_class, int v, const batch_job_device* jobs, int njobs,
+                                 long long total_pools, unsigned long long* counter, const batch_horizon_args& hz, long long warps)
+{
+  const variant& var = variants[job_class][v];
+  const long long resident = batch_horizon_warps(ctx, job_class, v);
+  const long long want = std::min(resident, std::max<long long>({warps, (long long)hz.in_count, 1}));
+  const unsigned grid = (unsigned)((want * 32 + var.threads - 1) / var.threads);
+  // every parked group needs a warp of its own to resume it
+  PARS_REQUIRE((long long)grid * (var.threads / 32) >= hz.in_count, "more parked groups than warps");
+  launch_scope scope(ctx, "batch_advect_horizon");
+  void* args[] = {(void*)&jobs, (void*)&njobs, (void*)&total_pools, (void*)&counter, (void*)&hz};
+  PARS_CUDA(cudaLaunchKernel(var.horizon_kernel, grid, var.threads, args, 0, ctx.stream));
 }
 }

@@ -195,6 +195,8 @@ struct timed_launch
   std::string name;
   cudaEvent_t start, stop;
 };
+
+struct batch_engine;   // continuous batched advection (pars_gpu.cu)
 }
 
 struct pars_gpu_context
@@ -246,6 +248,9 @@ struct pars_gpu_context
   int                                     sm_count = 0;
   // batched engine: resident CTAs per SM per job class and launch shape
   int                                     batch_ctas_per_sm[3][4] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}, {-1, -1, -1, -1}};
+  int                                     horizon_ctas_per_sm[3][4] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}, {-1, -1, -1, -1}};
+  // continuous batched advection: job tables that grow between horizon launches
+  std::shared_ptr<pars::batch_engine>     engine;
   static constexpr std::size_t            buffer_cache_limit = std::size_t(8) << 30;
   // instrumentation
   bool                                    profile = false;
@@ -450,6 +455,58 @@ int  batch_pool_seeds();
 // job_class: batch_steady, batch_unsteady or batch_frozen.
 void launch_batch_advect(pars_gpu_context& ctx, int job_class, int variant, const batch_job_device* jobs, int njobs,
                          long long total_chunks, unsigned long long* counter);
+
+// Horizon launches of the batched engine.  A warp that has taken `iterations`
+// steps, or that sees another warp's stop flag, parks as one group: its job (an index into the launch's job table),
+// the unconsumed seeds [pool_next, pool_end) of its pool, a pool it has taken
+// but not begun (pending, or -1), and its live particles, `count` lane
+// records at lanes[32 g ..].  The next launch resumes each group in a warp of
+// its own before the warps take new pools.
+struct batch_parked_group
+{
+  int       job;
+  int       count;
+  long long pool_next, pool_end;
+  long long pending;
+};
+struct batch_parked_lane
+{
+  long long seed;
+  int       steps;
+  int       started;             // frozen multistep schemes: history present
+  float4    pos;                 // frozen: absolute position
+  float3    hist_v;              // frozen multistep schemes: previous velocity
+  int       ix, iy, iz;          // re-sampled: cell
+  float     ux, uy, uz, lx, ly, lz;   // re-sampled: offset and compensation
+};
+struct batch_horizon_args
+{
+  int                       iterations = 0;   // steps per warp before it parks
+  int                       in_count = 0;     // parked groups to resume
+  const batch_parked_group* in_groups = nullptr;
+  const batch_parked_lane*  in_lanes = nullptr;
+  unsigned int*             in_counter = nullptr;   // groups resumed (zero before the launch)
+  batch_parked_group*       out_groups = nullptr;
+  batch_parked_lane*        out_lanes = nullptr;
+  unsigned int*             out_count = nullptr;    // groups parked (zero before the launch)
+  unsigned int*             stop = nullptr;         // raised by the first warp at the horizon (zero before the launch)
+};
+// Warps of a horizon launch of (class, variant) when every CTA is resident:
+// the most groups one launch can park.
+long long batch_horizon_warps(pars_gpu_context& ctx, int job_class, int variant);
+// warps: the warps the launch's work can use (at least the parked groups).
+void launch_batch_advect_horizon(pars_gpu_context& ctx, int job_class, int variant, const batch_job_device* jobs, int njobs,
+                                 long long total_pools, unsigned long long* counter, const batch_horizon_args& hz, long long warps);
+
+// Continuous batched advection.  engine_submit appends a job (re-sampled RK4
+// / Euler on steady or unsteady fields, or the frozen scheme on steady ones)
+// to its class's job table and returns its ticket; engine_advance runs one
+// horizon launch of `iterations` steps per warp for every class with work and
+// returns the jobs that completed (ticket, particle-steps); engine_open
+// counts the jobs submitted and not yet returned.
+long long engine_submit(pars_gpu_context& ctx, const batch_job_device& job);
+std::vector<std::pair<long long, unsigned long long>> engine_advance(pars_gpu_context& ctx, int iterations);
+long long engine_open(const pars_gpu_context& ctx);
 
 // The tracing round loop over particles already in ctx.particles_in (grouped
 // by block, ctx.block_of when there are several blocks); fills ctx.curves.

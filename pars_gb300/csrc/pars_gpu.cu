@@ -7,6 +7,7 @@
 // out-of-bounds exchange (:376-393) — here a device exit queue sorted by
 // destination block, so the next round's particles never leave the GPU.
 #include <algorithm>
+#include <utility>
 #include <cstring>
 #include <limits>
 #include <new>
@@ -786,12 +787,82 @@ void trace_single(pars_gpu_context& ctx, int32_t field, long long count, int32_t
   run_rounds(ctx, blocks, device_blocks, count, block_count, block_max, rule, false, summary);
 }
 
+int class_of_job(const batch_job_device& j)
+{
+  return j.rule.frozen ? batch_frozen : (j.time.nt > 1 ? batch_unsteady : batch_steady);
+}
+
+long long pools_of(long long seeds)
+{
+  const int pool = batch_pool_seeds();
+  return (seeds + pool - 1) / pool;
+}
+
+// Chooses the launch shape of job class c from `jobs` (all of class c, clocks
+// set): every shape runs a probe of the jobs twice (seed counts capped at four
+// times the seeds the GPU holds resident), timed with CUDA events.
+void tune_class(pars_gpu_context& ctx, int c, std::vector<batch_job_device> jobs)
+{
+  const int count = int(jobs.size());
+  if (count == 0) return;
+  ctx.batch_jobs.reserve(sizeof(batch_job_device) * count);
+  ctx.batch_counters.reserve(sizeof(unsigned long long) * (count + 1));
+  auto* counters = ctx.batch_counters.as<unsigned long long>();
+  auto* device_jobs = ctx.batch_jobs.as<batch_job_device>();
+  if (ctx.sm_count <= 0) PARS_CUDA(cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, ctx.device));
+  const long long probe = std::max(16384LL, 4LL * 2048LL * ctx.sm_count);
+  long long pools = 0;
+  for (int k = 0; k < count; ++k)
+  {
+    jobs[k].seed_count = std::min(jobs[k].seed_count, probe);
+    jobs[k].first_pool = pools;
+    jobs[k].steps = counters + 1 + k;
+    pools += pools_of(jobs[k].seed_count);
+  }
+  cudaEvent_t a, b;
+  PARS_CUDA(cudaEventCreate(&a));
+  PARS_CUDA(cudaEventCreate(&b));
+  std::vector<float> fastest(batch_variant_count(), 0.0f);
+  for (int v = 0; v < batch_variant_count(); ++v)
+  {
+    for (int rep = 0; rep < 2; ++rep)
+    {
+      PARS_CUDA(cudaMemcpyAsync(device_jobs, jobs.data(), sizeof(batch_job_device) * count, cudaMemcpyHostToDevice, ctx.stream));
+      PARS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (count + 1), ctx.stream));
+      PARS_CUDA(cudaEventRecord(a, ctx.stream));
+      launch_batch_advect(ctx, c, v, device_jobs, count, pools, counters);
+      PARS_CUDA(cudaEventRecord(b, ctx.stream));
+      PARS_CUDA(cudaEventSynchronize(b));
+      float ms = 0.0f;
+      PARS_CUDA(cudaEventElapsedTime(&ms, a, b));
+      fastest[v] = rep == 0 ? ms : std::min(fastest[v], ms);
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  // The probe's particles take a few hundred steps each, so its last
+  // particles' tail blurs differences of a few per cent between shapes:
+  // among the shapes within 3 % of the fastest, keep the one with the most
+  // resident warps per SM (on the 256^3 flow map the 96-register shape, five
+  // CTAs of 128, beats the 104-register ones by 7 %, which the probes alone
+  // do not resolve reliably).
+  const float best_time = *std::min_element(fastest.begin(), fastest.end());
+  int best_v = -1, best_warps = -1;
+  for (int v = 0; v < batch_variant_count(); ++v)
+  {
+    if (fastest[v] > 1.03f * best_time) continue;
+    const int warps = batch_resident_warps(ctx, c, v);
+    if (warps > best_warps || (warps == best_warps && fastest[v] < fastest[best_v])) { best_v = v; best_warps = warps; }
+  }
+  ctx.batch_variant[c] = best_v;
+}
+
 // Runs batched jobs and returns each job's steps.  Re-sampled jobs on steady
 // fields (one slice), re-sampled jobs on unsteady fields and frozen-scheme
 // jobs run in up to three persistent launches, one per job class, so that a
 // job's arithmetic, and so its result, does not depend on the other jobs of
-// the batch.  variant < 0 uses the context's tuned launch
-// shape for each class, tuning it first if needed: every job of the class
+// the batch.  variant < 0 uses the context's tuned launch shape for each
+// class, tuning it first if needed (tune_class): every job of the class
 // capped at four times the seeds the GPU holds resident (2048 lanes per SM),
 // so that each shape runs at its own occupancy in steady state, each shape
 // timed twice with CUDA events, the fastest kept.  (A cap of 16384 seeds fills
@@ -800,9 +871,6 @@ void trace_single(pars_gpu_context& ctx, int32_t field, long long count, int32_t
 std::vector<unsigned long long> execute_batch(pars_gpu_context& ctx, std::vector<batch_job_device>& jobs, int variant)
 {
   const int count = int(jobs.size());
-  auto class_of = [](const batch_job_device& j) {
-    return j.rule.frozen ? batch_frozen : (j.time.nt > 1 ? batch_unsteady : batch_steady);
-  };
   // jobs grouped by class; order[k] = caller's index of job k
   std::vector<int> order;
   order.reserve(count);
@@ -810,7 +878,7 @@ std::vector<unsigned long long> execute_batch(pars_gpu_context& ctx, std::vector
   for (int c = 0; c < batch_classes; ++c)
   {
     first[c] = int(order.size());
-    for (int j = 0; j < count; ++j) if (class_of(jobs[j]) == c) order.push_back(j);
+    for (int j = 0; j < count; ++j) if (class_of_job(jobs[j]) == c) order.push_back(j);
     size[c] = int(order.size()) - first[c];
   }
   std::vector<batch_job_device> queue(count);
@@ -820,80 +888,30 @@ std::vector<unsigned long long> execute_batch(pars_gpu_context& ctx, std::vector
     queue[k].clock = make_slice_clock(queue[k].time, queue[k].time_begin, queue[k].rule.h);
   }
   constexpr int C = batch_classes;
-  ctx.batch_jobs.reserve(sizeof(batch_job_device) * count);
-  ctx.batch_counters.reserve(sizeof(unsigned long long) * (count + C));
-  auto* counters = ctx.batch_counters.as<unsigned long long>();
-  auto* device_jobs = ctx.batch_jobs.as<batch_job_device>();
+  for (int c = 0; c < C; ++c)
+    if (variant < 0 && size[c] > 0 && ctx.batch_variant[c] < 0)
+      tune_class(ctx, c, std::vector<batch_job_device>(queue.begin() + first[c], queue.begin() + first[c] + size[c]));
 
   // The device queues: each job's seeds in pools of batch_pool_seeds(), numbered
   // per class; counters 0 .. C-1 hand out the pools of the classes, counters
   // C.. count each job's steps.
+  ctx.batch_jobs.reserve(sizeof(batch_job_device) * count);
+  ctx.batch_counters.reserve(sizeof(unsigned long long) * (count + C));
+  auto* counters = ctx.batch_counters.as<unsigned long long>();
+  auto* device_jobs = ctx.batch_jobs.as<batch_job_device>();
   long long pools[C] = {};
-  auto upload = [&] {
-    const int pool = batch_pool_seeds();
-    for (int c = 0; c < C; ++c)
-    {
-      pools[c] = 0;
-      for (int k = first[c]; k < first[c] + size[c]; ++k)
-      {
-        queue[k].first_pool = pools[c];
-        queue[k].steps = counters + C + k;
-        pools[c] += (queue[k].seed_count + pool - 1) / pool;
-      }
-    }
-    PARS_CUDA(cudaMemcpyAsync(device_jobs, queue.data(), sizeof(batch_job_device) * count, cudaMemcpyHostToDevice, ctx.stream));
-    PARS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (count + C), ctx.stream));
-  };
-  auto launch = [&](int c, int v) {
-    if (size[c] > 0) launch_batch_advect(ctx, c, v, device_jobs + first[c], size[c], pools[c], counters + c);
-  };
-
   for (int c = 0; c < C; ++c)
-  {
-    if (variant >= 0 || size[c] == 0 || ctx.batch_variant[c] >= 0) continue;
-    std::vector<long long> full(count);
-    if (ctx.sm_count <= 0) PARS_CUDA(cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, ctx.device));
-    const long long probe = std::max(16384LL, 4LL * 2048LL * ctx.sm_count);
-    for (int k = 0; k < count; ++k) { full[k] = queue[k].seed_count; queue[k].seed_count = std::min(full[k], probe); }
-    cudaEvent_t a, b;
-    PARS_CUDA(cudaEventCreate(&a));
-    PARS_CUDA(cudaEventCreate(&b));
-    std::vector<float> fastest(batch_variant_count(), 0.0f);
-    for (int v = 0; v < batch_variant_count(); ++v)
+    for (int k = first[c]; k < first[c] + size[c]; ++k)
     {
-      for (int rep = 0; rep < 2; ++rep)
-      {
-        upload();
-        PARS_CUDA(cudaEventRecord(a, ctx.stream));
-        launch(c, v);
-        PARS_CUDA(cudaEventRecord(b, ctx.stream));
-        PARS_CUDA(cudaEventSynchronize(b));
-        float ms = 0.0f;
-        PARS_CUDA(cudaEventElapsedTime(&ms, a, b));
-        fastest[v] = rep == 0 ? ms : std::min(fastest[v], ms);
-      }
+      queue[k].first_pool = pools[c];
+      queue[k].steps = counters + C + k;
+      pools[c] += pools_of(queue[k].seed_count);
     }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    // The probe's particles take a few hundred steps each, so its last
-    // particles' tail blurs differences of a few per cent between shapes:
-    // among the shapes within 3 % of the fastest, keep the one with the most
-    // resident warps per SM (on the 256^3 flow map the 96-register shape, five
-    // CTAs of 128, beats the 104-register ones by 7 %, which the probes alone
-    // do not resolve reliably).
-    const float best_time = *std::min_element(fastest.begin(), fastest.end());
-    int best_v = -1, best_warps = -1;
-    for (int v = 0; v < batch_variant_count(); ++v)
-    {
-      if (fastest[v] > 1.03f * best_time) continue;
-      const int warps = batch_resident_warps(ctx, c, v);
-      if (warps > best_warps || (warps == best_warps && fastest[v] < fastest[best_v])) { best_v = v; best_warps = warps; }
-    }
-    ctx.batch_variant[c] = best_v;
-    for (int k = 0; k < count; ++k) queue[k].seed_count = full[k];
-  }
-  upload();
-  for (int c = 0; c < C; ++c) launch(c, variant >= 0 ? variant : ctx.batch_variant[c]);
+  PARS_CUDA(cudaMemcpyAsync(device_jobs, queue.data(), sizeof(batch_job_device) * count, cudaMemcpyHostToDevice, ctx.stream));
+  PARS_CUDA(cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * (count + C), ctx.stream));
+  for (int c = 0; c < C; ++c)
+    if (size[c] > 0)
+      launch_batch_advect(ctx, c, variant >= 0 ? variant : ctx.batch_variant[c], device_jobs + first[c], size[c], pools[c], counters + c);
   std::vector<unsigned long long> steps(count + C);
   PARS_CUDA(cudaMemcpyAsync(steps.data(), counters, sizeof(unsigned long long) * (count + C), cudaMemcpyDeviceToHost, ctx.stream));
   PARS_CUDA(cudaStreamSynchronize(ctx.stream));
@@ -925,6 +943,249 @@ std::vector<unsigned long long> run_batch(pars_gpu_context& ctx, std::vector<bat
 }
 
 pars_partition_info partition(int ranks, int rank, const int32_t domain[3]) { return partition_of(ranks, rank, domain); }
+
+// ---- continuous batched advection ------------------------------------------------
+// One job table per job class.  Jobs are appended between horizon launches;
+// their pools continue the class's pool numbering, so the table's pool
+// counter hands them out after the earlier jobs' pools.  A launch's warps
+// that find the counter past the table's last pool increment it once more
+// each; the host puts it back to the number of pools before the next launch.
+// Completed jobs stay in the table until every job of the class is complete,
+// then the table starts again from zero.
+struct batch_engine_class
+{
+  std::vector<batch_job_device> jobs;       // host copy of the device table
+  std::vector<long long>        tickets;
+  std::vector<char>             complete;
+  std::vector<char>             counted;         // the job's device counters are zeroed
+  int                           uploaded = 0;    // jobs copied to the device table
+  int                           capacity = 0;    // jobs the device buffers hold
+  device_buffer                 table;
+  // [0] pools handed out, [1] groups resumed (u32), [2] groups parked (u32),
+  // [3] stop flag (u32), [4, 4 + capacity) steps per job
+  device_buffer                 counters;
+  device_buffer                 groups[2], lanes[2];
+  long long                     group_capacity = 0;
+  int                           parity = 0;      // parked groups are in groups[parity]
+  unsigned int                  parked = 0;
+  long long                     total_pools = 0;
+  unsigned long long            handed = 0;      // pools handed out (at most total_pools)
+  int                           variant = -1;
+  long long                     open = 0;
+};
+
+struct batch_engine
+{
+  batch_engine_class classes[batch_classes];
+  long long          next_ticket = 1;
+  std::vector<std::pair<long long, unsigned long long>> ready;   // completions not yet returned (C ABI)
+};
+
+namespace
+{
+void engine_reserve(pars_gpu_context& ctx, batch_engine_class& E, int jobs)
+{
+  if (jobs <= E.capacity) return;
+  const int capacity = std::max(jobs, std::max(64, 2 * E.capacity));
+  device_buffer table, counters;
+  table.reserve(sizeof(batch_job_device) * capacity);
+  counters.reserve(sizeof(unsigned long long) * (4 + std::size_t(capacity)));
+  PARS_CUDA(cudaMemsetAsync(counters.get(), 0, counters.bytes(), ctx.stream));
+  auto* fresh = counters.as<unsigned long long>();
+  if (E.capacity > 0)
+  {
+    // keep the pool counter and the jobs' step counts
+    PARS_CUDA(cudaMemcpyAsync(fresh, E.counters.get(), sizeof(unsigned long long) * (4 + E.capacity), cudaMemcpyDeviceToDevice,
+                              ctx.stream));
+  }
+  E.table = std::move(table);
+  E.counters = std::move(counters);
+  E.capacity = capacity;
+  for (std::size_t k = 0; k < E.jobs.size(); ++k) E.jobs[k].steps = fresh + 4 + k;
+  E.uploaded = 0;   // the steps pointers changed: upload the whole table again
+}
+
+void engine_reset(batch_engine_class& E)
+{
+  E.jobs.clear();
+  E.tickets.clear();
+  E.complete.clear();
+  E.counted.clear();
+  E.uploaded = 0;
+  E.parity = 0;
+  E.parked = 0;
+  E.total_pools = 0;
+  E.handed = 0;
+  E.open = 0;
+}
+}
+
+long long engine_submit(pars_gpu_context& ctx, const batch_job_device& job)
+{
+  if (!ctx.engine) ctx.engine = std::make_shared<batch_engine>();
+  batch_engine& engine = *ctx.engine;
+  const int c = class_of_job(job);
+  batch_engine_class& E = engine.classes[c];
+  batch_job_device j = job;
+  j.clock = make_slice_clock(j.time, j.time_begin, j.rule.h);
+  if (ctx.batch_variant[c] < 0) tune_class(ctx, c, {j});
+  if (E.open == 0) E.variant = ctx.batch_variant[c];   // fixed while the class has work
+  engine_reserve(ctx, E, int(E.jobs.size()) + 1);
+  j.first_pool = E.total_pools;
+  j.steps = E.counters.as<unsigned long long>() + 4 + E.jobs.size();
+  E.total_pools += pools_of(j.seed_count);
+  E.jobs.push_back(j);
+  const long long ticket = engine.next_ticket++;
+  E.tickets.push_back(ticket);
+  E.complete.push_back(0);
+  E.counted.push_back(0);
+  ++E.open;
+  return ticket;
+}
+
+long long engine_open(const pars_gpu_context& ctx)
+{
+  if (!ctx.engine) return 0;
+  long long open = 0;
+  for (const auto& E : ctx.engine->classes) open += E.open;
+  return open;
+}
+
+std::vector<std::pair<long long, unsigned long long>> engine_advance(pars_gpu_context& ctx, int iterations)
+{
+  PARS_REQUIRE(iterations >= 1, "iterations must be >= 1");
+  std::vector<std::pair<long long, unsigned long long>> done;
+  if (!ctx.engine) return done;
+  for (int c = 0; c < batch_classes; ++c)
+  {
+    batch_engine_class& E = ctx.engine->classes[c];
+    if (E.open == 0) continue;
+    const int n = int(E.jobs.size());
+    auto* counters = E.counters.as<unsigned long long>();
+    if (E.uploaded < n)
+    {
+      PARS_CUDA(cudaMemcpyAsync(E.table.as<batch_job_device>() + E.uploaded, E.jobs.data() + E.uploaded,
+                                sizeof(batch_job_device) * (n - E.uploaded), cudaMemcpyHostToDevice, ctx.stream));
+      // new jobs start from zero steps (the slots may hold the counts of
+      // the jobs of an earlier table)
+      for (int k = E.uploaded; k < n; ++k)
+        if (E.counted[k] == 0)
+        {
+          PARS_CUDA(cudaMemsetAsync(counters + 4 + k, 0, sizeof(unsigned long long), ctx.stream));
+          E.counted[k] = 1;
+        }
+      E.uploaded = n;
+    }
+    const long long resident = batch_horizon_warps(ctx, c, E.variant);
+    if (E.group_capacity < resident)
+    {
+      PARS_REQUIRE(E.parked == 0, "the engine's launch shape changed while groups are parked");
+      for (int b = 0; b < 2; ++b)
+      {
+        E.groups[b].reserve(sizeof(batch_parked_group) * resident);
+        E.lanes[b].reserve(sizeof(batch_parked_lane) * 32 * resident);
+      }
+      E.group_capacity = resident;
+    }
+    const long long remaining = E.total_pools - (long long)E.handed;
+    if (remaining > 0 || E.parked > 0)
+    {
+      const unsigned long long start[4] = {E.handed, 0, 0, 0};
+      PARS_CUDA(cudaMemcpyAsync(counters, start, sizeof(start), cudaMemcpyHostToDevice, ctx.stream));
+      batch_horizon_args hz;
+      hz.iterations = iterations;
+      hz.in_count = int(E.parked);
+      hz.in_groups = E.groups[E.parity].as<const batch_parked_group>();
+      hz.in_lanes = E.lanes[E.parity].as<const batch_parked_lane>();
+      hz.in_counter = reinterpret_cast<unsigned int*>(counters + 1);
+      hz.out_groups = E.groups[1 - E.parity].as<batch_parked_group>();
+      hz.out_lanes = E.lanes[1 - E.parity].as<batch_parked_lane>();
+      hz.out_count = reinterpret_cast<unsigned int*>(counters + 2);
+      hz.stop = reinterpret_cast<unsigned int*>(counters + 3);
+      launch_batch_advect_horizon(ctx, c, E.variant, E.table.as<const batch_job_device>(), n, E.total_pools, counters, hz,
+                                  remaining + E.parked);
+      E.parity = 1 - E.parity;
+    }
+    std::vector<unsigned long long> host(4 + std::size_t(E.capacity));
+    PARS_CUDA(cudaMemcpyAsync(host.data(), counters, sizeof(unsigned long long) * host.size(), cudaMemcpyDeviceToHost, ctx.stream));
+    PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+    E.handed = std::min<unsigned long long>(host[0], (unsigned long long)E.total_pools);
+    E.parked = (unsigned int)(host[2] & 0xffffffffu);
+    PARS_REQUIRE(E.parked <= (unsigned long long)E.group_capacity, "parked group count out of range");
+    // No warp runs between launches: a job's particles are all retired once
+    // all its pools are handed out and no parked group holds its particles,
+    // the rest of one of its pools, or one of its pools not yet begun.
+    std::vector<char> held(n, 0);
+    if (E.parked > 0)
+    {
+      std::vector<batch_parked_group> groups(E.parked);
+      PARS_CUDA(cudaMemcpyAsync(groups.data(), E.groups[E.parity].get(), sizeof(batch_parked_group) * groups.size(),
+                                cudaMemcpyDeviceToHost, ctx.stream));
+      PARS_CUDA(cudaStreamSynchronize(ctx.stream));
+      auto job_of_pool = [&](long long pool) {
+        int lo = 0, hi = n - 1;
+        while (lo < hi)
+        {
+          const int mid = (lo + hi + 1) / 2;
+          if (E.jobs[mid].first_pool <= pool) lo = mid;
+          else hi = mid - 1;
+        }
+        return lo;
+      };
+      for (const auto& g : groups)
+      {
+        PARS_REQUIRE(g.job >= 0 && g.job < n && g.count >= 0 && g.count <= 32, "parked group out of range");
+        held[g.job] = 1;
+        if (g.pending >= 0) held[job_of_pool(g.pending)] = 1;
+      }
+    }
+    for (int k = 0; k < n; ++k)
+    {
+      const long long last_pool = E.jobs[k].first_pool + pools_of(E.jobs[k].seed_count);
+      if (E.complete[k] || held[k] || (long long)E.handed < last_pool) continue;
+      E.complete[k] = 1;
+      --E.open;
+      done.emplace_back(E.tickets[k], host[4 + k]);
+    }
+    if (E.open == 0)
+    {
+      PARS_REQUIRE(E.parked == 0, "groups parked after every job completed");
+      engine_reset(E);
+    }
+  }
+  return done;
+}
+
+// A public batch job as the engine reads it (field, rule and seeds checked).
+batch_job_device device_job(pars_gpu_context& ctx, const pars_gpu_batch_job& in)
+{
+  auto& f = find_field(ctx, in.field);
+  batch_job_device d {};
+  d.field = f.view();
+  d.time = f.time();
+  d.rule = make_rule(in.integrator, in.stage_mode, in.step_size);
+  if (d.rule.frozen && d.time.nt > 1)
+    throw error(PARS_ERR_UNSUPPORTED, "batched frozen-scheme jobs run on steady fields");
+  if (!d.rule.frozen && d.rule.scheme != scheme_classic)
+    throw error(PARS_ERR_UNSUPPORTED, "batched re-sampled advection integrates with RK4 or Euler");
+  d.ux = d.uy = d.uz = 0;
+  PARS_REQUIRE(in.max_steps >= 0, "max_steps must be >= 0");
+  d.max_steps = in.max_steps;
+  d.time_begin = in.time_begin;
+  d.seeds = reinterpret_cast<const float4*>(in.seeds);
+  if (in.seeds) { PARS_REQUIRE(in.seed_count >= 0, "seed_count must be >= 0"); d.seed_count = in.seed_count; }
+  else
+  {
+    for (int i = 0; i < 3; ++i) PARS_REQUIRE(in.lattice_count[i] >= 0, "lattice counts must be >= 0");
+    d.seed_count = (long long)in.lattice_count[0] * in.lattice_count[1] * in.lattice_count[2];
+  }
+  d.ox = in.lattice_offset[0]; d.oy = in.lattice_offset[1]; d.oz = in.lattice_offset[2];
+  d.sx = in.lattice_stride[0]; d.sy = in.lattice_stride[1]; d.sz = in.lattice_stride[2];
+  d.px = in.lattice_count[0]; d.py = in.lattice_count[1]; d.pz = in.lattice_count[2];
+  d.end_positions = reinterpret_cast<float4*>(in.end_positions);
+  d.end_steps = in.end_steps;
+  return d;
+}
 }
 
 using namespace pars;
@@ -1654,37 +1915,35 @@ int32_t pars_gpu_batch_advect(pars_gpu_context* ctx, pars_gpu_batch_job* jobs, i
     PARS_REQUIRE(variant >= -1 && variant < batch_variant_count(), "unknown launch variant");
     if (count == 0) return;
     std::vector<batch_job_device> device_jobs(count);
-    for (int j = 0; j < count; ++j)
-    {
-      const pars_gpu_batch_job& in = jobs[j];
-      auto& f = find_field(*ctx, in.field);
-      batch_job_device& d = device_jobs[j];
-      d.field = f.view();
-      d.time = f.time();
-      d.rule = make_rule(in.integrator, in.stage_mode, in.step_size);
-      if (d.rule.frozen && d.time.nt > 1)
-        throw error(PARS_ERR_UNSUPPORTED, "batched frozen-scheme jobs run on steady fields");
-      if (!d.rule.frozen && d.rule.scheme != scheme_classic)
-        throw error(PARS_ERR_UNSUPPORTED, "batched re-sampled advection integrates with RK4 or Euler");
-      d.ux = d.uy = d.uz = 0;
-      PARS_REQUIRE(in.max_steps >= 0, "max_steps must be >= 0");
-      d.max_steps = in.max_steps;
-      d.time_begin = in.time_begin;
-      d.seeds = reinterpret_cast<const float4*>(in.seeds);
-      if (in.seeds) { PARS_REQUIRE(in.seed_count >= 0, "seed_count must be >= 0"); d.seed_count = in.seed_count; }
-      else
-      {
-        for (int i = 0; i < 3; ++i) PARS_REQUIRE(in.lattice_count[i] >= 0, "lattice counts must be >= 0");
-        d.seed_count = (long long)in.lattice_count[0] * in.lattice_count[1] * in.lattice_count[2];
-      }
-      d.ox = in.lattice_offset[0]; d.oy = in.lattice_offset[1]; d.oz = in.lattice_offset[2];
-      d.sx = in.lattice_stride[0]; d.sy = in.lattice_stride[1]; d.sz = in.lattice_stride[2];
-      d.px = in.lattice_count[0]; d.py = in.lattice_count[1]; d.pz = in.lattice_count[2];
-      d.end_positions = reinterpret_cast<float4*>(in.end_positions);
-      d.end_steps = in.end_steps;
-    }
+    for (int j = 0; j < count; ++j) device_jobs[j] = device_job(*ctx, jobs[j]);
     const std::vector<unsigned long long> steps = execute_batch(*ctx, device_jobs, variant);
     for (int j = 0; j < count; ++j) jobs[j].steps = (int64_t)steps[j];
+  });
+}
+
+int32_t pars_gpu_engine_submit(pars_gpu_context* ctx, const pars_gpu_batch_job* job, int64_t* ticket)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(job && ticket, "job and ticket are required");
+    *ticket = engine_submit(*ctx, device_job(*ctx, *job));
+  });
+}
+
+int32_t pars_gpu_engine_advance(pars_gpu_context* ctx, int32_t iterations, pars_gpu_engine_done* done, int32_t capacity,
+                                int32_t* done_count, int64_t* open)
+{
+  return guarded(ctx, [&] {
+    PARS_REQUIRE(capacity >= 0 && (capacity == 0 || done), "done is required when capacity > 0");
+    PARS_REQUIRE(done_count, "done_count is required");
+    const auto finished = engine_advance(*ctx, iterations);
+    if (!ctx->engine) ctx->engine = std::make_shared<batch_engine>();
+    auto& ready = ctx->engine->ready;
+    ready.insert(ready.end(), finished.begin(), finished.end());
+    const int32_t n = int32_t(std::min<std::size_t>(ready.size(), std::size_t(capacity)));
+    for (int32_t i = 0; i < n; ++i) { done[i].ticket = ready[i].first; done[i].steps = (int64_t)ready[i].second; }
+    ready.erase(ready.begin(), ready.begin() + n);
+    *done_count = n;
+    if (open) *open = engine_open(*ctx) + (int64_t)ready.size();
   });
 }
 

@@ -176,6 +176,9 @@ struct pars_gpu_service
   std::map<std::string, pars::profile_entry> profile_totals;
   int64_t                              next_ticket = 1;
   int                                  running_batches = 0;
+  // FTLE requests: steps per warp of each continuous-engine launch (0: each
+  // batch runs to completion in one launch)
+  int                                  horizon = 1024;
 };
 
 namespace pars
@@ -302,102 +305,218 @@ void copy_result(pars_gpu_service& svc, const request& r, std::size_t offset, vo
     throw error(PARS_ERR_STATE, "the request has no result");
 }
 
-// FTLE requests: flow maps as jobs of one batched launch, then the FTLE kernel
-// per request (pipeline::execute_ftle, pars/source/pipeline.cpp:345-409).
+// One FTLE request's flow-map job and flow-map buffer (the flow_map_generator
+// stage of pipeline::execute_ftle, pars/source/pipeline.cpp:345-409): seeds on
+// the dataset's lattice at 1 / stride resolution, flow map of that shape.
+struct ftle_work
+{
+  std::shared_ptr<request> r;
+  batch_job_device         job {};
+  device_buffer            flow;
+};
+
+ftle_work prepare_ftle(pars_gpu_service& svc, pars_gpu_context& c, const std::shared_ptr<request>& rp)
+{
+  request& r = *rp;
+  const dataset& d = svc.datasets[r.dataset];
+  const float scale = 1.0f / float(std::max(1, r.s.seed_generation_stride.empty() ? 1 : r.s.seed_generation_stride[0]));
+  ftle_work w;
+  w.r = rp;
+  batch_job_device& j = w.job;
+  j.field = d.view;
+  j.time.nt = 1; j.time.slice_stride = 0; j.time.t0 = 0.0; j.time.inv_slice_dt = 1.0;
+  j.rule = make_step_rule(r.integrator, r.stage_mode, r.s.particle_tracing_step_size);
+  j.max_steps = std::max(0, r.s.seed_generation_iterations - 1);
+  j.time_begin = 0.0;
+  j.seeds = nullptr;
+  int fm[3], seeds[3];
+  float fm_spacing[3];
+  for (int i = 0; i < 3; ++i)
+  {
+    fm[i] = std::max(1, int(float(d.shape[i]) * scale));
+    fm_spacing[i] = d.spacing[i] / scale;
+    const float q = d.size[i] / fm_spacing[i];
+    seeds[i] = (q > 0.0f && q < 2147483647.0f) ? int(q) : 0;
+    r.ftle_shape[i] = fm[i];
+  }
+  j.seed_count = (long long)seeds[0] * seeds[1] * seeds[2];
+  j.ox = d.offset[0]; j.oy = d.offset[1]; j.oz = d.offset[2];
+  j.sx = fm_spacing[0]; j.sy = fm_spacing[1]; j.sz = fm_spacing[2];
+  j.px = seeds[0]; j.py = seeds[1]; j.pz = seeds[2];
+  j.ux = fm[0]; j.uy = fm[1]; j.uz = fm[2];
+  w.flow = acquire_buffer(c, sizeof(float4) * (std::size_t)fm[0] * fm[1] * fm[2]);
+  if (seeds[0] < fm[0] || seeds[1] < fm[1] || seeds[2] < fm[2])
+    PARS_CUDA(cudaMemsetAsync(w.flow.get(), 0xff, w.flow.bytes(), c.stream));
+  j.end_positions = w.flow.as<float4>();
+  j.end_steps = nullptr;
+  return w;
+}
+
+// RK4 / Euler requests and the reference's frozen scheme run on the batched
+// engine; the other integrators' re-sampled schemes on the per-seed flow-map
+// kernel.
+bool engine_job(const batch_job_device& j) { return j.rule.frozen || j.rule.scheme == scheme_classic; }
+
+// The per-seed flow-map kernel for one request; returns its steps.
+long long per_seed_flow_map(pars_gpu_context& c, const ftle_work& w)
+{
+  device_buffer counter;
+  counter.reserve(sizeof(unsigned long long));
+  PARS_CUDA(cudaMemsetAsync(counter.get(), 0, sizeof(unsigned long long), c.stream));
+  const batch_job_device& j = w.job;
+  const float offset[3] = {j.ox, j.oy, j.oz}, spacing[3] = {j.sx, j.sy, j.sz};
+  const int seeds[3] = {j.px, j.py, j.pz}, shape[3] = {j.ux, j.uy, j.uz};
+  launch_flow_map(c, j.field, j.rule, w.r->s.seed_generation_iterations, offset, spacing, seeds, shape,
+                  w.flow.as<float4>(), counter.as<unsigned long long>());
+  unsigned long long steps = 0;
+  PARS_CUDA(cudaMemcpyAsync(&steps, counter.get(), sizeof(steps), cudaMemcpyDeviceToHost, c.stream));
+  PARS_CUDA(cudaStreamSynchronize(c.stream));
+  return (long long)steps;
+}
+
+// The ftle_map_generator stage of a request whose flow map is complete: the
+// result allocation and the FTLE kernel (queued on the lane's stream).
+void finish_ftle(pars_gpu_service& svc, pars_gpu_context& c, ftle_work& w, long long steps)
+{
+  request& r = *w.r;
+  r.steps = steps;
+  field_view fv {};
+  fv.data = w.flow.as<const float4>();
+  fv.nx = r.ftle_shape[0]; fv.ny = r.ftle_shape[1]; fv.nz = r.ftle_shape[2];
+  fv.hx = w.job.sx; fv.hy = w.job.sy; fv.hz = w.job.sz;
+  const long long voxels = (long long)fv.nx * fv.ny * fv.nz;
+  allocate_result(svc, c, r, sizeof(float) * voxels);
+  // time = step * iterations in FP32, as pipeline.cpp:403 sets it
+  const float time = r.s.particle_tracing_step_size * float(r.s.seed_generation_iterations);
+  launch_ftle(c, fv, time == 0.0f ? 1.0 : double(time), r.ftle_mode, reinterpret_cast<float*>(r.result));
+}
+
+// FTLE requests run to completion as one batch: flow maps as jobs of one
+// batched launch, then the FTLE kernel per request.
 void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std::shared_ptr<request>>& batch)
 {
   phase_clock clock {svc, c, c.profile};
-  std::vector<batch_job_device> jobs;
-  std::vector<device_buffer> flows;
-  std::vector<int> shapes;
-  for (auto& rp : batch)
-  {
-    request& r = *rp;
-    const dataset& d = svc.datasets[r.dataset];
-    const float scale = 1.0f / float(std::max(1, r.s.seed_generation_stride.empty() ? 1 : r.s.seed_generation_stride[0]));
-    batch_job_device j {};
-    j.field = d.view;
-    j.time.nt = 1; j.time.slice_stride = 0; j.time.t0 = 0.0; j.time.inv_slice_dt = 1.0;
-    j.rule = make_step_rule(r.integrator, r.stage_mode, r.s.particle_tracing_step_size);
-    j.max_steps = std::max(0, r.s.seed_generation_iterations - 1);
-    j.time_begin = 0.0;
-    j.seeds = nullptr;
-    int fm[3], seeds[3];
-    float fm_spacing[3];
-    for (int i = 0; i < 3; ++i)
-    {
-      fm[i] = std::max(1, int(float(d.shape[i]) * scale));
-      fm_spacing[i] = d.spacing[i] / scale;
-      const float q = d.size[i] / fm_spacing[i];
-      seeds[i] = (q > 0.0f && q < 2147483647.0f) ? int(q) : 0;
-      r.ftle_shape[i] = fm[i];
-    }
-    j.seed_count = (long long)seeds[0] * seeds[1] * seeds[2];
-    j.ox = d.offset[0]; j.oy = d.offset[1]; j.oz = d.offset[2];
-    j.sx = fm_spacing[0]; j.sy = fm_spacing[1]; j.sz = fm_spacing[2];
-    j.px = seeds[0]; j.py = seeds[1]; j.pz = seeds[2];
-    j.ux = fm[0]; j.uy = fm[1]; j.uz = fm[2];
-    flows.push_back(acquire_buffer(c, sizeof(float4) * (std::size_t)fm[0] * fm[1] * fm[2]));
-    if (seeds[0] < fm[0] || seeds[1] < fm[1] || seeds[2] < fm[2])
-      PARS_CUDA(cudaMemsetAsync(flows.back().get(), 0xff, flows.back().bytes(), c.stream));
-    j.end_positions = flows.back().as<float4>();
-    j.end_steps = nullptr;
-    jobs.push_back(j);
-  }
+  std::vector<ftle_work> work;
+  for (auto& rp : batch) work.push_back(prepare_ftle(svc, c, rp));
   clock.mark("ftle.setup");
-  // RK4 / Euler requests and the reference's frozen scheme: the persistent
-  // batched engine; the other integrators' re-sampled schemes: the per-seed
-  // flow-map kernel, one launch each
   std::vector<batch_job_device> classic;
-  std::vector<std::size_t> classic_of, general_of;
-  for (std::size_t k = 0; k < jobs.size(); ++k)
-  {
-    if (jobs[k].rule.frozen || jobs[k].rule.scheme == scheme_classic) { classic.push_back(jobs[k]); classic_of.push_back(k); }
-    else general_of.push_back(k);
-  }
-  std::vector<unsigned long long> steps(jobs.size(), 0);
+  std::vector<std::size_t> classic_of;
+  std::vector<long long> steps(work.size(), 0);
+  for (std::size_t k = 0; k < work.size(); ++k)
+    if (engine_job(work[k].job)) { classic.push_back(work[k].job); classic_of.push_back(k); }
   if (!classic.empty())
   {
     const auto s = run_batch(c, classic, -1);
-    for (std::size_t i = 0; i < classic_of.size(); ++i) steps[classic_of[i]] = s[i];
+    for (std::size_t i = 0; i < classic_of.size(); ++i) steps[classic_of[i]] = (long long)s[i];
   }
-  if (!general_of.empty())
-  {
-    device_buffer counters;
-    counters.reserve(sizeof(unsigned long long) * general_of.size());
-    PARS_CUDA(cudaMemsetAsync(counters.get(), 0, sizeof(unsigned long long) * general_of.size(), c.stream));
-    for (std::size_t i = 0; i < general_of.size(); ++i)
-    {
-      const batch_job_device& j = jobs[general_of[i]];
-      const request& r = *batch[general_of[i]];
-      const float offset[3] = {j.ox, j.oy, j.oz}, spacing[3] = {j.sx, j.sy, j.sz};
-      const int seeds[3] = {j.px, j.py, j.pz}, shape[3] = {j.ux, j.uy, j.uz};
-      launch_flow_map(c, j.field, j.rule, r.s.seed_generation_iterations, offset, spacing, seeds, shape,
-                      flows[general_of[i]].as<float4>(), counters.as<unsigned long long>() + i);
-    }
-    std::vector<unsigned long long> host(general_of.size());
-    PARS_CUDA(cudaMemcpyAsync(host.data(), counters.get(), sizeof(unsigned long long) * host.size(), cudaMemcpyDeviceToHost, c.stream));
-    PARS_CUDA(cudaStreamSynchronize(c.stream));
-    for (std::size_t i = 0; i < general_of.size(); ++i) steps[general_of[i]] = host[i];
-  }
+  for (std::size_t k = 0; k < work.size(); ++k)
+    if (!engine_job(work[k].job)) steps[k] = per_seed_flow_map(c, work[k]);
   clock.mark("ftle.advect");
-  for (std::size_t k = 0; k < batch.size(); ++k)
-  {
-    request& r = *batch[k];
-    r.steps = (long long)steps[k];
-    field_view fv {};
-    fv.data = flows[k].as<const float4>();
-    fv.nx = r.ftle_shape[0]; fv.ny = r.ftle_shape[1]; fv.nz = r.ftle_shape[2];
-    fv.hx = jobs[k].sx; fv.hy = jobs[k].sy; fv.hz = jobs[k].sz;
-    const long long voxels = (long long)fv.nx * fv.ny * fv.nz;
-    allocate_result(svc, c, r, sizeof(float) * voxels);
-    // time = step * iterations in FP32, as pipeline.cpp:403 sets it
-    const float time = r.s.particle_tracing_step_size * float(r.s.seed_generation_iterations);
-    launch_ftle(c, fv, time == 0.0f ? 1.0 : double(time), r.ftle_mode, reinterpret_cast<float*>(r.result));
-  }
+  for (std::size_t k = 0; k < work.size(); ++k) finish_ftle(svc, c, work[k], steps[k]);
   PARS_CUDA(cudaStreamSynchronize(c.stream));
   clock.mark("ftle.field");
-  for (auto& f : flows) recycle_buffer(c, std::move(f));
+  for (auto& w : work) recycle_buffer(c, std::move(w.flow));
+}
+
+// FTLE requests through the context's continuous engine: each request's flow
+// map is a job of the engine's table, advanced one horizon launch (svc.horizon
+// steps per warp) at a time.  Between launches the requests whose flow maps
+// completed get their FTLE field and are handed to the client at once, and
+// FTLE requests that arrived meanwhile are admitted (within the budget and
+// max_batch in flight) and join the running table.  Admission pauses while
+// requests of the other kind wait and no other lane is free, so streamline
+// requests are not starved.  Requests leave `batch` as they finish; their
+// estimates leave `reserved`.  Returns the number of requests served.
+std::size_t run_ftle_continuous(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std::shared_ptr<request>>& batch,
+                                std::size_t& reserved)
+{
+  std::map<long long, ftle_work> in_engine;   // by engine ticket
+  std::size_t served = batch.size();
+  auto complete = [&](ftle_work& w, long long steps) {
+    {
+      phase_clock clock {svc, c, c.profile};
+      finish_ftle(svc, c, w, steps);
+      PARS_CUDA(cudaStreamSynchronize(c.stream));
+      clock.mark("ftle.field");
+    }
+    recycle_buffer(c, std::move(w.flow));
+    {
+      std::lock_guard<std::mutex> lock(svc.mutex);
+      request& r = *w.r;
+      svc.in_use -= std::min(svc.in_use, r.estimate);
+      reserved -= std::min(reserved, r.estimate);
+      if (r.result) { svc.in_use += r.result_bytes; svc.held += r.result_bytes; }
+      r.state = done;
+      r.finished = clock_type::now();
+      batch.erase(std::find(batch.begin(), batch.end(), w.r));
+    }
+    svc.finished.notify_all();
+    svc.work.notify_all();
+  };
+  auto start = [&](const std::shared_ptr<request>& rp) {
+    ftle_work w = prepare_ftle(svc, c, rp);
+    if (engine_job(w.job))
+    {
+      const long long ticket = engine_submit(c, w.job);
+      in_engine.emplace(ticket, std::move(w));
+    }
+    else complete(w, per_seed_flow_map(c, w));
+  };
+  try
+  {
+    const std::vector<std::shared_ptr<request>> first(batch);
+    for (const auto& rp : first) start(rp);
+    while (engine_open(c) > 0)
+    {
+      {
+        phase_clock clock {svc, c, c.profile};
+        const auto finished = engine_advance(c, svc.horizon);
+        clock.mark("ftle.advect");
+        for (const auto& d : finished)
+        {
+          auto it = in_engine.find(d.first);
+          if (it == in_engine.end()) throw error(PARS_ERR_STATE, "the engine reported an unknown job");
+          complete(it->second, (long long)d.second);
+          in_engine.erase(it);
+        }
+      }
+      std::vector<std::shared_ptr<request>> joined;
+      {
+        std::lock_guard<std::mutex> lock(svc.mutex);
+        bool other_waiting = false;
+        for (const auto& q : svc.queue) other_waiting = other_waiting || q->kind != ftle;
+        if (!(other_waiting && svc.running_batches >= int(svc.lanes.size())))
+        {
+          for (auto it = svc.queue.begin(); it != svc.queue.end() && (int)batch.size() < svc.max_batch;)
+          {
+            request& r = **it;
+            if (r.kind == ftle && svc.in_use + r.estimate <= svc.budget)
+            {
+              svc.in_use += r.estimate;
+              reserved += r.estimate;
+              r.state = running;
+              r.started = clock_type::now();
+              batch.push_back(*it);
+              joined.push_back(*it);
+              it = svc.queue.erase(it);
+            }
+            else ++it;
+          }
+        }
+      }
+      served += joined.size();
+      for (const auto& rp : joined) start(rp);
+    }
+  }
+  catch (...)
+  {
+    // the table's jobs write into flow maps that are about to be freed
+    cudaStreamSynchronize(c.stream);
+    c.engine.reset();
+    for (auto& entry : in_engine) recycle_buffer(c, std::move(entry.second.flow));
+    throw;
+  }
+  return served;
 }
 
 // Streamline requests: one block per request in one tracing round loop, then
@@ -699,9 +818,11 @@ void worker(pars_gpu_service* svc, int lane)
     }
     bool ok = true;
     std::size_t store_bytes = 0;
+    std::size_t served = batch.size();
     try
     {
-      if (kind == ftle) run_ftle_batch(*svc, c, batch);
+      if (kind == ftle && svc->horizon > 0) served = run_ftle_continuous(*svc, c, batch, reserved);
+      else if (kind == ftle) run_ftle_batch(*svc, c, batch);
       else store_bytes = run_streamline_batch(*svc, c, batch, stage_mode);
     }
     catch (const error& e) { ok = false; for (auto& r : batch) fail(*r, e.status, e.what()); }
@@ -728,7 +849,7 @@ void worker(pars_gpu_service* svc, int lane)
       }
       auto& b = svc->profile_totals[kind == ftle ? "batches.ftle" : "batches.streamlines"];
       b.launches += 1;
-      b.milliseconds += double(batch.size());   // requests in these batches
+      b.milliseconds += double(served);   // requests in these batches
     }
     {
       std::lock_guard<std::mutex> lock(svc->mutex);
@@ -879,6 +1000,15 @@ int32_t pars_gpu_service_create(pars_gpu_service** service, int32_t device, int6
   for (int i = 0; i < lanes; ++i) svc->workers.emplace_back(worker, svc, i);
   *service = svc;
   return PARS_OK;
+}
+
+int32_t pars_gpu_service_set_horizon(pars_gpu_service* svc, int32_t iterations)
+{
+  return service_guard(svc, [&] {
+    PARS_REQUIRE(iterations >= 0, "iterations must be >= 0");
+    std::lock_guard<std::mutex> lock(svc->mutex);
+    svc->horizon = iterations;
+  });
 }
 
 int32_t pars_gpu_service_destroy(pars_gpu_service* svc)

@@ -55,6 +55,11 @@ class BatchJob(ctypes.Structure):
                 ("end_positions", ctypes.c_void_p), ("end_steps", ctypes.c_void_p), ("steps", ctypes.c_int64)]
 
 
+class EngineDone(ctypes.Structure):
+    """pars_gpu_engine_done (include/pars_gpu.h)."""
+    _fields_ = [("ticket", ctypes.c_int64), ("steps", ctypes.c_int64)]
+
+
 class SettingsSummary(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_char * 64), ("dataset_filepath", ctypes.c_char * 256),
                 ("particle_tracing_integrator", ctypes.c_char * 64), ("color_generation_mode", ctypes.c_char * 64),
@@ -124,10 +129,13 @@ SIGNATURES = {
     "pars_gpu_batch_advect": [_P, _P, _I32, _I32],
     "pars_gpu_batch_variants": [_P, ctypes.POINTER(_I32)],
     "pars_gpu_batch_tuned": [_P, _I32, ctypes.POINTER(_I32), ctypes.POINTER(_I32)],
+    "pars_gpu_engine_submit": [_P, ctypes.POINTER(BatchJob), ctypes.POINTER(_I64)],
+    "pars_gpu_engine_advance": [_P, _I32, ctypes.POINTER(EngineDone), _I32, ctypes.POINTER(_I32), ctypes.POINTER(_I64)],
     "pars_gpu_settings_decode": [_P, _I64, ctypes.POINTER(SettingsSummary)],
     "pars_gpu_settings_from_json": [ctypes.c_char_p, _I64, _P, _I64, ctypes.POINTER(_I64)],
     "pars_gpu_service_create": [ctypes.POINTER(_P), _I32, _I64, _I32, _I32],
     "pars_gpu_service_destroy": [_P],
+    "pars_gpu_service_set_horizon": [_P, _I32],
     "pars_gpu_service_add_dataset": [_P, ctypes.c_char_p, _P, _P, _P, _P, _P],
     "pars_gpu_service_add_dataset_device": [_P, ctypes.c_char_p, _P, _P, _P, _P, _P],
     "pars_gpu_service_submit": [_P, _P, _I64, ctypes.POINTER(_I64)],
@@ -458,6 +466,20 @@ class Context:
         self._call("pars_gpu_batch_advect", ctypes.cast(arr, ctypes.c_void_p), len(jobs), variant)
         return [arr[i].steps for i in range(len(jobs))]
 
+    def engine_submit(self, job):
+        """Appends a BatchJob to the continuous engine; returns its ticket."""
+        t = _I64()
+        self._call("pars_gpu_engine_submit", ctypes.byref(job), ctypes.byref(t))
+        return t.value
+
+    def engine_advance(self, iterations, capacity=1024):
+        """One horizon launch per job class with work; returns ([(ticket, steps)
+        of the jobs completed], jobs still open)."""
+        done = (EngineDone * max(1, capacity))()
+        n, left = _I32(), _I64()
+        self._call("pars_gpu_engine_advance", iterations, done, capacity, ctypes.byref(n), ctypes.byref(left))
+        return [(done[i].ticket, done[i].steps) for i in range(n.value)], left.value
+
     def batch_tuned(self, job_class):
         v, t = _I32(), _I32()
         self._call("pars_gpu_batch_tuned", job_class, ctypes.byref(v), ctypes.byref(t))
@@ -704,6 +726,11 @@ class Service:
             self.close()
         except Exception:
             pass
+
+    def set_horizon(self, iterations):
+        """Steps per warp of each continuous-engine launch for FTLE requests
+        (0: each FTLE batch in one launch)."""
+        self._check(self.lib.pars_gpu_service_set_horizon(self.handle, iterations), "pars_gpu_service_set_horizon")
 
     def add_dataset(self, name, field):
         self._check(self.lib.pars_gpu_service_add_dataset(self.handle, name.encode(), _ptr(field.xyz), _ptr(field.dims),

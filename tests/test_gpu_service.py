@@ -210,7 +210,7 @@ def test_profile_reports_kernels_and_phases(service):
     for t in tickets:
         assert service.wait(t) == 2
         service.release(t)
-    for name in ("trace_streamlines", "color_generate", "batch_advect", "ftle_fused",
+    for name in ("trace_streamlines", "color_generate", "batch_advect_horizon", "ftle_fused",
                  "streamlines.trace", "streamlines.index_color", "ftle.advect"):
         ms, count = service.profile_get(name)
         assert count >= 1 and ms > 0.0, name
@@ -289,3 +289,59 @@ def test_requests_admitted_mid_flight_equal_their_results_alone(service):
         alone = _result(service, t, kind)
         service.release(t)
         assert _same(alone, m, kind), r
+
+
+def test_ftle_requests_join_the_running_engine_and_leave_first():
+    """One lane, continuous engine with 64-step horizons: FTLE requests
+    submitted while a long FTLE request runs join its launch sequence and are
+    handed out before it completes (with run-to-completion batches on one
+    lane they would wait for it); each result equals the same request run as
+    a one-launch batch (horizon 0), bit for bit."""
+    import time
+    from pars_gb300 import native, workloads as W
+    from pars_gb300.requests import encode_settings
+    svc = native.Service(0, budget_bytes=8 << 30, lanes=1, max_batch=16)
+    try:
+        svc.add_dataset("abc40", W.abc_field(40, noise_sigma=0.01, seed=4))
+        svc.add_dataset("abc28", W.abc_field(28))
+        svc.set_horizon(64)
+        base = {"particle_tracing_integrator": "runge_kutta_4", "particle_tracing_step_size": 0.01}
+        long_request = dict(base, mode="ftle", dataset_filepath="abc40", seed_generation_stride=[1, 1, 1],
+                            seed_generation_iterations=20001, particle_tracing_step_size=0.001)
+        short = [dict(base, mode="ftle", dataset_filepath="abc28", seed_generation_stride=[2, 2, 2],
+                      seed_generation_iterations=201),
+                 dict(base, mode="ftle_reference", dataset_filepath="abc28", seed_generation_stride=[1, 1, 1],
+                      seed_generation_iterations=101),
+                 dict(base, mode="ftle_fractional_anisotropy", dataset_filepath="abc40",
+                      seed_generation_stride=[3, 3, 3], seed_generation_iterations=151),
+                 dict(base, mode="ftle", dataset_filepath="abc28", seed_generation_stride=[2, 2, 2],
+                      seed_generation_iterations=101, particle_tracing_integrator="runge_kutta_dormand_prince_5")]
+        t_long = svc.submit(encode_settings(long_request))
+        t_long_submitted = time.perf_counter()
+        for _ in range(200000):
+            if svc.wait(t_long, 0) != 0:
+                break
+            time.sleep(0.0005)
+        submitted, tickets = [], []
+        for r in short:
+            submitted.append(time.perf_counter())
+            tickets.append(svc.submit(encode_settings(r)))
+        for t in tickets + [t_long]:
+            assert svc.wait(t) == 2
+        long_end = t_long_submitted + svc.info(t_long).latency_ms / 1e3
+        ends = [s + svc.info(t).latency_ms / 1e3 for s, t in zip(submitted, tickets)]
+        print(f"\nlong request done at {long_end - t_long_submitted:.3f} s; short ones at "
+              + ", ".join(f"{e - t_long_submitted:.3f}" for e in ends))
+        assert all(e < long_end for e in ends), "a request waited for the long one"
+        joined = [svc.ftle(t) for t in tickets]
+        long_result = svc.ftle(t_long)
+        for t in tickets + [t_long]:
+            svc.release(t)
+        svc.set_horizon(0)
+        for r, got in zip(short + [long_request], joined + [long_result]):
+            t = svc.submit(encode_settings(r))
+            assert svc.wait(t) == 2
+            assert np.array_equal(svc.ftle(t), got, equal_nan=True), r["mode"]
+            svc.release(t)
+    finally:
+        svc.close()
