@@ -54,7 +54,7 @@ def parse_args():
     p.add_argument("--serve-arms", default="plain,batched,cpu", help="served workload: arms to run (plain, batched, cpu)")
     p.add_argument("--serve-cpu-seconds", type=float, default=15.0, help="served workload: CPU reference arm's sample length")
     p.add_argument("--serve-loads", default="0.5,0.9", help="served workload: offered loads as fractions of saturation")
-    p.add_argument("--serve-lanes", type=int, default=1, help="served workload: service lanes of the batched arm")
+    p.add_argument("--serve-lanes", type=int, default=2, help="served workload: service lanes of the batched arm")
     p.add_argument("--serve-reply", choices=["curves", "image"], default="image",
                    help="served workload: what a streamline request returns to the client -- the pars_service reply, "
                         "an image of the curves ray traced on the GPU (pipeline.cpp:264-337), or every curve buffer")
@@ -451,8 +451,10 @@ def run_serve(args):
               field from (pinned) host memory, seeds + trace + index + colour
               or flow map + FTLE, download every result buffer into pinned
               host buffers, release.
-    batched : the service (one lane by default, batches of up to 64, datasets
-              resident; the other lane count is timed at saturation beside it):
+    batched : the service (two lanes by default, batches of up to 64, datasets
+              resident, FTLE requests on the continuous engine; the other lane
+              count is timed at saturation beside it, and the batched arm also
+              runs at the plain path's 50 % offered load):
               requests are submitted as reference `settings` messages at their
               Poisson arrival times; a client thread collects each finished
               request's buffers into the same pinned host buffers.
@@ -686,6 +688,14 @@ def run_serve(args):
         svc = service(args.serve_lanes)
         results["batched"] = summarise(run_service, svc)
         results["batched"]["lanes"] = args.serve_lanes
+        if "plain" in results and "load50" in results["plain"]:
+            # latency at the plain path's own 50 % load: both arms at one offered rate
+            rate = results["plain"]["load50"]["offered_requests_per_s"]
+            span, lat, _ = run_service(svc, rate)
+            results["batched"]["at_plain_load50"] = {"offered_requests_per_s": rate,
+                                                     "achieved_requests_per_s": len(messages) / span,
+                                                     "p50_ms": float(np.percentile(lat, 50)),
+                                                     "p99_ms": float(np.percentile(lat, 99))}
         svc.close()
         # the other lane count, at saturation only
         other = 2 if args.serve_lanes == 1 else 1
