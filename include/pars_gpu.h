@@ -379,9 +379,11 @@ typedef struct pars_gpu_engine_done
  * returns its ticket.  The first job of a class tunes the class's launch shape
  * if the context has not tuned it yet. */
 int32_t pars_gpu_engine_submit (pars_gpu_context* context, const pars_gpu_batch_job* job, int64_t* ticket);
-/* One horizon launch per job class with work (iterations >= 1 steps per warp),
- * then returns up to `capacity` completed jobs (the rest on later calls) and,
- * in *open, the jobs submitted and not yet returned. */
+/* One horizon launch per job class with work (iterations >= 1 steps per warp;
+ * 0: the engine chooses the steps per launch for launches of about 2 ms from
+ * the class's last launch, 256 for its first), then returns up to `capacity`
+ * completed jobs (the rest on later calls) and, in *open, the jobs submitted
+ * and not yet returned. */
 int32_t pars_gpu_engine_advance(pars_gpu_context* context, int32_t iterations, pars_gpu_engine_done* done, int32_t capacity,
                                 int32_t* done_count, int64_t* open);
 
@@ -460,10 +462,10 @@ int32_t pars_gpu_service_create      (pars_gpu_service** service, int32_t device
 int32_t pars_gpu_service_destroy     (pars_gpu_service* service);
 /* FTLE requests run through the lane's continuous batched engine
  * (pars_gpu_engine_advance) with `iterations` steps per warp per launch
- * (default 1024): between launches finished requests are handed out and FTLE
- * requests that arrived meanwhile join the running launch sequence.  0 runs
- * each FTLE batch to completion in one launch instead.  Results are the same
- * bits either way. */
+ * (default -1: chosen by the engine for launches of about 2 ms): between
+ * launches finished requests are handed out and FTLE requests that arrived
+ * meanwhile join the running launch sequence.  0 runs each FTLE batch to
+ * completion in one launch instead.  Results are the same bits either way. */
 int32_t pars_gpu_service_set_horizon (pars_gpu_service* service, int32_t iterations);
 /* Registers a dataset (HOST xyz [X][Y][Z][3], as pars_gpu_field_upload) under `name`. */
 int32_t pars_gpu_service_add_dataset (pars_gpu_service* service, const char* name, const float* xyz, const int32_t shape[3],

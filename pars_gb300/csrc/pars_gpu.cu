@@ -972,17 +972,31 @@ struct batch_engine_class
   unsigned long long            handed = 0;      // pools handed out (at most total_pools)
   int                           variant = -1;
   long long                     open = 0;
+  // steps per launch chosen for a launch time (iterations = 0): the last
+  // launch's kernel time per step of its horizon, measured with CUDA events
+  double                        ms_per_iteration = 0.0;
+  int                           last_iterations = 0;
 };
 
 struct batch_engine
 {
   batch_engine_class classes[batch_classes];
   long long          next_ticket = 1;
+  cudaEvent_t        launch_start = nullptr, launch_stop = nullptr;
+  ~batch_engine()
+  {
+    if (launch_start) cudaEventDestroy(launch_start);
+    if (launch_stop) cudaEventDestroy(launch_stop);
+  }
   std::vector<std::pair<long long, unsigned long long>> ready;   // completions not yet returned (C ABI)
 };
 
 namespace
 {
+// Launch time the engine aims at when it chooses the steps per launch itself:
+// about the longest a job submitted meanwhile waits before it starts.
+constexpr double engine_launch_ms = 2.0;
+
 void engine_reserve(pars_gpu_context& ctx, batch_engine_class& E, int jobs)
 {
   if (jobs <= E.capacity) return;
@@ -1053,9 +1067,15 @@ long long engine_open(const pars_gpu_context& ctx)
 
 std::vector<std::pair<long long, unsigned long long>> engine_advance(pars_gpu_context& ctx, int iterations)
 {
-  PARS_REQUIRE(iterations >= 1, "iterations must be >= 1");
+  PARS_REQUIRE(iterations >= 0, "iterations must be >= 0");
   std::vector<std::pair<long long, unsigned long long>> done;
   if (!ctx.engine) return done;
+  batch_engine& engine = *ctx.engine;
+  if (!engine.launch_start)
+  {
+    PARS_CUDA(cudaEventCreate(&engine.launch_start));
+    PARS_CUDA(cudaEventCreate(&engine.launch_stop));
+  }
   for (int c = 0; c < batch_classes; ++c)
   {
     batch_engine_class& E = ctx.engine->classes[c];
@@ -1093,7 +1113,14 @@ std::vector<std::pair<long long, unsigned long long>> engine_advance(pars_gpu_co
       const unsigned long long start[4] = {E.handed, 0, 0, 0};
       PARS_CUDA(cudaMemcpyAsync(counters, start, sizeof(start), cudaMemcpyHostToDevice, ctx.stream));
       batch_horizon_args hz;
-      hz.iterations = iterations;
+      // iterations 0: steps per launch for a launch of engine_launch_ms, from
+      // the last launch's time per step (a first launch takes 256 steps)
+      int steps = iterations;
+      if (steps == 0)
+      {
+        steps = E.ms_per_iteration > 0.0 ? int(std::min(1.0e6, std::max(16.0, engine_launch_ms / E.ms_per_iteration))) : 256;
+      }
+      hz.iterations = steps;
       hz.in_count = int(E.parked);
       hz.in_groups = E.groups[E.parity].as<const batch_parked_group>();
       hz.in_lanes = E.lanes[E.parity].as<const batch_parked_lane>();
@@ -1102,15 +1129,26 @@ std::vector<std::pair<long long, unsigned long long>> engine_advance(pars_gpu_co
       hz.out_lanes = E.lanes[1 - E.parity].as<batch_parked_lane>();
       hz.out_count = reinterpret_cast<unsigned int*>(counters + 2);
       hz.stop = reinterpret_cast<unsigned int*>(counters + 3);
+      PARS_CUDA(cudaEventRecord(engine.launch_start, ctx.stream));
       launch_batch_advect_horizon(ctx, c, E.variant, E.table.as<const batch_job_device>(), n, E.total_pools, counters, hz,
                                   remaining + E.parked);
+      PARS_CUDA(cudaEventRecord(engine.launch_stop, ctx.stream));
       E.parity = 1 - E.parity;
+      E.last_iterations = steps;
     }
     std::vector<unsigned long long> host(4 + std::size_t(E.capacity));
     PARS_CUDA(cudaMemcpyAsync(host.data(), counters, sizeof(unsigned long long) * host.size(), cudaMemcpyDeviceToHost, ctx.stream));
     PARS_CUDA(cudaStreamSynchronize(ctx.stream));
     E.handed = std::min<unsigned long long>(host[0], (unsigned long long)E.total_pools);
     E.parked = (unsigned int)(host[2] & 0xffffffffu);
+    if (E.last_iterations > 0 && E.parked > 0)
+    {
+      // a launch that parked ran its full horizon: its time per step sets the next one's
+      float ms = 0.0f;
+      PARS_CUDA(cudaEventElapsedTime(&ms, engine.launch_start, engine.launch_stop));
+      E.ms_per_iteration = double(ms) / double(E.last_iterations);
+    }
+    E.last_iterations = 0;
     PARS_REQUIRE(E.parked <= (unsigned long long)E.group_capacity, "parked group count out of range");
     // No warp runs between launches: a job's particles are all retired once
     // all its pools are handed out and no parked group holds its particles,

@@ -177,8 +177,9 @@ struct pars_gpu_service
   int64_t                              next_ticket = 1;
   int                                  running_batches = 0;
   // FTLE requests: steps per warp of each continuous-engine launch (0: each
-  // batch runs to completion in one launch)
-  int                                  horizon = 1024;
+  // batch runs to completion in one launch; -1: the engine chooses them for
+  // launches of about 2 ms)
+  int                                  horizon = -1;
 };
 
 namespace pars
@@ -420,7 +421,7 @@ void run_ftle_batch(pars_gpu_service& svc, pars_gpu_context& c, std::vector<std:
 
 // FTLE requests through the context's continuous engine: each request's flow
 // map is a job of the engine's table, advanced one horizon launch (svc.horizon
-// steps per warp) at a time.  Between launches the requests whose flow maps
+// steps per warp, or as many as fill about 2 ms) at a time.  Between launches the requests whose flow maps
 // completed get their FTLE field and are handed to the client at once, and
 // FTLE requests that arrived meanwhile are admitted (within the budget and
 // max_batch in flight) and join the running table.  Admission pauses while
@@ -470,7 +471,7 @@ std::size_t run_ftle_continuous(pars_gpu_service& svc, pars_gpu_context& c, std:
     {
       {
         phase_clock clock {svc, c, c.profile};
-        const auto finished = engine_advance(c, svc.horizon);
+        const auto finished = engine_advance(c, std::max(0, svc.horizon));
         clock.mark("ftle.advect");
         for (const auto& d : finished)
         {
@@ -821,7 +822,7 @@ void worker(pars_gpu_service* svc, int lane)
     std::size_t served = batch.size();
     try
     {
-      if (kind == ftle && svc->horizon > 0) served = run_ftle_continuous(*svc, c, batch, reserved);
+      if (kind == ftle && svc->horizon != 0) served = run_ftle_continuous(*svc, c, batch, reserved);
       else if (kind == ftle) run_ftle_batch(*svc, c, batch);
       else store_bytes = run_streamline_batch(*svc, c, batch, stage_mode);
     }
@@ -1005,7 +1006,7 @@ int32_t pars_gpu_service_create(pars_gpu_service** service, int32_t device, int6
 int32_t pars_gpu_service_set_horizon(pars_gpu_service* svc, int32_t iterations)
 {
   return service_guard(svc, [&] {
-    PARS_REQUIRE(iterations >= 0, "iterations must be >= 0");
+    PARS_REQUIRE(iterations >= -1, "iterations must be >= -1");
     std::lock_guard<std::mutex> lock(svc->mutex);
     svc->horizon = iterations;
   });

@@ -473,8 +473,9 @@ class Context:
         return t.value
 
     def engine_advance(self, iterations, capacity=1024):
-        """One horizon launch per job class with work; returns ([(ticket, steps)
-        of the jobs completed], jobs still open)."""
+        """One horizon launch per job class with work (iterations 0: chosen by
+        the engine for launches of about 2 ms); returns ([(ticket, steps) of the
+        jobs completed], jobs still open)."""
         done = (EngineDone * max(1, capacity))()
         n, left = _I32(), _I64()
         self._call("pars_gpu_engine_advance", iterations, done, capacity, ctypes.byref(n), ctypes.byref(left))
@@ -729,7 +730,8 @@ class Service:
 
     def set_horizon(self, iterations):
         """Steps per warp of each continuous-engine launch for FTLE requests
-        (0: each FTLE batch in one launch)."""
+        (0: each FTLE batch in one launch; -1, the default: chosen by the engine
+        for launches of about 2 ms)."""
         self._check(self.lib.pars_gpu_service_set_horizon(self.handle, iterations), "pars_gpu_service_set_horizon")
 
     def add_dataset(self, name, field):
