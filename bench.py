@@ -21,6 +21,7 @@ scaling; value = all ranks' steps / max-over-ranks time.
 import argparse
 import json
 import os
+import platform
 import subprocess
 import sys
 import threading
@@ -177,6 +178,36 @@ def cpu_reference_run(field, iterations, stride, steps, warmup):
         total += s
     dt = time.perf_counter() - t0
     return total / dt, threads, dt
+
+
+def host_cpu():
+    """The host's CPU model and logical core count."""
+    model = platform.processor() or platform.machine()
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for line in fh:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+                if key == "cpu part" and model == platform.machine():
+                    model = f"{platform.machine()} (CPU part {line.split(':', 1)[1].strip()})"
+    except OSError:
+        pass
+    return {"cpu_model": model, "nproc": os.cpu_count()}
+
+
+def cpu_single_thread(field, iterations, stride):
+    """The same CPU leg on one thread, on every (16 stride)-th seed."""
+    import oracle
+    port = oracle.port()
+    threads = port.max_threads()
+    port.set_threads(1)
+    try:
+        value, _, _ = cpu_reference_run(field, iterations, stride * 16, 1, 0)
+    finally:
+        port.set_threads(threads)
+    return {"value": value, "sample": f"every {stride * 16}th seed in C order, one thread"}
 
 
 def cpu_sample_text(seeds, stride, n):
@@ -826,7 +857,8 @@ def main():
                           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
                           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                           "data": "synthetic", "config": config,
-                          "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+                          "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                                           **host_cpu()},
                           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
 
@@ -941,7 +973,8 @@ def main():
     if rank == 0 and world == 1:
         cpu_value, threads, _ = cpu_reference_run(field, args.iterations, args.cpu_stride, 1, 0)
         cpu = {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": cpu_sample_text(seeds, args.cpu_stride, n)}
+               "sample": cpu_sample_text(seeds, args.cpu_stride, n),
+               "single_thread": cpu_single_thread(field, args.iterations, args.cpu_stride), **host_cpu()}
 
     if rank == 0:
         l1 = peaks["l1_coalesced"]
