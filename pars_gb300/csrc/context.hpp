@@ -155,6 +155,7 @@ struct render_state
   render_state();
   // scene: one capsule per line index; prim_vertex[k] = its segment's start vertex
   long long     prims = 0;
+  long long     leaves = 0;                     // BVH leaves (runs of 1 or 2 consecutive segments)
   const float4* vertices = nullptr;
   const float4* colors = nullptr;               // nullptr: white
   float         radius = 1.0f;
@@ -164,7 +165,7 @@ struct render_state
   bool          tree_valid = false;
   bool          status_pending = false;         // the build's status word is not read yet
   device_buffer bounds, leaf_lo_unsorted, leaf_hi_unsorted, keys, values, leaf_lo, leaf_hi, leaf_vertex, nodes,
-                node_parent, leaf_parent, arrivals;
+                node_parent, leaf_parent, arrivals, leaf_flags, leaf_index, leaf_first, leaf_run;
   // volume: float [x][y][z] (volume_data: the tracer's own copy in `volume`,
   // or a buffer the caller keeps alive, such as a service dataset)
   bool          has_volume = false;

@@ -159,6 +159,19 @@ def test_many_segments(ctx, port):
     _assert_same(got, expected)
 
 
+def test_scene_of_segment_pairs(ctx, port):
+    """A scene above 2 M capsules, whose BVH leaves hold runs of two
+    consecutive segments of a curve (split at curve breaks and at even start
+    vertices): each segment's own box and capsule are still tested, so the
+    image equals the oracle's."""
+    f, batches = _curves(port, n=64, stride=2, iterations=102, color="rgb")
+    assert sum(len(i) for _, _, i in batches) > 2_300_000
+    cam = ((3.2, 3.0, 10.0), (-0.03, 0.02, -1.0), (0.0, 1.0, 0.0))
+    got = _render_gpu(ctx, batches, 0.01, cam, (128, 96), 2)
+    expected, _ = port.render(batches, 0.01, cam, (128, 96), frames=2)
+    _assert_same(got, expected)
+
+
 def test_service_renders_requests_that_ask_for_an_image(port):
     """Streamline requests with raytracing settings come back with the image
     ray_tracer::serialize would reply with (pipeline.cpp:264-337): each equals
