@@ -820,6 +820,21 @@ def extra_workloads(args):
     return out
 
 
+def served_summary(serve):
+    """The served stream's headline figures (batched service against the plain
+    single-request path), from the served workload's own line."""
+    if not serve or "batched" not in serve or "plain" not in serve:
+        return None
+    b, p = serve["batched"], serve["plain"]
+    return {"workload": serve.get("workload", "").split(":")[0], "reply": serve.get("reply"), "lanes": b.get("lanes"),
+            "req_per_s": b["saturation_requests_per_s"], "plain_req_per_s": p["saturation_requests_per_s"],
+            "ratio": b["saturation_requests_per_s"] / p["saturation_requests_per_s"],
+            "p50_ms": b.get("load50", {}).get("p50_ms"), "p99_ms": b.get("load50", {}).get("p99_ms"),
+            "plain_p50_ms": p.get("load50", {}).get("p50_ms"), "plain_p99_ms": p.get("load50", {}).get("p99_ms"),
+            "load": "50 % of each arm's own saturation throughput",
+            "at_plain_load50": b.get("at_plain_load50")}
+
+
 def main():
     args = parse_args()
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
@@ -1010,6 +1025,7 @@ def main():
     if rank == 0:
         if world == 1 and not args.no_extra:
             line["workloads"] = extra_workloads(args)
+            line["served"] = served_summary(line["workloads"].get("serve"))
         print(json.dumps(line))
 
 
