@@ -400,10 +400,12 @@ __device__ __forceinline__ void capsule_test(float3 o, float3 d, float4 a4, floa
 // The capsules of one leaf's run of consecutive segments.  In a run of more
 // than one, each segment's own padded box (the box its one-segment leaf would
 // have) is tested before its capsule, as the tree's bottom levels would.
+// RUNS false: every leaf is one segment (scenes below leaf_pairs_from).
+template <bool RUNS>
 __device__ __forceinline__ void leaf_test(const render_args& A, float3 o, float3 d, float3 inv, long long packed, hit_record& best)
 {
   const long long g = packed & leaf_vertex_mask;
-  const int count = int(packed >> 56) + 1;
+  const int count = RUNS ? int(packed >> 56) + 1 : 1;
   float4 a = A.vertices[g];
   if (count == 1) { capsule_test(o, d, a, A.vertices[g + 1], A.radius, g, best); return; }
   const float pad = A.radius + (A.radius + key_float(A.bounds[6])) * (1.0f / 65536.0f);
@@ -418,6 +420,7 @@ __device__ __forceinline__ void leaf_test(const render_args& A, float3 o, float3
   }
 }
 
+template <bool RUNS>
 __device__ hit_record closest_hit(const render_args& A, float3 o, float3 d, float3 inv)
 {
   hit_record best {INFINITY, LLONG_MAX, -1};
@@ -426,7 +429,7 @@ __device__ hit_record closest_hit(const render_args& A, float3 o, float3 d, floa
   {
     float tn;
     const float4 lo = A.leaf_lo[0], hi = A.leaf_hi[0];
-    if (box_hit(o, inv, lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, INFINITY, tn)) leaf_test(A, o, d, inv, A.leaf_vertex[0], best);
+    if (box_hit(o, inv, lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, INFINITY, tn)) leaf_test<RUNS>(A, o, d, inv, A.leaf_vertex[0], best);
     return best;
   }
   int stack[stack_depth];
@@ -447,12 +450,12 @@ __device__ hit_record closest_hit(const render_args& A, float3 o, float3 d, floa
     // leaves are tested at once; internal children are visited nearest first
     if (hl)
     {
-      if (nd.x < 0) leaf_test(A, o, d, inv, A.leaf_vertex[~nd.x], best);
+      if (nd.x < 0) leaf_test<RUNS>(A, o, d, inv, A.leaf_vertex[~nd.x], best);
       else next[count++] = nd.x;
     }
     if (hr)
     {
-      if (nd.y < 0) leaf_test(A, o, d, inv, A.leaf_vertex[~nd.y], best);
+      if (nd.y < 0) leaf_test<RUNS>(A, o, d, inv, A.leaf_vertex[~nd.y], best);
       else next[count++] = nd.y;
     }
     if (count == 2)
@@ -532,6 +535,7 @@ __device__ float3 shade(const render_args& A, float3 o, float3 d, const hit_reco
   return out;
 }
 
+template <bool RUNS>
 __global__ void __launch_bounds__(render_tile * render_tile) render_kernel(render_args A)
 {
   const int px = blockIdx.x * render_tile + threadIdx.x, py = blockIdx.y * render_tile + threadIdx.y;
@@ -548,7 +552,7 @@ __global__ void __launch_bounds__(render_tile * render_tile) render_kernel(rende
     const float3 d = normalize3(r);
     const float3 inv = make_float3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     const float3 o = A.origin;
-    const hit_record h = closest_hit(A, o, d, inv);
+    const hit_record h = closest_hit<RUNS>(A, o, d, inv);
     float cr = 0.0f, cg = 0.0f, cb = 0.0f, alpha = 0.0f;
     if (A.volume)
     {
@@ -887,7 +891,8 @@ void render_frames(pars_gpu_context& ctx, render_state& r, int iterations)
   const dim3 grid((r.width + render_tile - 1) / render_tile, (r.height + render_tile - 1) / render_tile);
   {
     launch_scope scope(ctx, "render");
-    render_kernel<<<grid, block, 0, ctx.stream>>>(A);
+    if (r.leaves < r.prims) render_kernel<true><<<grid, block, 0, ctx.stream>>>(A);
+    else render_kernel<false><<<grid, block, 0, ctx.stream>>>(A);
   }
   PARS_CUDA(cudaGetLastError());
   int status = 0;
