@@ -346,8 +346,9 @@ typedef struct pars_gpu_batch_job
 /* Advects every job in one persistent launch that drains a device queue of
  * seed chunks.  variant selects the launch shape (threads per CTA, register
  * budget) among pars_gpu_batch_variants(); -1 = autotuned: the first call of
- * each job class (steady / unsteady) times every variant on a probe of the
- * batch and keeps the fastest for the context.  Each class (re-sampled
+ * each job class (steady / unsteady / frozen) on a device times every variant on
+ * a probe of the batch and keeps the fastest for every context of that device in
+ * the process.  Each class (re-sampled
  * steady, re-sampled unsteady, frozen) runs in its own launch. */
 int32_t pars_gpu_batch_advect  (pars_gpu_context* context, pars_gpu_batch_job* jobs, int32_t count, int32_t variant);
 int32_t pars_gpu_batch_variants(pars_gpu_context* context, int32_t* count);

@@ -7,6 +7,8 @@
 // out-of-bounds exchange (:376-393) — here a device exit queue sorted by
 // destination block, so the next round's particles never leave the GPU.
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <utility>
 #include <cstring>
 #include <limits>
@@ -801,10 +803,21 @@ long long pools_of(long long seeds)
 // Chooses the launch shape of job class c from `jobs` (all of class c, clocks
 // set): every shape runs a probe of the jobs twice (seed counts capped at four
 // times the seeds the GPU holds resident), timed with CUDA events.
+// Tuned launch shapes of the process's contexts, per device and job class: a
+// context whose class is untuned takes the shape another context of the same
+// device chose (the service's lanes are contexts of one device).
+std::mutex tuned_mutex;
+std::map<std::pair<int, int>, int> tuned_shapes;
+
 void tune_class(pars_gpu_context& ctx, int c, std::vector<batch_job_device> jobs)
 {
   const int count = int(jobs.size());
   if (count == 0) return;
+  {
+    std::lock_guard<std::mutex> lock(tuned_mutex);
+    const auto it = tuned_shapes.find({ctx.device, c});
+    if (it != tuned_shapes.end()) { ctx.batch_variant[c] = it->second; return; }
+  }
   ctx.batch_jobs.reserve(sizeof(batch_job_device) * count);
   ctx.batch_counters.reserve(sizeof(unsigned long long) * (count + 1));
   auto* counters = ctx.batch_counters.as<unsigned long long>();
@@ -855,6 +868,8 @@ void tune_class(pars_gpu_context& ctx, int c, std::vector<batch_job_device> jobs
     if (warps > best_warps || (warps == best_warps && fastest[v] < fastest[best_v])) { best_v = v; best_warps = warps; }
   }
   ctx.batch_variant[c] = best_v;
+  std::lock_guard<std::mutex> lock(tuned_mutex);
+  tuned_shapes.emplace(std::make_pair(ctx.device, c), best_v);
 }
 
 // Runs batched jobs and returns each job's steps.  Re-sampled jobs on steady
