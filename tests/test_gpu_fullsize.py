@@ -16,6 +16,10 @@
   reference's frozen scheme, bit-exact per (block, round) batch against the
   oracle's round-by-round restatement of particle_tracer::trace with the
   block exchange (particle_tracer.cpp:253-409).
+* Batched pathlines (32 unsteady double gyres, edge 32-256, 16-64 slices,
+  2.9 M seeds, seed 3; RK4 in space-time, h = 0.01, 1000 steps): all 32 jobs
+  in one launch, step totals consistent, six fields' strided seeds within
+  1e-3 cells of the FP64 unsteady oracle.
 """
 import numpy as np
 import pytest
@@ -169,3 +173,60 @@ def test_partitioned_domain_512_frozen_matches_oracle(ctx, port):
     assert s["rounds"] > 1
     assert s["steps"] == expected.steps
     compare(got, expected.batches)
+
+
+def test_pathline_workload_all_32_fields_in_one_launch(ctx, port):
+    """The batched-pathline workload as the benchmark runs it: 32 unsteady
+    double gyres (edge 32-256 log-uniform, 16-64 slices, 2.9 M seeds, seed 3)
+    in one launch, RK4 in space-time, h = 0.01, 1000 steps.  Every job's step
+    total equals the sum of its per-seed counts; on up to six of the fields of
+    edge <= 96 (their slices copied to the host), 400 strided seeds each
+    against the FP64 unsteady oracle: more than 99 % with the oracle's step
+    count, and those within 1e-3 cells."""
+    import torch
+    from pars_gb300 import native, workloads as W
+    specs = W.pathline_batch_config(seed=3)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(3)
+    jobs, keep, handles = [], [], []
+    for spec in specs:
+        n, slices, c = spec["edge"], spec["slices"], spec["seeds"]
+        xyz, offset, spacing, t0, dt = W.double_gyre_device(torch, n, slices)
+        h = ctx.upload_unsteady_field_device(xyz.data_ptr(), (n, n, n), slices, offset,
+                                             np.array([n, n, n], np.float32) * spacing, spacing, t0, dt)
+        handles.append(h)
+        host = xyz.cpu().numpy() if n <= 96 and sum(k[1] is not None for k in keep) < 6 else None
+        del xyz
+        seeds = torch.zeros((c, 4), dtype=torch.float32, device="cuda")
+        seeds[:, 0] = 0.05 + 1.9 * torch.rand(c, device="cuda", generator=gen)
+        seeds[:, 1] = 0.05 + 0.9 * torch.rand(c, device="cuda", generator=gen)
+        seeds[:, 2] = 0.05 + 0.9 * torch.rand(c, device="cuda", generator=gen)
+        end = torch.empty((c, 4), dtype=torch.float32, device="cuda")
+        steps = torch.empty(c, dtype=torch.int32, device="cuda")
+        j = native.BatchJob()
+        j.field, j.integrator, j.stage_mode, j.max_steps, j.step_size = h, native.RUNGE_KUTTA_4, native.STAGES_RESAMPLED, 1000, 0.01
+        j.time_begin, j.seeds, j.seed_count = 0.0, seeds.data_ptr(), c
+        j.end_positions, j.end_steps = end.data_ptr(), steps.data_ptr()
+        jobs.append(j)
+        keep.append((spec, host, offset, spacing, t0, dt, seeds, end, steps))
+    torch.cuda.empty_cache()
+    totals = ctx.batch_advect(jobs)
+    checked = 0
+    for (spec, host, offset, spacing, t0, dt, seeds, end, steps), total in zip(keep, totals):
+        assert int(steps.sum(dtype=torch.int64).item()) == total
+        if host is None:
+            continue
+        idx = np.linspace(0, spec["seeds"] - 1, 400).astype(np.int64)
+        s = seeds.cpu().numpy()[idx, :3]
+        e64, s64 = port.advect_unsteady_fp64(host, offset, spacing, t0, dt, s, 0.0, 0.01, 1000)
+        got_steps = steps.cpu().numpy()[idx]
+        got = end.cpu().numpy()[idx, :3].astype(np.float64)
+        same = got_steps == s64
+        assert same.mean() > 0.99, (spec, same.mean())
+        err = np.linalg.norm(got[same] - e64[same], axis=1) / float(spacing.min())
+        assert err.max() <= 1e-3, (spec, err.max())
+        checked += 1
+    print(f"\n{len(specs)} fields, {sum(s['seeds'] for s in specs)} seeds, {sum(totals)} steps; {checked} fields checked against FP64")
+    assert checked >= 4
+    for h in handles:
+        ctx.release_field(h)
