@@ -17,7 +17,11 @@
  *
  * Threading: calls on one context are serialised by the context; separate
  * contexts are independent.  Work is issued on the context's CUDA stream
- * (its own, or one set with pars_gpu_set_stream).
+ * (its own, or one set with pars_gpu_set_stream).  On its own stream a call's
+ * work starts after the work already submitted to the legacy default stream;
+ * callers that produce device inputs on another stream synchronise it first
+ * or pass it with pars_gpu_set_stream.  Uploads return once their copy is
+ * done, so the caller's buffer may be reused at once.
  */
 #ifndef PARS_GPU_H
 #define PARS_GPU_H

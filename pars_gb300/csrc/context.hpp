@@ -258,6 +258,7 @@ struct pars_gpu_context
   std::map<std::string, pars::profile_entry> profile_totals;
   std::vector<pars::timed_launch>         pending;
   std::vector<cudaEvent_t>                event_pool;
+  cudaEvent_t                             legacy_event = nullptr;   // orders the own stream after the legacy default stream
   long long                               launches = 0;
   long long                               held_bytes() const;
 };

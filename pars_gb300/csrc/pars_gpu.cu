@@ -168,6 +168,15 @@ int32_t guarded(pars_gpu_context* ctx, body_type&& body)
   try
   {
     PARS_CUDA(cudaSetDevice(ctx->device));
+    if (ctx->stream == ctx->own_stream)
+    {
+      // The context's own stream does not synchronise with the legacy default
+      // stream, where a caller's device inputs are usually produced: the
+      // call's work starts after the work already submitted there.
+      if (!ctx->legacy_event) PARS_CUDA(cudaEventCreateWithFlags(&ctx->legacy_event, cudaEventDisableTiming));
+      PARS_CUDA(cudaEventRecord(ctx->legacy_event, cudaStreamLegacy));
+      PARS_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->legacy_event, 0));
+    }
     body();
     if (ctx->pending.size() > 4096) flush_profile(*ctx);
     ctx->last_error.clear();
@@ -1279,6 +1288,7 @@ int32_t pars_gpu_destroy(pars_gpu_context* ctx)
     cudaStreamSynchronize(ctx->stream);
     for (auto& p : ctx->pending) { cudaEventDestroy(p.start); cudaEventDestroy(p.stop); }
     for (auto e : ctx->event_pool) cudaEventDestroy(e);
+    if (ctx->legacy_event) cudaEventDestroy(ctx->legacy_event);
     ctx->pending.clear();
     ctx->event_pool.clear();
     ctx->fields.clear();
@@ -1325,6 +1335,8 @@ int32_t pars_gpu_field_upload(pars_gpu_context* ctx, const float* xyz, const int
     entry->data = acquire_buffer(*ctx, sizeof(float4) * count);
     PARS_CUDA(cudaMemcpyAsync(ctx->staging.get(), xyz, sizeof(float) * 3 * count, cudaMemcpyHostToDevice, ctx->stream));
     launch_pack_field(*ctx, ctx->staging.as<const float>(), entry->data.as<float4>(), count);
+    // the caller may reuse or free its buffer once the call returns
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
     *field = add_field(*ctx, std::move(entry));
   });
 }
@@ -1339,6 +1351,8 @@ int32_t pars_gpu_field_upload_device(pars_gpu_context* ctx, const float* device_
     const long long count = (long long)shape[0] * shape[1] * shape[2];
     entry->data = acquire_buffer(*ctx, sizeof(float4) * count);
     launch_pack_field(*ctx, device_xyz, entry->data.as<float4>(), count);
+    // the caller may reuse or free its buffer once the call returns
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
     *field = add_field(*ctx, std::move(entry));
   });
 }
@@ -1358,6 +1372,8 @@ int32_t pars_gpu_unsteady_field_upload(pars_gpu_context* ctx, const float* xyz, 
     entry->data = acquire_buffer(*ctx, sizeof(float4) * count);
     PARS_CUDA(cudaMemcpyAsync(ctx->staging.get(), xyz, sizeof(float) * 3 * count, cudaMemcpyHostToDevice, ctx->stream));
     launch_pack_field(*ctx, ctx->staging.as<const float>(), entry->data.as<float4>(), count);
+    // the caller may reuse or free its buffer once the call returns
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
     *field = add_field(*ctx, std::move(entry));
   });
 }
@@ -1375,6 +1391,8 @@ int32_t pars_gpu_unsteady_field_upload_device(pars_gpu_context* ctx, const float
     const long long count = (long long)shape[0] * shape[1] * shape[2] * slices;
     entry->data = acquire_buffer(*ctx, sizeof(float4) * count);
     launch_pack_field(*ctx, device_xyz, entry->data.as<float4>(), count);
+    // the caller may reuse or free its buffer once the call returns
+    PARS_CUDA(cudaStreamSynchronize(ctx->stream));
     *field = add_field(*ctx, std::move(entry));
   });
 }

@@ -211,6 +211,13 @@ def test_pathline_workload_all_32_fields_in_one_launch(ctx, port):
         keep.append((spec, host, offset, spacing, t0, dt, seeds, end, steps))
     torch.cuda.empty_cache()
     totals = ctx.batch_advect(jobs)
+    first = [(end.clone(), steps.clone()) for *_, end, steps in keep]
+    # a second run gives the same bits (inputs made on the caller's stream are
+    # complete before the context reads them)
+    assert ctx.batch_advect(jobs) == totals
+    for (e, st), (*_, end, steps) in zip(first, keep):
+        assert torch.equal(e, end) and torch.equal(st, steps)
+    del first
     checked = 0
     for (spec, host, offset, spacing, t0, dt, seeds, end, steps), total in zip(keep, totals):
         assert int(steps.sum(dtype=torch.int64).item()) == total
