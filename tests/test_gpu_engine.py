@@ -161,3 +161,67 @@ def test_engine_edge_cases(ctx):
     rest, left = ctx.engine_advance(16, capacity=2)
     assert [d[0] for d in rest] == tickets[2:] and left == 0
     ctx.release_field(h)
+
+
+def test_engine_table_grows_while_jobs_are_parked(ctx):
+    """200 small jobs of all three classes (120 re-sampled steady, 40
+    unsteady, 40 frozen), submitted in waves of 40 between 16-step launches,
+    so that the steady table grows past its first 64 slots while earlier jobs
+    are parked: the counters move with the table and every job equals the
+    one-launch engine."""
+    import torch
+    from pars_gb300 import native, workloads as W
+    rng = np.random.default_rng(21)
+    steady = W.abc_field(24, noise_sigma=0.01, seed=7)
+    hs = ctx.upload_field(steady)
+    hu = _gyre_fields(ctx, [(20, 9)])[0][0]
+    specs = []
+    for k in range(200):
+        kind = {3: 1, 4: 2}.get(k % 5, 0)
+        c = int(rng.integers(50, 400))
+        if kind == 1:
+            seeds = _seeds(rng, c, 0)
+        else:
+            seeds = np.concatenate([rng.uniform(0.2, 6.0, (c, 3)), np.zeros((c, 1))], 1).astype(np.float32)
+        specs.append((kind, torch.from_numpy(seeds).cuda(), c))
+
+    def job(kind, sd, c):
+        ed = torch.zeros((c, 4), dtype=torch.float32, device="cuda")
+        st = torch.zeros(c, dtype=torch.int32, device="cuda")
+        j = _job(native, hu if kind == 1 else hs, sd, c, ed, st, 200, 0.01)
+        if kind == 2:
+            j.stage_mode = native.STAGES_FROZEN
+            j.integrator = native.INTEGRATORS["adams_bashforth_2"]
+        return j, ed, st
+
+    alone = []
+    for kind, sd, c in specs:
+        j, ed, st = job(kind, sd, c)
+        n = ctx.batch_advect([j])[0]
+        alone.append((ed.cpu().numpy(), st.cpu().numpy(), n))
+    made = [job(kind, sd, c) for kind, sd, c in specs]
+    tickets, got = {}, {}
+    open_before_growth = None
+    for wave in range(5):
+        for k in range(40 * wave, 40 * wave + 40):
+            tickets[ctx.engine_submit(made[k][0])] = k
+        done, left = ctx.engine_advance(16)
+        for t, s in done:
+            got[tickets[t]] = s
+        if wave == 1:
+            open_before_growth = left
+    assert open_before_growth >= 64      # the third wave's steady jobs grow a table that still runs
+    for _ in range(100000):
+        done, left = ctx.engine_advance(16)
+        for t, s in done:
+            got[tickets[t]] = s
+        if left == 0:
+            break
+    assert len(got) == len(specs)
+    for k, (j, ed, st) in enumerate(made):
+        e, s, n = alone[k]
+        assert got[k] == n, k
+        assert np.array_equal(st.cpu().numpy(), s), k
+        assert np.array_equal(ed.cpu().numpy(), e), k
+    ctx.release_field(hs)
+    ctx.release_field(hu)
