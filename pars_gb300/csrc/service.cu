@@ -449,7 +449,8 @@ std::size_t run_ftle_continuous(pars_gpu_service& svc, pars_gpu_context& c, std:
       if (r.result) { svc.in_use += r.result_bytes; svc.held += r.result_bytes; }
       r.state = done;
       r.finished = clock_type::now();
-      batch.erase(std::find(batch.begin(), batch.end(), w.r));
+      const auto it = std::find(batch.begin(), batch.end(), w.r);
+      if (it != batch.end()) batch.erase(it);
     }
     svc.finished.notify_all();
     svc.work.notify_all();
