@@ -68,3 +68,24 @@ def test_bench_launches_one_process_per_gpu():
     assert line["launcher_check"] is True
     assert line["n_gpus"] == 2 and line["requested_gpus"] == 2
     assert line["max_rank_seconds"] == 2.0 and line["sum_units"] == 3000.0
+
+
+def test_served_summary_and_host_cpu():
+    """The bench line's served-stream summary is taken from the served
+    workload's own line (batched service against the plain path), and the CPU
+    baseline names the host's CPU and core count."""
+    sys.path.insert(0, ROOT)
+    import bench
+    serve = {"workload": "served_100: ...", "reply": "image",
+             "plain": {"saturation_requests_per_s": 100.0, "load50": {"p50_ms": 12.0, "p99_ms": 40.0}},
+             "batched": {"saturation_requests_per_s": 250.0, "lanes": 2, "load50": {"p50_ms": 10.0, "p99_ms": 30.0},
+                         "at_plain_load50": {"p50_ms": 8.0, "p99_ms": 25.0}}}
+    s = bench.served_summary(serve)
+    assert s["workload"] == "served_100" and s["lanes"] == 2
+    assert s["req_per_s"] == 250.0 and s["plain_req_per_s"] == 100.0 and s["ratio"] == 2.5
+    assert (s["p50_ms"], s["p99_ms"], s["plain_p50_ms"], s["plain_p99_ms"]) == (10.0, 30.0, 12.0, 40.0)
+    assert s["at_plain_load50"]["p50_ms"] == 8.0
+    assert bench.served_summary(None) is None
+    assert bench.served_summary({"error": "failed"}) is None
+    cpu = bench.host_cpu()
+    assert cpu["nproc"] == os.cpu_count() and isinstance(cpu["cpu_model"], str) and cpu["cpu_model"]
