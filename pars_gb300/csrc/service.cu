@@ -26,6 +26,7 @@
 // traced (pipeline.cpp:264-337): its image is rendered on the lane right after
 // its batch and kept in host memory with the request.
 #include <algorithm>
+#include <atomic>
 #include <array>
 #include <chrono>
 #include <cstdio>
@@ -179,7 +180,7 @@ struct pars_gpu_service
   // FTLE requests: steps per warp of each continuous-engine launch (0: each
   // batch runs to completion in one launch; -1: the engine chooses them for
   // launches of about 2 ms)
-  int                                  horizon = -1;
+  std::atomic<int>                     horizon {-1};
 };
 
 namespace pars
@@ -472,7 +473,7 @@ std::size_t run_ftle_continuous(pars_gpu_service& svc, pars_gpu_context& c, std:
     {
       {
         phase_clock clock {svc, c, c.profile};
-        const auto finished = engine_advance(c, std::max(0, svc.horizon));
+        const auto finished = engine_advance(c, std::max(0, svc.horizon.load()));
         clock.mark("ftle.advect");
         for (const auto& d : finished)
         {
@@ -823,7 +824,7 @@ void worker(pars_gpu_service* svc, int lane)
     std::size_t served = batch.size();
     try
     {
-      if (kind == ftle && svc->horizon != 0) served = run_ftle_continuous(*svc, c, batch, reserved);
+      if (kind == ftle && svc->horizon.load() != 0) served = run_ftle_continuous(*svc, c, batch, reserved);
       else if (kind == ftle) run_ftle_batch(*svc, c, batch);
       else store_bytes = run_streamline_batch(*svc, c, batch, stage_mode);
     }
@@ -1008,8 +1009,7 @@ int32_t pars_gpu_service_set_horizon(pars_gpu_service* svc, int32_t iterations)
 {
   return service_guard(svc, [&] {
     PARS_REQUIRE(iterations >= -1, "iterations must be >= -1");
-    std::lock_guard<std::mutex> lock(svc->mutex);
-    svc->horizon = iterations;
+    svc->horizon.store(iterations);
   });
 }
 
