@@ -216,8 +216,9 @@ __device__ __forceinline__ bool sample_inside_cached(const field_view& f, corner
 }
 
 // lerp_fast on a pair of components with the packed FP32x2 instructions
-// (FADD2 / FFMA2, round-to-nearest per component): the same two roundings per
-// component as lerp_fast, so each component is bit-identical to it.
+// (FADD2 / FFMA2, round-to-nearest per component): the difference feeds an
+// explicit FMA, so nothing can be folded into it, and each component is
+// bit-identical to lerp_fast (the 256^3 flow map's end points were).
 __device__ __forceinline__ float2 lerp_fast2(float2 a, float2 b, float2 w)
 {
   return __ffma2_rn(w, __fadd2_rn(b, make_float2(-a.x, -a.y)), a);
@@ -357,9 +358,14 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
 // left is that of the (tiny) compensation term itself.  A plain FP32 sum and
 // product lose about two ulps of the increment per step, which the flow's
 // stretching amplifies: on the 256^3 ABC workload this halves the largest
-// end-point errors against an FP64 integration.  Every operation is an
-// explicit round-to-nearest one (no contraction), so the scalar form below
-// and the packed pair form (rk4_update2) give the same bits per component.
+// end-point errors against an FP64 integration.  Every operation of this
+// scalar form is an explicit round-to-nearest one, never contracted.  The
+// packed pair form (rk4_update2) is not contraction-proof: the compiler folds
+// a packed product into the packed sum that consumes it (a sum of two packed
+// products differed from two roundings in 43 % of random cases, with the
+// intrinsics, with explicit-rounding PTX and with --fmad=false alike), so its
+// x and y can differ from this form in the last bits; both meet the
+// end-point bar against FP64.
 __device__ __forceinline__ void rk4_update(float& u, float& l, float h6, float k1, float k2, float k3, float k4)
 {
   float a, ea, b, eb, t, et;
@@ -374,10 +380,11 @@ __device__ __forceinline__ void rk4_update(float& u, float& l, float h6, float k
 
 // ---- Packed pairs (FP32x2) ----------------------------------------------------
 // The x and y components of the re-sampled RK4 step go through the packed
-// FP32x2 instructions (FADD2 / FMUL2 / FFMA2: two independent round-to-nearest
-// operations in one instruction), z through the scalar forms above.  Each
-// packed operation rounds exactly like its scalar counterpart, so every
-// component gets the bits of the scalar code.
+// FP32x2 instructions (FADD2 / FMUL2 / FFMA2: two round-to-nearest operations
+// in one instruction), z through the scalar forms above.  A packed product
+// that feeds a packed sum may be folded into one FFMA2 (see rk4_update), so
+// these forms are not bit-identical to the scalar ones; the frozen scheme,
+// which must give the reference's bits, stays scalar.
 __device__ __forceinline__ float2 pair(float v) { return make_float2(v, v); }
 
 // a - b as FMA(b, -1, a): one rounding, one instruction.
